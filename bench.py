@@ -1,0 +1,346 @@
+"""Benchmark: peptide-spectrum XCorrs/s of the SEQUEST search hot path.
+
+One step = one full search (stages a-e) of one batch of synthetic spectra
+against the synthetic database: the 'full' configuration (20,000 random
+proteins, 10,000 spectra at charge 1-4, 50-400 peaks, +-3 Da, 1.0005 Da bins,
+top-10).  `value` times steps whose inputs are already resident in HBM
+(hfx_search_device); `e2e` times the same search through hfx_search_host
+with pinned host buffers, copies included.  Between timed steps the L2 is
+flushed by writing a 512 MB buffer (outside the timed events).
+
+--impl reference times the reference's search restated on the CPU (the
+oracle port: the reference's Haskell host and CUDA kernels cannot run on
+this machine) on the same workload, with every host thread.
+
+Multi-GPU: spectra are independent, so each rank searches its own batch
+(weak scaling, no collective on the data path); value = all ranks' pairs /
+max over ranks of the elapsed time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "peptide-spectrum XCorrs/s"
+UNIT = "PSM/s"
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="full")
+    ap.add_argument("--spectra", type=int, default=0, help="override the number of spectra")
+    ap.add_argument("--precision", type=int, default=-1, help="0 fp32, 1 bf16+rescore, 2 fp16+rescore")
+    ap.add_argument("--batch-mode", type=int, default=-1, help="0 per-spectrum launches, 1 batched")
+    ap.add_argument("--cpu-sample", type=int, default=2000, help="spectra in the CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--out", default="")
+    return ap.parse_args()
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def _workload(name, n, rank):
+    from hfx_gb300 import synth
+    prot, sp, cfg = synth.workload(name, n_spectra=n or None)
+    if rank:
+        # each rank its own batch of spectra over the same database
+        peps = synth.tryptic_peptides(prot)
+        sp = synth.spectra(prot, len(sp), seed=1000 + rank, charge_p={1: 0.05, 2: 0.5, 3: 0.35, 4: 0.10},
+                           npeaks=(50, 400), peps=peps)
+    return prot, sp, cfg
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        if not sm:
+            return None
+        load = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _bytes_per_psm(eng, rows_dtype_bytes, wb, we, lens, charges, idx_tc_tn, rng, n=4000):
+    """Algorithmic bytes per pair: U*s + L + 16 (U = distinct in-range ion
+    bins, s = stored element size, L = residue bytes, 16 = r, tc, tn, id),
+    averaged over a random sample of the pairs the step scores."""
+    import torch
+    counts = (we - wb).astype(np.int64)
+    ok = np.nonzero(counts > 0)[0]
+    sp = rng.choice(ok, n, p=counts[ok] / counts[ok].sum())
+    pos = (wb[sp] + (rng.random(n) * counts[sp]).astype(np.int64)).astype(np.int32)
+    d = torch.device("cuda")
+    cap = 8192
+    bins = torch.zeros((n, cap), dtype=torch.int32, device=d)
+    lvl = torch.zeros((n, cap), dtype=torch.uint8, device=d)
+    cnt = torch.zeros(n, dtype=torch.int32, device=d)
+    eng.ion_bins(torch.from_numpy(pos).to(d), torch.from_numpy(charges[sp].astype(np.int32)).to(d),
+                 torch.from_numpy(lens[sp].astype(np.int32)).to(d), cap, bins, lvl, cnt)
+    U = cnt.cpu().numpy().astype(np.float64)
+    tc, tn = idx_tc_tn
+    L = (tn[pos] - tc[pos]).astype(np.float64)
+    return float(np.mean(U * rows_dtype_bytes + L + 16)), float(U.mean())
+
+
+def run_reference(a, rank, world):
+    """CPU arm: the oracle port of the reference search, all host threads."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from hfx_gb300 import synth
+    O.build()
+    prot, sp, cfg = _workload(a.workload, a.spectra, 0)
+    mt = O.mass_table(True, synth.static_mods())
+    d = {k: v for k, v in synth.DIGEST.items() if k != "mono"}
+    r, tc, tn = O.digest(prot.seq, prot.seg, mt, **d)
+    idx = O.sort_idx(r)
+    ions = O.pack_ions(prot.seq)
+    sample = sp.subset(np.arange(min(len(sp), max(50, a.cpu_sample // 4))))
+    threads = os.cpu_count() or 1
+    for _ in range(max(1, min(a.warmup, 1))):
+        O.search(ions, mt, r, tc, tn, idx, sample.subset(np.arange(min(20, len(sample)))), topn=cfg["top_n"],
+                 nthreads=threads)
+    t0 = time.perf_counter()
+    psm = 0
+    for _ in range(a.steps):
+        res = O.search(ions, mt, r, tc, tn, idx, sample, topn=cfg["top_n"], nthreads=threads)
+        psm += int(res[4].sum())
+    dt = time.perf_counter() - t0
+    v = psm / dt
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": 1000 * dt / a.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": a.workload + f" ({len(sample)} of {len(sp)} spectra per step)"},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{len(sample)} spectra of the {a.workload} workload per step"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = _args()
+    rank, world, local = _dist()
+    if a.impl == "reference":
+        return run_reference(a, rank, world)
+    import torch
+    import hfx_gb300
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    prot, sp, cfg = _workload(a.workload, a.spectra, rank)
+    from hfx_gb300 import synth
+    eng = hfx_gb300.Engine(local)
+    eng.build_db(prot.seq, prot.seg, static_add=synth.static_mods(), **synth.DIGEST)
+    stream = torch.cuda.current_stream()
+    eng.set_stream(stream.cuda_stream)
+    prec = a.precision if a.precision >= 0 else 0
+    mode = a.batch_mode if a.batch_mode >= 0 else 0
+    p = hfx_gb300.default_params(top_n=cfg["top_n"], bin_width=cfg["bin_width"], precision=prec, batch_mode=mode,
+                                 rescore_k=32 if prec else 0)
+    d = torch.device("cuda", local)
+    dev = dict(mz=torch.from_numpy(sp.mz).to(d), it=torch.from_numpy(sp.it).to(d),
+               off=torch.from_numpy(sp.off).to(d), pcr=torch.from_numpy(sp.pcr).to(d),
+               z=torch.from_numpy(sp.z).to(d), tol=torch.from_numpy(sp.tol).to(d))
+    ns, tn_ = len(sp), cfg["top_n"]
+    out = dict(score=torch.empty((ns, tn_), dtype=torch.float32, device=d),
+               key=torch.empty((ns, tn_), dtype=torch.int64, device=d),
+               pep=torch.empty((ns, tn_), dtype=torch.int32, device=d),
+               ncand=torch.empty(ns, dtype=torch.int64, device=d))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=d)
+    for _ in range(a.warmup):
+        eng.search_device(dev, p, out)
+    torch.cuda.synchronize()
+    psm_step = int(out["ncand"].sum().item())
+    eng.set_profiling(True)
+    eng.stage_stats(reset=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clk = Clocks(local)
+    total_ms = 0.0
+    for _ in range(a.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        eng.search_device(dev, p, out)
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    stats = eng.stage_stats(reset=True)
+    eng.set_profiling(False)
+    if world > 1:
+        t = torch.tensor([total_ms], device=d)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / a.steps
+    value = psm_step * world / (ms_step / 1000.0)
+    # e2e through the host-buffer C ABI (pinned buffers, copies in the timed region)
+    pin = {k: torch.from_numpy(v).pin_memory() for k, v in
+           dict(mz=sp.mz, it=sp.it, off=sp.off, pcr=sp.pcr, z=sp.z, tol=sp.tol).items()}
+
+    class Pinned:
+        def arrays(self):
+            return tuple(pin[k].numpy() for k in ("mz", "it", "off", "pcr", "z", "tol"))
+    h2d = sum(int(v.numel() * v.element_size()) for v in pin.values())
+    d2h = ns * tn_ * (4 + 8 + 4) + ns * 8
+    eng.search(Pinned(), p)
+    torch.cuda.synchronize()
+    e2e_tot = 0.0
+    for _ in range(a.e2e_steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        eng.search(Pinned(), p)
+        e2e_tot += time.perf_counter() - t1
+    e2e_value = psm_step * world / (e2e_tot / a.e2e_steps)
+    # roofline of the dominant kernel (the scorer)
+    sc_ms, sc_launch, sc_units = stats["score"]
+    rng = np.random.Generator(np.random.PCG64(7))
+    r, tc, tn, idx, mt = eng.db_export()
+    bsz = 2 if prec else 4
+    b_dev = torch.empty(ns, dtype=torch.int32, device=d)
+    e_dev = torch.empty(ns, dtype=torch.int32, device=d)
+    eng.find_windows(dev, p, b_dev, e_dev)
+    wb = b_dev.cpu().numpy().astype(np.int64)
+    we = e_dev.cpu().numpy().astype(np.int64)
+    rows = torch.empty((ns, 4096), dtype=torch.float32, device=d)
+    lens_d = torch.empty(ns, dtype=torch.int32, device=d)
+    eng.preprocess(dev, p, 4096, rows, None, None, lens_d, None)
+    lens = lens_d.cpu().numpy().astype(np.int64)
+    del rows
+    charges = np.array([_charges(z) for z in sp.z], np.int64)
+    bpp, meanU = _bytes_per_psm(eng, bsz, wb, we, lens, charges, (tc[idx], tn[idx]), rng)
+    per_launch_ms = sc_ms / max(1, sc_launch)
+    per_launch_psm = sc_units / max(1, sc_launch)
+    achieved = bpp * per_launch_psm / (per_launch_ms / 1000.0) / 1e9
+    peak, peak_kind = _peaks()
+    launches_per_step = sum(v[1] for v in stats.values()) / a.steps
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": ["f32", "bf16-store/f32", "f16-store/f32"][prec], "data": "synthetic",
+        "config": {"workload": f"{a.workload}: 20000 proteins, {ns} spectra, +-3 Da, 1.0005 Da bins, top-{tn_}",
+                   "psm_per_step": psm_step, "precision": ["fp32", "bf16+fp32 rescore", "fp16+fp32 rescore"][prec],
+                   "batch_mode": ["per-spectrum launches", "persistent batched"][mode],
+                   "l2": "flushed between timed steps (512 MB write)",
+                   "stage_ms_per_step": {k: v[0] / a.steps for k, v in stats.items() if v[1]}},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches_per_step),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "k_score_spectrum" if mode == 0 else "k_score_batched",
+                     "bytes_per_psm": bpp, "mean_distinct_bins": meanU, "peak_kind": peak_kind},
+        "clocks": clocks,
+    }
+    if rank == 0 and not a.no_cpu:
+        line["cpu_baseline"] = _cpu_baseline(a, prot, sp, cfg)
+    if rank == 0:
+        s = json.dumps(line)
+        print(s, flush=True)
+        if a.out:
+            with open(a.out, "w") as f:
+                f.write(s + "\n")
+    eng.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def _charges(z):
+    zm = z - 1.0
+    mc = zm if zm >= 1.0 else 1.0
+    ch = int(np.rint(mc))
+    return ch if 1 <= ch <= 4 else 0
+
+
+def _cpu_baseline(a, prot, sp, cfg):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from hfx_gb300 import synth
+    O.build()
+    mt = O.mass_table(True, synth.static_mods())
+    d = {k: v for k, v in synth.DIGEST.items() if k != "mono"}
+    r, tc, tn = O.digest(prot.seq, prot.seg, mt, **d)
+    idx = O.sort_idx(r)
+    ions = O.pack_ions(prot.seq)
+    sample = sp.subset(np.arange(min(len(sp), a.cpu_sample)))
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    res = O.search(ions, mt, r, tc, tn, idx, sample, topn=cfg["top_n"], nthreads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": float(res[4].sum()) / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {len(sample)} of {len(sp)} spectra, {int(res[4].sum())} pairs, {dt:.1f} s"}
+
+
+if __name__ == "__main__":
+    main()

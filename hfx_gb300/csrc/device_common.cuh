@@ -1,0 +1,343 @@
+// Device building blocks shared by the search kernels (sm_103a).
+//
+// One warp scores one candidate peptide.  The warp
+//   1. builds the b-ion mass ladder with the same FP32 Hillis-Steele order as
+//      the reference warp scan (ion_series.cu:25-56, 176-213),
+//   2. turns every (prefix, charge) into its ten ion bins
+//      (ion_series.cu:78-123) and ORs them into three per-warp bit planes in
+//      shared memory -- "any ion", "weight >= 25", "weight 50" -- which is the
+//      reference's atomicMax-into-a-dense-row (ion_series.cu:71-75) without
+//      the dense row,
+//   3. compacts the planes into the ascending list of distinct bins and
+//      gathers the spectrum at those bins (the sparse form of the reference's
+//      cuBLAS sgemv over the dense row, Search.hs:245).
+// Canonical FP32 order of the gather-dot: list entry i is accumulated by lane
+// i % 32 with fmaf in ascending i; the 32 partial sums are combined by an XOR
+// butterfly with offsets 16, 8, 4, 2, 1.  The oracle computes the same order.
+#pragma once
+#include <cstdint>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include "hfx_internal.h"
+
+namespace hfx {
+
+// Device masses, ion_series.h:16-26 (they differ from the host masses).
+constexpr float kH2O = 18.01056f;
+constexpr float kNH3 = 17.02655f;
+constexpr float kCO = 27.9949f;
+constexpr float kH = 1.0078246f;
+constexpr float kBinMono = 1.0005079f;
+
+constexpr uint32_t kFullMask = 0xFFFFFFFFu;
+
+__device__ __forceinline__ float div_ieee(float a, float b) { return __fdiv_rn(a, b); }
+
+// ion_series.cu:59-69: ionMZ and binMZ.  IEEE division unless FastDiv, which
+// calls __fdividef exactly where the reference did.
+template <bool FastDiv>
+__device__ __forceinline__ float dev_div(float a, float b) {
+    if constexpr (FastDiv) return __fdividef(a, b);
+    else return __fdiv_rn(a, b);
+}
+
+// float -> uint32 conversion (saturating, NaN -> 0) reinterpreted as int32.
+__device__ __forceinline__ int32_t sat_bin(float r) {
+    return (int32_t)__float2uint_rz(r);
+}
+
+template <bool FastDiv>
+__device__ __forceinline__ int32_t bin_of(float mz) {
+    return sat_bin(rintf(dev_div<FastDiv>(mz, kBinMono)));
+}
+
+struct ChargeConst {
+    float cf, hc, dh2o, dnh3;
+};
+
+template <bool FastDiv>
+__device__ __forceinline__ ChargeConst charge_const(int c) {
+    ChargeConst k;
+    k.cf = (float)c;
+    k.hc = __fmul_rn(kH, k.cf);
+    k.dh2o = dev_div<FastDiv>(kH2O, k.cf);
+    k.dnh3 = dev_div<FastDiv>(kNH3, k.cf);
+    return k;
+}
+
+// Bit planes of one warp: A = any ion, H = weight >= 25, T = weight 50.
+// (Weight 25 and 50 bins are only ever set through H and T; "any" is A|H.)
+struct Planes {
+    uint32_t *A, *H, *T;
+};
+
+__device__ __forceinline__ void set_bit(uint32_t *p, int32_t x) {
+    atomicOr(&p[x >> 5], 1u << (x & 31));
+}
+
+// x-1, x, x+1 at weight 25/50/25 (ion_series.cu:92-94, 109-111).
+__device__ __forceinline__ void set_triplet(const Planes &pl, int32_t x, int32_t nbins) {
+    if (x >= 1 && x + 1 < nbins && (x & 31) != 0 && (x & 31) != 31) {
+        atomicOr(&pl.H[x >> 5], 7u << ((x - 1) & 31));
+        atomicOr(&pl.T[x >> 5], 1u << (x & 31));
+        return;
+    }
+    if (0 <= x - 1 && x - 1 < nbins) set_bit(pl.H, x - 1);
+    if (0 <= x + 1 && x + 1 < nbins) set_bit(pl.H, x + 1);
+    if (0 <= x && x < nbins) { set_bit(pl.H, x); set_bit(pl.T, x); }
+}
+
+__device__ __forceinline__ void set_single(const Planes &pl, int32_t x, int32_t nbins) {
+    if (0 <= x && x < nbins) set_bit(pl.A, x);
+}
+
+// The ten ions of one (b, y, charge), ion_series.cu:78-123.
+template <bool FastDiv>
+__device__ __forceinline__ void emit_ions(const Planes &pl, float b, float y,
+                                          const ChargeConst &k, int32_t nbins) {
+    // A ion
+    set_single(pl, bin_of<FastDiv>(dev_div<FastDiv>(__fadd_rn(__fsub_rn(b, kCO), k.hc), k.cf)), nbins);
+    // B ions
+    float m = dev_div<FastDiv>(__fadd_rn(b, k.hc), k.cf);
+    set_triplet(pl, bin_of<FastDiv>(m), nbins);
+    set_single(pl, bin_of<FastDiv>(__fsub_rn(m, k.dh2o)), nbins);
+    set_single(pl, bin_of<FastDiv>(__fsub_rn(m, k.dnh3)), nbins);
+    // Y ions
+    m = dev_div<FastDiv>(__fadd_rn(__fadd_rn(y, kH2O), k.hc), k.cf);
+    set_triplet(pl, bin_of<FastDiv>(m), nbins);
+    set_single(pl, bin_of<FastDiv>(__fsub_rn(m, k.dnh3)), nbins);
+}
+
+// Mass of one packed residue byte (utils.h:92-101; an out-of-range texture
+// fetch of an unpacked byte reads 0).  mt_lane: lane l holds mass[l].
+__device__ __forceinline__ float residue_mass(float mt_lane, uint32_t byte) {
+    uint32_t i = byte & 0x1Fu;
+    float m = __shfl_sync(kFullMask, mt_lane, (int)i);
+    return i < 26u ? m : 0.0f;
+}
+
+// Per-residue modification hook: returns the mass to add (0 = unmodified).
+struct NoMods {
+    __device__ __forceinline__ bool modded(uint32_t /*pos*/) const { return false; }
+    __device__ __forceinline__ float add(uint32_t /*byte*/) const { return 0.0f; }
+};
+
+// Build the ion bit planes of one candidate.  Residues [tc, tn) of `ions`,
+// `charges` ion charges (0 = none), bins >= nbins dropped.
+template <bool FastDiv, typename Mods>
+__device__ __forceinline__ void build_planes(const Planes &pl, const uint8_t *__restrict__ ions,
+                                             uint32_t tc, uint32_t tn, float residual,
+                                             int charges, int32_t nbins, float mt_lane,
+                                             const Mods &mods) {
+    const int lane = threadIdx.x & 31;
+    if (charges <= 0) return;
+    float carry = 0.0f;
+    for (uint32_t base = tc; base < tn; base += 32) {
+        const int cnt = (int)min(32u, tn - base);
+        uint32_t byte = 0;
+        if (lane < cnt) byte = __ldg(ions + base + lane);
+        float v = residue_mass(mt_lane, byte);
+        if (lane < cnt && mods.modded(base + lane - tc)) v = __fadd_rn(v, mods.add(byte));
+        if (lane >= cnt) v = 0.0f;
+        if (lane == 0) v = __fadd_rn(v, carry);
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            float t = __shfl_up_sync(kFullMask, v, d);
+            if (lane >= d) v = __fadd_rn(v, t);
+        }
+        carry = __shfl_sync(kFullMask, v, cnt - 1);
+        const float y = __fsub_rn(residual, v);
+        // balanced (prefix, charge) items: item = (c-1)*cnt + k
+        const int items = cnt * charges;
+        const uint32_t inv = (65536u + (uint32_t)cnt - 1u) / (uint32_t)cnt;
+        for (int it0 = 0; it0 < items; it0 += 32) {
+            const int it = it0 + lane;
+            const int cm1 = (int)(((uint32_t)it * inv) >> 16);
+            const int k = it - cm1 * cnt;
+            const float bk = __shfl_sync(kFullMask, v, k & 31);
+            const float yk = __shfl_sync(kFullMask, y, k & 31);
+            if (it < items) {
+                const ChargeConst kc = charge_const<FastDiv>(cm1 + 1);
+                emit_ions<FastDiv>(pl, bk, yk, kc, nbins);
+            }
+        }
+    }
+    __syncwarp();
+}
+
+// Warp-wide inclusive scan of an int.
+__device__ __forceinline__ int warp_incl_scan(int v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        int t = __shfl_up_sync(kFullMask, v, d);
+        if (lane >= d) v += t;
+    }
+    return v;
+}
+
+template <typename T> __device__ __forceinline__ float load_x(const T *row, uint32_t i);
+template <> __device__ __forceinline__ float load_x<float>(const float *row, uint32_t i) { return row[i]; }
+template <> __device__ __forceinline__ float load_x<__nv_bfloat16>(const __nv_bfloat16 *row, uint32_t i) {
+    return __bfloat162float(row[i]);
+}
+template <> __device__ __forceinline__ float load_x<__half>(const __half *row, uint32_t i) {
+    return __half2float(row[i]);
+}
+
+__device__ __forceinline__ float level_weight(uint32_t lvl) {
+    return lvl == 3u ? 50.0f : (lvl == 2u ? 25.0f : 10.0f);
+}
+
+// A set of spectra scored against the same candidate list.
+template <typename T, int G>
+struct SpecSet {
+    const T *row[G];
+    int32_t len[G];
+    uint32_t active;     // bit g set: score this candidate against spectrum g
+};
+
+// Accumulate list entries [0, n) into acc[] (entry i by lane i%32).
+template <typename T, int G>
+__device__ __forceinline__ void dot_list(const uint16_t *list, int n, const SpecSet<T, G> &ss,
+                                         float (&acc)[G]) {
+    const int lane = threadIdx.x & 31;
+    for (int i = lane; i < n; i += 32) {
+        const uint32_t e = list[i];
+        const uint32_t bin = e >> 2;
+        const float w = level_weight(e & 3u);
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            if (((ss.active >> g) & 1u) && (int32_t)bin < ss.len[g])
+                acc[g] = __fmaf_rn(w, load_x<T>(ss.row[g], bin), acc[g]);
+        }
+    }
+}
+
+// Compact the planes (clearing them) into the sorted distinct-bin list and
+// accumulate the gather-dot for every active spectrum.  words = planes'
+// used word count (multiple of 32 not required).
+template <typename T, int G>
+__device__ __forceinline__ void planes_dot(const Planes &pl, uint16_t *list, int words,
+                                           const SpecSet<T, G> &ss, float (&acc)[G],
+                                           int *n_distinct = nullptr) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int g = 0; g < G; ++g) acc[g] = 0.0f;
+    int nbuf = 0;
+    int ntot = 0;
+    for (int w0 = 0; w0 < words; w0 += 32) {
+        const int w = w0 + lane;
+        uint32_t a = 0, h = 0, t = 0;
+        if (w < words) {
+            h = pl.H[w];
+            t = pl.T[w];
+            a = pl.A[w] | h;
+            pl.A[w] = 0u;
+            pl.H[w] = 0u;
+            pl.T[w] = 0u;
+        }
+        const int pc = __popc(a);
+        const int incl = warp_incl_scan(pc);
+        const int total = __shfl_sync(kFullMask, incl, 31);
+        if (nbuf + total > kListCap) {
+            // flush whole multiples of 32 so that lane = global rank % 32 holds
+            const int full = nbuf & ~31;
+            dot_list<T, G>(list, full, ss, acc);
+            __syncwarp();
+            const int rem = nbuf - full;
+            uint16_t keep = 0;
+            if (lane < rem) keep = list[full + lane];
+            __syncwarp();
+            if (lane < rem) list[lane] = keep;
+            __syncwarp();
+            nbuf = rem;
+        }
+        int pos = nbuf + incl - pc;
+        while (a) {
+            const int b = __ffs(a) - 1;
+            a &= a - 1u;
+            const uint32_t lvl = ((t >> b) & 1u) ? 3u : (((h >> b) & 1u) ? 2u : 1u);
+            list[pos++] = (uint16_t)((((uint32_t)w << 5 | (uint32_t)b) << 2) | lvl);
+        }
+        nbuf += total;
+        ntot += total;
+        __syncwarp();
+    }
+    dot_list<T, G>(list, nbuf, ss, acc);
+    __syncwarp();
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1)
+            acc[g] = __fadd_rn(acc[g], __shfl_xor_sync(kFullMask, acc[g], off));
+    }
+    if (n_distinct) *n_distinct = ntot;
+}
+
+// ---------------------------------------------------------------- top-K ---
+// Final order (Search.hs:118-124 over b40c + sortBy): score descending, then
+// the smaller key (plain keys < modified keys; position/rank ascending).
+__device__ __forceinline__ bool better(float sa, uint64_t ka, float sb, uint64_t kb) {
+    return sa > sb || (sa == sb && ka < kb);
+}
+
+// Warp-distributed sorted list: lane i holds entry i (i < K).
+struct WarpTopK {
+    float s;
+    uint64_t k;
+    __device__ __forceinline__ void init() {
+        s = -INFINITY;
+        k = ~0ull;
+    }
+    // Insert (ns, nk); all lanes pass the same values.
+    __device__ __forceinline__ void insert(float ns, uint64_t nk, int K) {
+        const int lane = threadIdx.x & 31;
+        const bool mine_better = (lane < K) && better(s, k, ns, nk);
+        const uint32_t bal = __ballot_sync(kFullMask, mine_better);
+        const int pos = __popc(bal);
+        const float us = __shfl_up_sync(kFullMask, s, 1);
+        const uint64_t uk = __shfl_up_sync(kFullMask, k, 1);
+        if (pos < K) {
+            if (lane == pos) { s = ns; k = nk; }
+            else if (lane > pos && lane < K) { s = us; k = uk; }
+        }
+    }
+};
+
+// Bounded spin on an mbarrier phase: returns false after max_iter tries.
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t phase, uint32_t max_iter) {
+    for (uint32_t i = 0; i < max_iter; ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(ok)
+            : "r"(smem_u32(bar)), "r"(phase)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+}  // namespace hfx

@@ -1,0 +1,748 @@
+// C++ host side of libhfx_gpu.so: context, database build and upload,
+// orchestration of the search kernels and the C ABI (include/hfx_gpu.h).
+//
+// Mirrors the reference's Haskell host for the search path:
+//   makeSeqDB / withDeviceDB      Sequence/Fragment.hs:197-258
+//   makeModInfo                   Sequence/Fragment.hs:260-289
+//   searchForMatches              Sequence/Search.hs:98-277
+// with the per-spectrum Haskell loops replaced by device kernels.
+#include "hfx_internal.h"
+#include "search_kernels.h"
+#include "../../include/hfx_gpu.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <string>
+#include <vector>
+
+using namespace hfx;
+
+namespace {
+
+// Residue masses, Mass.hs:37-69 (mono) and :76-103 (average), by c - 'A'.
+const float kMonoMass[26] = {
+    71.037114f,  114.53494f, 103.009185f, 115.026943f, 129.042593f, 147.068414f, 57.021464f,
+    137.058912f, 113.084064f, 113.16472f, 128.094963f, 113.084064f, 131.040485f, 114.042927f,
+    114.07931f,  97.052764f, 128.058578f, 156.101111f, 87.032028f,  101.047679f, 150.04344f,
+    99.068414f,  186.079313f, 113.08406f, 163.06332f, 128.55059f};
+const float kAvgMass[26] = {
+    71.0788f,  114.5962f, 103.1388f, 115.0886f, 129.1155f, 147.1766f, 57.0519f,  137.1411f, 113.1594f,
+    113.240178f, 128.1741f, 113.1594f, 131.1926f, 114.1038f, 114.1472f, 97.1167f, 128.1307f, 156.1875f,
+    87.0782f,  101.1051f, 150.0388f, 99.1326f,  186.2132f, 113.1594f, 163.1760f, 128.6231f};
+const float kHostH2O = 18.010565f;  // Mass.hs:20
+const float kHostH = 1.007276f;     // Mass.hs:25
+
+bool cleaves_after(int rule, uint8_t c) {  // Config.hs:415-431
+    static const char *const sets[14] = {"",  "KR", "FWY", "R", "M", "W", "P",
+                                         "E", "K",  "R",   "D", "FWYL", "ALIV", "ALIVKRWFY"};
+    if (rule < 0 || rule > 13) return false;
+    return c != 0 && std::strchr(sets[rule], (int)c) != nullptr;
+}
+
+// Grow-only device buffer.
+struct DBuf {
+    void *p = nullptr;
+    size_t n = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= n) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        size_t want = bytes < 256 ? 256 : bytes;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) n = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+}  // namespace
+
+struct hfx_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    // database (residual-mass order on the device)
+    uint64_t num_ions = 0, num_pep = 0;
+    float mt[26] = {0};
+    std::vector<uint8_t> h_ascii;
+    std::vector<float> h_r;        // fragment order
+    std::vector<uint32_t> h_tc, h_tn;
+    std::vector<uint32_t> h_idx;   // mass order -> fragment
+    DBuf d_ions, d_r, d_tc, d_tn, d_idx;
+    // variable modifications
+    int32_t num_ma = 0, max_ma = 0, per_type = 0, num_mod = 0;
+    uint8_t ma[8] = {0};
+    float ma_mass[8] = {0};
+    std::vector<int32_t> mod_counts;
+    std::vector<float> mod_delta;
+    DBuf d_mod_counts, d_mod_delta;
+    // workspace
+    std::map<std::string, DBuf> ws;
+    DBuf d_err;
+    // stage timing (CUDA events on the context stream) and launch counts
+    bool profile = false;
+    cudaEvent_t ev[HFX_NSTAGES][2] = {};
+    bool ev_pending[HFX_NSTAGES] = {};
+    double stage_ms[HFX_NSTAGES] = {0};
+    int64_t stage_launches[HFX_NSTAGES] = {0};
+    int64_t stage_units[HFX_NSTAGES] = {0};
+
+    void stage_begin(int s) {
+        if (!profile) return;
+        if (!ev[s][0]) { cudaEventCreate(&ev[s][0]); cudaEventCreate(&ev[s][1]); }
+        cudaEventRecord(ev[s][0], stream);
+    }
+    void stage_end(int s, int64_t launches, int64_t units = 0) {
+        stage_launches[s] += launches;
+        stage_units[s] += units;
+        if (!profile) return;
+        cudaEventRecord(ev[s][1], stream);
+        ev_pending[s] = true;
+    }
+    void stage_collect() {
+        for (int s = 0; s < HFX_NSTAGES; ++s) {
+            if (!ev_pending[s]) continue;
+            float ms = 0.0f;
+            cudaEventSynchronize(ev[s][1]);
+            cudaEventElapsedTime(&ms, ev[s][0], ev[s][1]);
+            stage_ms[s] += ms;
+            ev_pending[s] = false;
+        }
+    }
+
+    template <typename T> T *buf(const char *name, size_t count, cudaError_t &e) {
+        DBuf &b = ws[name];
+        e = b.ensure(count * sizeof(T) + 16);
+        return b.as<T>();
+    }
+    DevDB devdb() const {
+        DevDB db;
+        db.ions = d_ions.as<uint8_t>();
+        db.r_sorted = d_r.as<float>();
+        db.tc_sorted = d_tc.as<uint32_t>();
+        db.tn_sorted = d_tn.as<uint32_t>();
+        db.idx_sorted = d_idx.as<uint32_t>();
+        db.num_pep = (uint32_t)num_pep;
+        for (int i = 0; i < 32; ++i) db.mt[i] = i < 26 ? mt[i] : 0.0f;
+        return db;
+    }
+};
+
+namespace {
+
+int32_t fail(hfx_ctx *c, int32_t code, const std::string &msg) {
+    if (c) c->err = msg;
+    return code;
+}
+int32_t cuda_fail(hfx_ctx *c, cudaError_t e, const char *where) {
+    if (e == cudaErrorMemoryAllocation)
+        return fail(c, HFX_ERR_OOM, std::string(where) + ": " + cudaGetErrorString(e));
+    return fail(c, HFX_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define HFX_CUDA(call, where)                         \
+    do {                                              \
+        cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, where); \
+    } while (0)
+
+// prepare_ions.cu:29-52 packing: (c - 'A') | (index of c in ma + 1) << 5.
+void pack_ions(const std::vector<uint8_t> &ascii, const uint8_t *ma, int num_ma, std::vector<uint8_t> &out) {
+    out.resize(ascii.size());
+    uint8_t code[256];
+    for (int c = 0; c < 256; ++c) {
+        uint8_t mod = 0;
+        for (int j = 0; j < num_ma; ++j)
+            if (ma[j] == c) { mod = (uint8_t)(j + 1); break; }
+        code[c] = (uint8_t)((uint8_t)(c - 'A') | (uint8_t)(mod << 5));
+    }
+    for (size_t i = 0; i < ascii.size(); ++i) out[i] = code[ascii[i]];
+}
+
+int32_t upload_db(hfx_ctx *ctx) {
+    const uint64_t np = ctx->num_pep;
+    ctx->h_idx.resize(np);
+    std::iota(ctx->h_idx.begin(), ctx->h_idx.end(), 0u);
+    // sort.cu:28-35: key-value sort of residual masses with iota (stable)
+    std::stable_sort(ctx->h_idx.begin(), ctx->h_idx.end(),
+                     [&](uint32_t a, uint32_t b) { return ctx->h_r[a] < ctx->h_r[b]; });
+    std::vector<float> rs(np);
+    std::vector<uint32_t> tcs(np), tns(np);
+    for (uint64_t i = 0; i < np; ++i) {
+        rs[i] = ctx->h_r[ctx->h_idx[i]];
+        tcs[i] = ctx->h_tc[ctx->h_idx[i]];
+        tns[i] = ctx->h_tn[ctx->h_idx[i]];
+        if (tns[i] < tcs[i] || tns[i] > ctx->num_ions) return fail(ctx, HFX_ERR_ARG, "fragment outside the residues");
+    }
+    std::vector<uint8_t> packed;
+    pack_ions(ctx->h_ascii, ctx->ma, ctx->num_ma, packed);
+    HFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    HFX_CUDA(ctx->d_ions.ensure(packed.size() + 64), "alloc ions");
+    HFX_CUDA(ctx->d_r.ensure(np * 4 + 16), "alloc r");
+    HFX_CUDA(ctx->d_tc.ensure(np * 4 + 16), "alloc tc");
+    HFX_CUDA(ctx->d_tn.ensure(np * 4 + 16), "alloc tn");
+    HFX_CUDA(ctx->d_idx.ensure(np * 4 + 16), "alloc idx");
+    HFX_CUDA(cudaMemcpy(ctx->d_ions.p, packed.data(), packed.size(), cudaMemcpyHostToDevice), "H2D ions");
+    HFX_CUDA(cudaMemcpy(ctx->d_r.p, rs.data(), np * 4, cudaMemcpyHostToDevice), "H2D r");
+    HFX_CUDA(cudaMemcpy(ctx->d_tc.p, tcs.data(), np * 4, cudaMemcpyHostToDevice), "H2D tc");
+    HFX_CUDA(cudaMemcpy(ctx->d_tn.p, tns.data(), np * 4, cudaMemcpyHostToDevice), "H2D tn");
+    HFX_CUDA(cudaMemcpy(ctx->d_idx.p, ctx->h_idx.data(), np * 4, cudaMemcpyHostToDevice), "H2D idx");
+    return HFX_OK;
+}
+
+// Fragment.hs:260-289 makeModInfo: count vectors over 0..max_ma with
+// dimension 0 most significant, all-zero dropped, sum < max_ma kept.
+void make_mod_table(hfx_ctx *ctx) {
+    ctx->mod_counts.clear();
+    ctx->mod_delta.clear();
+    ctx->num_mod = 0;
+    const int n = ctx->num_ma;
+    if (n <= 0) return;
+    std::vector<int32_t> c(n, 0);
+    for (;;) {
+        int d = n - 1;
+        while (d >= 0 && c[d] == ctx->max_ma) c[d--] = 0;
+        if (d < 0) break;
+        ++c[d];
+        int s = 0;
+        for (int i = 0; i < n; ++i) s += c[i];
+        if (s >= ctx->max_ma) continue;
+        float delta = 0.0f;
+        for (int i = 0; i < n; ++i) delta = delta + ctx->ma_mass[i] * (float)c[i];
+        ctx->mod_counts.insert(ctx->mod_counts.end(), c.begin(), c.end());
+        ctx->mod_delta.push_back(delta);
+        ++ctx->num_mod;
+    }
+}
+
+struct Batch {
+    const float *mz, *it, *pcr, *z, *tol;
+    const int64_t *off;
+    int32_t nspec;
+};
+
+int32_t check_params(hfx_ctx *ctx, const hfx_search_params *p) {
+    if (!p) return fail(ctx, HFX_ERR_ARG, "null params");
+    if (p->top_n < 1 || p->top_n > kMaxTopK) return fail(ctx, HFX_ERR_ARG, "top_n must be 1..32");
+    if (!(p->bin_width > 0.0f)) return fail(ctx, HFX_ERR_ARG, "bin_width must be > 0");
+    if (p->precision < 0 || p->precision > 2) return fail(ctx, HFX_ERR_ARG, "precision must be 0, 1 or 2");
+    if (ctx->num_pep == 0) return fail(ctx, HFX_ERR_ARG, "no database uploaded");
+    return HFX_OK;
+}
+
+LayoutParams layout_params(const hfx_search_params *p) {
+    LayoutParams lp;
+    lp.bw = p->bin_width;
+    lp.custom_bw = p->custom_bin_width;
+    lp.remove_pcr = p->remove_precursor_peak;
+    lp.ppm = p->tol_ppm;
+    lp.max_len = p->max_len > 0 ? p->max_len : 8192;
+    return lp;
+}
+
+// Layout + preprocess a batch into the workspace rows.  Returns stride.
+int32_t run_stage_a(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, int64_t &stride,
+                    SpecMeta *&meta, float *&rows, __nv_bfloat16 *&rows_bf, __half *&rows_h, bool want_bf,
+                    bool want_h) {
+    cudaError_t e;
+    const LayoutParams lp = layout_params(p);
+    meta = ctx->buf<SpecMeta>("meta", b.nspec, e);
+    if (e) return cuda_fail(ctx, e, "alloc meta");
+    uint32_t *d_max = ctx->buf<uint32_t>("maxlen", 4, e);
+    if (e) return cuda_fail(ctx, e, "alloc maxlen");
+    HFX_CUDA(cudaMemsetAsync(d_max, 0, 4, ctx->stream), "memset");
+    ctx->stage_begin(HFX_STAGE_LAYOUT);
+    int rc = hfx_launch_layout(b.mz, b.off, b.pcr, b.z, b.tol, b.nspec, lp, meta, d_max, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_layout");
+    ctx->stage_end(HFX_STAGE_LAYOUT, 1, b.nspec);
+    uint32_t maxlen = 0;
+    HFX_CUDA(cudaMemcpyAsync(&maxlen, d_max, 4, cudaMemcpyDeviceToHost, ctx->stream), "D2H maxlen");
+    HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    if (maxlen == 0) maxlen = 16;
+    stride = ((int64_t)maxlen + 15) & ~(int64_t)15;
+    rows = ctx->buf<float>("rows32", (size_t)b.nspec * stride, e);
+    if (e) return cuda_fail(ctx, e, "alloc rows");
+    rows_bf = nullptr;
+    rows_h = nullptr;
+    if (want_bf) {
+        rows_bf = ctx->buf<__nv_bfloat16>("rowsbf", (size_t)b.nspec * stride, e);
+        if (e) return cuda_fail(ctx, e, "alloc rows bf16");
+    }
+    if (want_h) {
+        rows_h = ctx->buf<__half>("rowsh", (size_t)b.nspec * stride, e);
+        if (e) return cuda_fail(ctx, e, "alloc rows fp16");
+    }
+    ctx->stage_begin(HFX_STAGE_PREPROCESS);
+    rc = hfx_launch_preprocess(b.mz, b.it, b.off, b.pcr, lp, meta, b.nspec, stride, rows, rows_bf, rows_h,
+                               ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_preprocess");
+    ctx->stage_end(HFX_STAGE_PREPROCESS, 1, b.nspec);
+    return HFX_OK;
+}
+
+int32_t search_plain_per_spectrum(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, const SpecMeta *meta,
+                                  const float *rows, int64_t stride, float *out_s, uint64_t *out_k,
+                                  uint32_t *out_pep, int64_t *out_ncand) {
+    cudaError_t e;
+    uint32_t *wb = ctx->buf<uint32_t>("wb", b.nspec, e);
+    if (e) return cuda_fail(ctx, e, "alloc wb");
+    uint32_t *we = ctx->buf<uint32_t>("we", b.nspec, e);
+    if (e) return cuda_fail(ctx, e, "alloc we");
+    ctx->stage_begin(HFX_STAGE_WINDOWS);
+    int rc = hfx_launch_windows(ctx->d_r.as<float>(), (uint32_t)ctx->num_pep, meta, b.nspec, wb, we, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_windows");
+    ctx->stage_end(HFX_STAGE_WINDOWS, 1, b.nspec);
+    // Search.hs:184-185 peeks the counts to the host; so does the plain path.
+    std::vector<uint32_t> hb(b.nspec), he(b.nspec);
+    std::vector<SpecMeta> hm(b.nspec);
+    HFX_CUDA(cudaMemcpyAsync(hb.data(), wb, 4ull * b.nspec, cudaMemcpyDeviceToHost, ctx->stream), "D2H wb");
+    HFX_CUDA(cudaMemcpyAsync(he.data(), we, 4ull * b.nspec, cudaMemcpyDeviceToHost, ctx->stream), "D2H we");
+    HFX_CUDA(cudaMemcpyAsync(hm.data(), meta, sizeof(SpecMeta) * b.nspec, cudaMemcpyDeviceToHost, ctx->stream),
+             "D2H meta");
+    HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    const int32_t K = std::max(p->top_n, std::min(p->rescore_k > 0 ? p->rescore_k : p->top_n, kMaxTopK));
+    std::vector<int64_t> part_off(b.nspec + 1, 0);
+    std::vector<int32_t> nblk(b.nspec, 0);
+    for (int32_t s = 0; s < b.nspec; ++s) {
+        const uint32_t nc = he[s] - hb[s];
+        int32_t nb = 0;
+        if (nc > 0 && hm[s].status == 0) nb = (int32_t)std::min<uint32_t>((nc + 31) / 32, 304u);
+        nblk[s] = nb;
+        part_off[s + 1] = part_off[s] + nb;
+    }
+    float *ps = ctx->buf<float>("part_s", (size_t)part_off[b.nspec] * K + 1, e);
+    if (e) return cuda_fail(ctx, e, "alloc parts");
+    uint64_t *pk = ctx->buf<uint64_t>("part_k", (size_t)part_off[b.nspec] * K + 1, e);
+    if (e) return cuda_fail(ctx, e, "alloc parts");
+    int64_t *d_off = ctx->buf<int64_t>("part_off", b.nspec + 1, e);
+    if (e) return cuda_fail(ctx, e, "alloc part_off");
+    HFX_CUDA(cudaMemcpyAsync(d_off, part_off.data(), 8ull * (b.nspec + 1), cudaMemcpyHostToDevice, ctx->stream),
+             "H2D part_off");
+    const DevDB db = ctx->devdb();
+    int64_t nl = 0, psm = 0;
+    ctx->stage_begin(HFX_STAGE_SCORE);
+    for (int32_t s = 0; s < b.nspec; ++s) {
+        if (nblk[s] == 0) continue;
+        ++nl;
+        psm += he[s] - hb[s];
+        const int32_t ch = hm[s].charges_plain;
+        rc = hfx_launch_score_spectrum(db, rows + (size_t)s * stride, hm[s].len, ch, hb[s], he[s], K, nblk[s],
+                                       p->fastdiv, ps + part_off[s] * K, pk + part_off[s] * K,
+                                       ctx->d_err.as<uint32_t>(), ctx->stream);
+        if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_spectrum");
+    }
+    ctx->stage_end(HFX_STAGE_SCORE, nl, psm);
+    ctx->stage_begin(HFX_STAGE_TOPN);
+    rc = hfx_launch_merge_parts(ps, pk, d_off, b.nspec, K, p->top_n, ctx->d_idx.as<uint32_t>(), out_s, out_k,
+                                out_pep, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_merge_parts");
+    ctx->stage_end(HFX_STAGE_TOPN, 1, b.nspec);
+    if (out_ncand) {
+        std::vector<int64_t> nc(b.nspec);
+        for (int32_t s = 0; s < b.nspec; ++s) nc[s] = (hm[s].status == 0) ? (int64_t)(he[s] - hb[s]) : 0;
+        HFX_CUDA(cudaMemcpyAsync(out_ncand, nc.data(), 8ull * b.nspec, cudaMemcpyHostToDevice, ctx->stream),
+                 "H2D ncand");
+        HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    }
+    return HFX_OK;
+}
+
+int32_t search_device(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, float *out_s, uint64_t *out_k,
+                      uint32_t *out_pep, int64_t *out_ncand) {
+    int32_t rc = check_params(ctx, p);
+    if (rc) return rc;
+    if (b.nspec <= 0) return HFX_OK;
+    HFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    HFX_CUDA(ctx->d_err.ensure(16), "alloc err");
+    HFX_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, 4, ctx->stream), "memset err");
+    int64_t stride = 0;
+    SpecMeta *meta = nullptr;
+    float *rows = nullptr;
+    __nv_bfloat16 *rows_bf = nullptr;
+    __half *rows_h = nullptr;
+    rc = run_stage_a(ctx, p, b, stride, meta, rows, rows_bf, rows_h, p->precision == 1, p->precision == 2);
+    if (rc) return rc;
+    if (p->search_mods && ctx->num_mod > 0) return fail(ctx, HFX_ERR_UNSUPPORTED, "modification search not built yet");
+    rc = search_plain_per_spectrum(ctx, p, b, meta, rows, stride, out_s, out_k, out_pep, out_ncand);
+    if (rc) return rc;
+    uint32_t herr = 0;
+    HFX_CUDA(cudaMemcpyAsync(&herr, ctx->d_err.p, 4, cudaMemcpyDeviceToHost, ctx->stream), "D2H err");
+    HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    ctx->stage_collect();
+    if (herr & kErrTimeout) return fail(ctx, HFX_ERR_TIMEOUT, "device wait timed out");
+    if (herr) return fail(ctx, HFX_ERR_UNSUPPORTED, "device error word " + std::to_string(herr));
+    return HFX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void hfx_default_params(hfx_search_params *p) {
+    std::memset(p, 0, sizeof(*p));
+    p->bin_width = 1.0005079f;
+    p->custom_bin_width = 0;
+    p->remove_precursor_peak = 1;
+    p->tol_ppm = 0;
+    p->top_n = 10;
+    p->precision = 0;
+    p->rescore_k = 0;
+    p->batch_mode = 0;
+    p->fastdiv = 0;
+    p->search_plain = 1;
+    p->search_mods = 1;
+    p->group_size = 0;
+    p->chunk = 0;
+    p->max_len = 0;
+}
+
+int32_t hfx_ctx_create(int32_t device, hfx_ctx **out) {
+    if (!out) return HFX_ERR_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return HFX_ERR_CUDA;
+    hfx_ctx *c = new hfx_ctx();
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) {
+        delete c;
+        return HFX_ERR_CUDA;
+    }
+    c->own_stream = true;
+    *out = c;
+    return HFX_OK;
+}
+
+int32_t hfx_ctx_destroy(hfx_ctx *ctx) {
+    if (!ctx) return HFX_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto &kv : ctx->ws) kv.second.release();
+    ctx->d_ions.release();
+    ctx->d_r.release();
+    ctx->d_tc.release();
+    ctx->d_tn.release();
+    ctx->d_idx.release();
+    ctx->d_mod_counts.release();
+    ctx->d_mod_delta.release();
+    ctx->d_err.release();
+    for (int s = 0; s < HFX_NSTAGES; ++s)
+        if (ctx->ev[s][0]) { cudaEventDestroy(ctx->ev[s][0]); cudaEventDestroy(ctx->ev[s][1]); }
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return HFX_OK;
+}
+
+int32_t hfx_set_stream(hfx_ctx *ctx, void *stream) {
+    if (!ctx) return HFX_ERR_ARG;
+    if (!stream) return HFX_OK;
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    ctx->stream = (cudaStream_t)stream;
+    ctx->own_stream = false;
+    return HFX_OK;
+}
+
+const char *hfx_last_error(const hfx_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int32_t hfx_set_profiling(hfx_ctx *ctx, int32_t on) {
+    if (!ctx) return HFX_ERR_ARG;
+    ctx->profile = on != 0;
+    return HFX_OK;
+}
+
+int32_t hfx_stage_stats(hfx_ctx *ctx, double *ms, int64_t *launches, int64_t *units, int32_t reset) {
+    if (!ctx) return HFX_ERR_ARG;
+    ctx->stage_collect();
+    for (int s = 0; s < HFX_NSTAGES; ++s) {
+        if (ms) ms[s] = ctx->stage_ms[s];
+        if (launches) launches[s] = ctx->stage_launches[s];
+        if (units) units[s] = ctx->stage_units[s];
+        if (reset) {
+            ctx->stage_ms[s] = 0.0;
+            ctx->stage_launches[s] = 0;
+            ctx->stage_units[s] = 0;
+        }
+    }
+    return HFX_OK;
+}
+
+int64_t hfx_digest(const uint8_t *seq, const uint32_t *seg, int32_t nprot, const float *mt26, int32_t rule,
+                   int32_t missed, float min_mass, float max_mass, int32_t proline_rule, int32_t min_len,
+                   int32_t max_len, float *r, uint32_t *tc, uint32_t *tn, int64_t cap) {
+    if (!seq || !seg || !mt26 || nprot < 0 || missed < 0 || rule < 0 || rule > 13) return -1;
+    struct Frag { float m; uint32_t c, n, len; };
+    std::vector<Frag> fr;
+    int64_t nf = 0;
+    for (int32_t pi = 0; pi < nprot; ++pi) {
+        // Fragment.hs:376-390: split after each cleavage residue; the last
+        // piece of a protein ends one past its final residue.
+        fr.clear();
+        uint32_t c = seg[pi];
+        const uint32_t y = seg[pi + 1];
+        while (c < y) {
+            uint32_t i = c;
+            for (; i < y; ++i) {
+                if (!cleaves_after(rule, seq[i])) continue;
+                if (proline_rule && i + 1 < y && seq[i + 1] == 'P') continue;
+                break;
+            }
+            float m = 0.0f;  // G.foldl' (+) 0
+            if (i == y) {
+                for (uint32_t j = c; j < y; ++j) m = m + mt26[seq[j] - 'A'];
+                fr.push_back({m, c, y, y - c});
+                break;
+            }
+            for (uint32_t j = c; j <= i; ++j) m = m + mt26[seq[j] - 'A'];
+            fr.push_back({m, c, i, i - c + 1});
+            c = i + 1;
+        }
+        // Fragment.hs:397-405 splice, :365-369 mass filter
+        for (size_t i = 0; i < fr.size(); ++i) {
+            Frag a = fr[i];
+            for (int k = 0; k <= missed && i + k < fr.size(); ++k) {
+                if (k) a = {a.m + fr[i + k].m, a.c, fr[i + k].n, a.len + fr[i + k].len};
+                const float mm = (a.m + kHostH2O) + kHostH;
+                if (!(min_mass <= mm && mm <= max_mass)) continue;
+                if (min_len > 0 && (int32_t)a.len < min_len) continue;
+                if (max_len > 0 && (int32_t)a.len > max_len) continue;
+                if (r) {
+                    if (nf >= cap) return -2;
+                    r[nf] = a.m;
+                    tc[nf] = a.c;
+                    tn[nf] = a.n;
+                }
+                ++nf;
+            }
+        }
+    }
+    return nf;
+}
+
+int32_t hfx_pack_ions(const uint8_t *ascii, uint64_t n, const uint8_t *ma, int32_t num_ma, uint8_t *out) {
+    if (!ascii || !out || num_ma < 0 || num_ma > 7) return HFX_ERR_ARG;
+    std::vector<uint8_t> in(ascii, ascii + n), packed;
+    pack_ions(in, ma, num_ma, packed);
+    std::memcpy(out, packed.data(), n);
+    return HFX_OK;
+}
+
+int32_t hfx_build_db(hfx_ctx *ctx, const uint8_t *seq, const uint32_t *seg, int32_t nprot, const float *add26,
+                     int32_t mono, int32_t rule, int32_t missed, float min_mass, float max_mass,
+                     int32_t proline_rule, int32_t min_len, int32_t max_len) {
+    if (!ctx || !seq || !seg || nprot < 0 || missed < 0 || rule < 0 || rule > 13)
+        return fail(ctx, HFX_ERR_ARG, "bad hfx_build_db arguments");
+    // Config.hs:266-272: table = static add + residue mass
+    for (int i = 0; i < 26; ++i) ctx->mt[i] = (add26 ? add26[i] : 0.0f) + (mono ? kMonoMass[i] : kAvgMass[i]);
+    const uint32_t nion = seg[nprot];
+    for (uint32_t i = 0; i < nion; ++i)
+        if (seq[i] < 'A' || seq[i] > 'Z') return fail(ctx, HFX_ERR_ARG, "residue outside A-Z");
+    const int64_t nf = hfx_digest(seq, seg, nprot, ctx->mt, rule, missed, min_mass, max_mass, proline_rule,
+                                  min_len, max_len, nullptr, nullptr, nullptr, 0);
+    if (nf < 0) return fail(ctx, HFX_ERR_ARG, "digest failed");
+    if (nf >= (1ll << 27)) return fail(ctx, HFX_ERR_UNSUPPORTED, "more than 2^27 fragments");
+    ctx->h_ascii.assign(seq, seq + nion);
+    ctx->h_r.resize(nf);
+    ctx->h_tc.resize(nf);
+    ctx->h_tn.resize(nf);
+    hfx_digest(seq, seg, nprot, ctx->mt, rule, missed, min_mass, max_mass, proline_rule, min_len, max_len,
+               ctx->h_r.data(), ctx->h_tc.data(), ctx->h_tn.data(), nf);
+    ctx->num_ions = nion;
+    ctx->num_pep = (uint64_t)nf;
+    return upload_db(ctx);
+}
+
+int32_t hfx_upload_db(hfx_ctx *ctx, const uint8_t *ions, uint64_t num_ions, const float *r, const uint32_t *tc,
+                      const uint32_t *tn, uint64_t num_pep, const float *mt26) {
+    if (!ctx || !ions || !r || !tc || !tn || !mt26) return fail(ctx, HFX_ERR_ARG, "bad hfx_upload_db arguments");
+    if (num_pep >= (1ull << 27)) return fail(ctx, HFX_ERR_UNSUPPORTED, "more than 2^27 fragments");
+    ctx->h_ascii.assign(ions, ions + num_ions);
+    ctx->h_r.assign(r, r + num_pep);
+    ctx->h_tc.assign(tc, tc + num_pep);
+    ctx->h_tn.assign(tn, tn + num_pep);
+    std::memcpy(ctx->mt, mt26, sizeof(ctx->mt));
+    ctx->num_ions = num_ions;
+    ctx->num_pep = num_pep;
+    return upload_db(ctx);
+}
+
+int32_t hfx_db_info(const hfx_ctx *ctx, uint64_t *num_ions, uint64_t *num_pep) {
+    if (!ctx) return HFX_ERR_ARG;
+    if (num_ions) *num_ions = ctx->num_ions;
+    if (num_pep) *num_pep = ctx->num_pep;
+    return HFX_OK;
+}
+
+int32_t hfx_db_export(const hfx_ctx *ctx, float *r, uint32_t *tc, uint32_t *tn, uint32_t *idx, float *mt26) {
+    if (!ctx) return HFX_ERR_ARG;
+    const size_t n = ctx->num_pep;
+    if (r) std::memcpy(r, ctx->h_r.data(), n * 4);
+    if (tc) std::memcpy(tc, ctx->h_tc.data(), n * 4);
+    if (tn) std::memcpy(tn, ctx->h_tn.data(), n * 4);
+    if (idx) std::memcpy(idx, ctx->h_idx.data(), n * 4);
+    if (mt26) std::memcpy(mt26, ctx->mt, sizeof(ctx->mt));
+    return HFX_OK;
+}
+
+int32_t hfx_set_mods(hfx_ctx *ctx, int32_t num_ma, const uint8_t *ma, const float *ma_mass, int32_t max_ma,
+                     int32_t per_type) {
+    if (!ctx || num_ma < 0 || num_ma > 7 || (num_ma > 0 && (!ma || !ma_mass)))
+        return fail(ctx, HFX_ERR_ARG, "num_ma must be 0..7 (3-bit field, utils.h:97)");
+    ctx->num_ma = num_ma;
+    ctx->max_ma = max_ma;
+    ctx->per_type = per_type;
+    for (int i = 0; i < num_ma; ++i) {
+        ctx->ma[i] = ma[i];
+        ctx->ma_mass[i] = ma_mass[i];
+    }
+    make_mod_table(ctx);
+    if (ctx->num_mod >= 512) return fail(ctx, HFX_ERR_UNSUPPORTED, "more than 511 modification combinations");
+    if (ctx->num_mod > 0) {
+        HFX_CUDA(ctx->d_mod_counts.ensure(ctx->mod_counts.size() * 4 + 16), "alloc mods");
+        HFX_CUDA(ctx->d_mod_delta.ensure(ctx->mod_delta.size() * 4 + 16), "alloc mods");
+        HFX_CUDA(cudaMemcpy(ctx->d_mod_counts.p, ctx->mod_counts.data(), ctx->mod_counts.size() * 4,
+                            cudaMemcpyHostToDevice), "H2D mods");
+        HFX_CUDA(cudaMemcpy(ctx->d_mod_delta.p, ctx->mod_delta.data(), ctx->mod_delta.size() * 4,
+                            cudaMemcpyHostToDevice), "H2D mods");
+    }
+    if (ctx->num_pep > 0) return upload_db(ctx);
+    return HFX_OK;
+}
+
+int32_t hfx_mod_table(const hfx_ctx *ctx, int32_t *num_mod, int32_t *counts, float *deltas, int32_t cap) {
+    if (!ctx) return HFX_ERR_ARG;
+    if (num_mod) *num_mod = ctx->num_mod;
+    if (ctx->num_mod > cap) return HFX_ERR_ARG;
+    if (counts) std::memcpy(counts, ctx->mod_counts.data(), ctx->mod_counts.size() * 4);
+    if (deltas) std::memcpy(deltas, ctx->mod_delta.data(), ctx->mod_delta.size() * 4);
+    return HFX_OK;
+}
+
+int32_t hfx_search_device(hfx_ctx *ctx, const hfx_search_params *p, const float *mz, const float *it,
+                          const int64_t *off, const float *pcr, const float *z, const float *tol, int32_t nspec,
+                          float *out_s, uint64_t *out_k, uint32_t *out_pep, int64_t *out_ncand) {
+    if (!ctx) return HFX_ERR_ARG;
+    Batch b{mz, it, pcr, z, tol, off, nspec};
+    return search_device(ctx, p, b, out_s, out_k, out_pep, out_ncand);
+}
+
+int32_t hfx_search_host(hfx_ctx *ctx, const hfx_search_params *p, const float *mz, const float *it,
+                        const int64_t *off, const float *pcr, const float *z, const float *tol, int32_t nspec,
+                        float *out_s, uint64_t *out_k, uint32_t *out_pep, int64_t *out_ncand) {
+    if (!ctx || nspec < 0 || !off) return fail(ctx, HFX_ERR_ARG, "bad hfx_search_host arguments");
+    HFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const int64_t npk = off[nspec];
+    cudaError_t e;
+    float *d_mz = ctx->buf<float>("in_mz", npk + 1, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    float *d_it = ctx->buf<float>("in_it", npk + 1, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    int64_t *d_off = ctx->buf<int64_t>("in_off", nspec + 1, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    float *d_meta = ctx->buf<float>("in_pzt", 3ull * nspec + 1, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    const int32_t topn = p ? p->top_n : 0;
+    float *d_os = ctx->buf<float>("out_s", (size_t)nspec * topn + 1, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    uint64_t *d_ok = ctx->buf<uint64_t>("out_k", (size_t)nspec * topn + 1, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    uint32_t *d_op = ctx->buf<uint32_t>("out_p", (size_t)nspec * topn + 1, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    int64_t *d_nc = ctx->buf<int64_t>("out_nc", nspec + 1, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    cudaStream_t st = ctx->stream;
+    HFX_CUDA(cudaMemcpyAsync(d_mz, mz, 4ull * npk, cudaMemcpyHostToDevice, st), "H2D mz");
+    HFX_CUDA(cudaMemcpyAsync(d_it, it, 4ull * npk, cudaMemcpyHostToDevice, st), "H2D it");
+    HFX_CUDA(cudaMemcpyAsync(d_off, off, 8ull * (nspec + 1), cudaMemcpyHostToDevice, st), "H2D off");
+    HFX_CUDA(cudaMemcpyAsync(d_meta, pcr, 4ull * nspec, cudaMemcpyHostToDevice, st), "H2D pcr");
+    HFX_CUDA(cudaMemcpyAsync(d_meta + nspec, z, 4ull * nspec, cudaMemcpyHostToDevice, st), "H2D z");
+    HFX_CUDA(cudaMemcpyAsync(d_meta + 2 * nspec, tol, 4ull * nspec, cudaMemcpyHostToDevice, st), "H2D tol");
+    Batch b{d_mz, d_it, d_meta, d_meta + nspec, d_meta + 2 * nspec, d_off, nspec};
+    int32_t rc = search_device(ctx, p, b, d_os, d_ok, d_op, out_ncand ? d_nc : nullptr);
+    if (rc) return rc;
+    HFX_CUDA(cudaMemcpyAsync(out_s, d_os, 4ull * nspec * topn, cudaMemcpyDeviceToHost, st), "D2H score");
+    HFX_CUDA(cudaMemcpyAsync(out_k, d_ok, 8ull * nspec * topn, cudaMemcpyDeviceToHost, st), "D2H key");
+    if (out_pep) HFX_CUDA(cudaMemcpyAsync(out_pep, d_op, 4ull * nspec * topn, cudaMemcpyDeviceToHost, st), "D2H pep");
+    if (out_ncand) HFX_CUDA(cudaMemcpyAsync(out_ncand, d_nc, 8ull * nspec, cudaMemcpyDeviceToHost, st), "D2H nc");
+    HFX_CUDA(cudaStreamSynchronize(st), "sync");
+    return HFX_OK;
+}
+
+int32_t hfx_preprocess(hfx_ctx *ctx, const hfx_search_params *p, const float *mz, const float *it,
+                       const int64_t *off, const float *pcr, const float *z, int32_t nspec, int64_t stride,
+                       float *rows, void *rows_bf16, void *rows_fp16, int32_t *lens, float *masses) {
+    if (!ctx || !p || nspec < 0 || !rows) return fail(ctx, HFX_ERR_ARG, "bad hfx_preprocess arguments");
+    if (nspec == 0) return HFX_OK;
+    HFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaError_t e;
+    LayoutParams lp = layout_params(p);
+    lp.max_len = (int32_t)std::min<int64_t>(stride, lp.max_len > stride ? stride : lp.max_len);
+    lp.max_len = (int32_t)stride;
+    SpecMeta *meta = ctx->buf<SpecMeta>("meta", nspec, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    uint32_t *d_max = ctx->buf<uint32_t>("maxlen", 4, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    float *tol = ctx->buf<float>("tol0", nspec, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    HFX_CUDA(cudaMemsetAsync(tol, 0, 4ull * nspec, ctx->stream), "memset");
+    int rc = hfx_launch_layout(mz, off, pcr, z, tol, nspec, lp, meta, d_max, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_layout");
+    rc = hfx_launch_preprocess(mz, it, off, pcr, lp, meta, nspec, stride, rows, (__nv_bfloat16 *)rows_bf16,
+                               (__half *)rows_fp16, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_preprocess");
+    std::vector<SpecMeta> hm(nspec);
+    HFX_CUDA(cudaMemcpyAsync(hm.data(), meta, sizeof(SpecMeta) * nspec, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    std::vector<int32_t> hl(nspec);
+    std::vector<float> hmass(nspec);
+    for (int32_t s = 0; s < nspec; ++s) {
+        hl[s] = hm[s].status == 0 ? hm[s].len : 0;
+        hmass[s] = hm[s].mass;
+    }
+    if (lens) HFX_CUDA(cudaMemcpy(lens, hl.data(), 4ull * nspec, cudaMemcpyHostToDevice), "H2D lens");
+    if (masses) HFX_CUDA(cudaMemcpy(masses, hmass.data(), 4ull * nspec, cudaMemcpyHostToDevice), "H2D masses");
+    return HFX_OK;
+}
+
+int32_t hfx_find_windows(hfx_ctx *ctx, const hfx_search_params *p, const float *mz, const int64_t *off,
+                         const float *pcr, const float *z, const float *tol, int32_t nspec, uint32_t *begin,
+                         uint32_t *end) {
+    if (!ctx || !p || nspec < 0 || !begin || !end) return fail(ctx, HFX_ERR_ARG, "bad hfx_find_windows arguments");
+    if (nspec == 0) return HFX_OK;
+    HFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaError_t e;
+    const LayoutParams lp = layout_params(p);
+    SpecMeta *meta = ctx->buf<SpecMeta>("meta", nspec, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    uint32_t *d_max = ctx->buf<uint32_t>("maxlen", 4, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    int rc = hfx_launch_layout(mz, off, pcr, z, tol, nspec, lp, meta, d_max, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_layout");
+    rc = hfx_launch_windows(ctx->d_r.as<float>(), (uint32_t)ctx->num_pep, meta, nspec, begin, end, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_windows");
+    HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    return HFX_OK;
+}
+
+int32_t hfx_ion_bins(hfx_ctx *ctx, const uint32_t *pos, const int32_t *charges, const int32_t *lens, int32_t n,
+                     int32_t cap, int32_t fastdiv, uint32_t *bins, uint8_t *levels, int32_t *count) {
+    if (!ctx || n < 0 || !pos || !charges || !lens || !bins || !levels || !count)
+        return fail(ctx, HFX_ERR_ARG, "bad hfx_ion_bins arguments");
+    if (n == 0) return HFX_OK;
+    HFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    int rc = hfx_launch_ion_bins(ctx->devdb(), pos, charges, lens, n, kMaxWords * 32, cap, fastdiv, bins, levels,
+                                 count, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_ion_bins");
+    HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    return HFX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,161 @@
+/*
+ * hfx_gpu.h -- C ABI of the GB300 SEQUEST search engine (libhfx_gpu.so).
+ *
+ * This is the drop-in boundary for the search path of kevyin/hfx.  In the
+ * reference the Haskell host calls CUDA through `foreign import ccall`
+ * (src/haskell/Foreign/CUDA/Algorithms.hs:44-371) into the functions declared
+ * in src/common/include/algorithms.h:80-325, plus cuBLAS sgemv called
+ * directly from Sequence/Search.hs:245 and :529.  Here the same work is
+ * behind a context-based API: plain pointers and sizes, int32 status codes,
+ * no C++ or torch types.  Each function names the reference interface it
+ * replaces.
+ *
+ * Status codes: every call returns HFX_OK or an error; hfx_last_error()
+ * gives the message.  (The reference checks no errors: utils.h:27-76.)
+ */
+#ifndef HFX_GPU_H
+#define HFX_GPU_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HFX_OK 0
+#define HFX_ERR_ARG 1
+#define HFX_ERR_OOM 2
+#define HFX_ERR_CUDA 3
+#define HFX_ERR_TIMEOUT 4
+#define HFX_ERR_UNSUPPORTED 5
+
+typedef struct hfx_ctx hfx_ctx;
+
+/* Search parameters: the hfx.params / command-line keys that reach the
+ * search path (Config.hs:55-104), plus the keys of the new engine. */
+typedef struct hfx_search_params {
+    float bin_width;               /* Correlation.hs:29-30: 1.0005079 mono, 1.0011413 average */
+    int32_t custom_bin_width;      /* 1: bin_width is a custom width (e.g. 0.02 Da)           */
+    int32_t remove_precursor_peak; /* remove-precursor-peak (Config.hs:312-317)               */
+    int32_t tol_ppm;               /* 0: mass-tolerance in Da (Config.hs:308); 1: ppm          */
+    int32_t top_n;                 /* matches kept per spectrum, 1..32                         */
+    int32_t precision;             /* 0 FP32 rows; 1 BF16 rows + FP32 rescore; 2 FP16 + rescore */
+    int32_t rescore_k;             /* candidates rescored in FP32 (>= top_n, <= 32)            */
+    int32_t batch_mode;            /* 0 one launch per spectrum; 1 persistent batched launch   */
+    int32_t fastdiv;               /* 1: __fdividef in ion m/z, as ion_series.cu:59-69         */
+    int32_t search_plain;          /* score unmodified candidates                              */
+    int32_t search_mods;           /* score variable-modification isoforms (needs hfx_set_mods) */
+    int32_t group_size;            /* spectra per batched work item (1..8), 0 = default       */
+    int32_t chunk;                 /* candidates per batched work item, 0 = default            */
+    int32_t max_len;               /* longest spectrum row accepted, 0 = default               */
+} hfx_search_params;
+
+/* Fill p with the engine defaults (reference behaviour where it has one). */
+void hfx_default_params(hfx_search_params *p);
+
+/* Create a context on CUDA device `device`.  All work is issued on the
+ * context's stream (hfx_set_stream).  Replaces Execution.hs:49-53
+ * withExecutionPlan (cuBLAS handle + streams). */
+int32_t hfx_ctx_create(int32_t device, hfx_ctx **out);
+int32_t hfx_ctx_destroy(hfx_ctx *ctx);
+/* stream: a cudaStream_t passed as a pointer; NULL = the context's own. */
+int32_t hfx_set_stream(hfx_ctx *ctx, void *stream);
+const char *hfx_last_error(const hfx_ctx *ctx);
+
+/* Stage timing: with profiling on, every search records CUDA events around
+ * each stage on the context stream.  hfx_stage_stats returns, per stage,
+ * accumulated milliseconds, kernel launches and units processed (spectra,
+ * or peptide-spectrum pairs for the scoring stage).  New; the reference's
+ * only timer is CPU time around the whole search (Util/Time.hs:42-47). */
+#define HFX_STAGE_LAYOUT 0      /* per-spectrum layout, mass, window bounds */
+#define HFX_STAGE_PREPROCESS 1  /* stage (a)                                */
+#define HFX_STAGE_WINDOWS 2     /* stage (b), work planning                 */
+#define HFX_STAGE_SCORE 3       /* stages (c)+(d): ion ladders, gather-dot  */
+#define HFX_STAGE_TOPN 4        /* stage (e): top-N merge                   */
+#define HFX_STAGE_RESCORE 5     /* FP32 rescoring of the kept candidates    */
+#define HFX_STAGE_MODS 6        /* variable-modification isoforms           */
+#define HFX_NSTAGES 8
+int32_t hfx_set_profiling(hfx_ctx *ctx, int32_t on);
+int32_t hfx_stage_stats(hfx_ctx *ctx, double *ms, int64_t *launches, int64_t *units, int32_t reset);
+
+/* Digest proteins into the search database and upload it.  Replaces
+ * Fragment.hs:197-233 makeSeqDB + :239-258 withDeviceDB + sort.cu:28-35
+ * sort_idx_f + prepare_ions.cu:105-132 prepare_ions.  seq: concatenated
+ * upper-case residues, seg[nprot+1] protein offsets.  static_add26: add_X
+ * static modifications (Config.hs:204-218), mono: aa-mass-type.
+ * proline_rule / min_len / max_len extend the reference digest (its rule 1
+ * ignores P and it has no length filter; 0 = off). */
+int32_t hfx_build_db(hfx_ctx *ctx, const uint8_t *seq, const uint32_t *seg, int32_t nprot,
+                     const float *static_add26, int32_t mono, int32_t rule, int32_t missed,
+                     float min_mass, float max_mass, int32_t proline_rule, int32_t min_len,
+                     int32_t max_len);
+/* Host-only helpers (no device work), the two host steps of the database
+ * build: the digest of Fragment.hs:363-405 into r/tc/tn (returns the
+ * fragment count, -2 if cap is exceeded; pass r = NULL to count), and the
+ * residue packing of prepare_ions.cu:29-52 (byte = (c-'A') | (ma index+1)<<5). */
+int64_t hfx_digest(const uint8_t *seq, const uint32_t *seg, int32_t nprot, const float *mass_table26,
+                   int32_t rule, int32_t missed, float min_mass, float max_mass, int32_t proline_rule,
+                   int32_t min_len, int32_t max_len, float *r, uint32_t *tc, uint32_t *tn, int64_t cap);
+int32_t hfx_pack_ions(const uint8_t *ascii, uint64_t n, const uint8_t *ma, int32_t num_ma, uint8_t *out);
+
+/* Upload a prebuilt database (r, tc, tn per fragment, ASCII residues) --
+ * the SequenceDB fields of Fragment.hs:151-158. */
+int32_t hfx_upload_db(hfx_ctx *ctx, const uint8_t *ions_ascii, uint64_t num_ions, const float *r,
+                      const uint32_t *tc, const uint32_t *tn, uint64_t num_pep,
+                      const float *mass_table26);
+/* Database sizes and host copies in residual-mass order. */
+int32_t hfx_db_info(const hfx_ctx *ctx, uint64_t *num_ions, uint64_t *num_pep);
+int32_t hfx_db_export(const hfx_ctx *ctx, float *r, uint32_t *tc, uint32_t *tn, uint32_t *idx_sorted,
+                      float *mass_table26);
+
+/* Variable modifications: mod_X keys (Config.hs:204-218) and
+ * max-modable-acids; builds the combination table of Fragment.hs:260-289
+ * and repacks the residues (prepare_ions.cu:105-132).  num_ma = 0 clears.
+ * per_type selects the i-th acid counter: 0 = the reference kernel's
+ * (mion_series.cu:252-269), 1 = per acid type (check_series.cu:62-100). */
+int32_t hfx_set_mods(hfx_ctx *ctx, int32_t num_ma, const uint8_t *ma, const float *ma_mass,
+                     int32_t max_ma, int32_t per_type);
+int32_t hfx_mod_table(const hfx_ctx *ctx, int32_t *num_mod, int32_t *counts, float *deltas,
+                      int32_t cap);
+
+/* Full search of a batch of spectra, HOST buffers in and out (the host
+ * copies are part of the call).  Replaces Search.hs:98-124 searchForMatches
+ * (stages a-e and the per-spectrum sort).  Spectrum i has peaks
+ * [off[i], off[i+1]) of mz/it (sorted by m/z), precursor m/z pcr[i],
+ * charge z[i], tolerance tol[i].  Outputs, top_n per spectrum in final
+ * order: score (raw XCorr; the displayed value is score/10000,
+ * Search.hs:122), key (position in mass order for plain matches;
+ * 1<<63 | mod<<54 | position<<27 | isoform rank for modified ones), pep
+ * (fragment index), ncand[i] = candidates scored. */
+int32_t hfx_search_host(hfx_ctx *ctx, const hfx_search_params *p, const float *mz, const float *it,
+                        const int64_t *off, const float *pcr, const float *z, const float *tol,
+                        int32_t nspec, float *out_score, uint64_t *out_key, uint32_t *out_pep,
+                        int64_t *out_ncand);
+/* The same with DEVICE buffers (inputs resident in HBM). */
+int32_t hfx_search_device(hfx_ctx *ctx, const hfx_search_params *p, const float *mz, const float *it,
+                          const int64_t *off, const float *pcr, const float *z, const float *tol,
+                          int32_t nspec, float *out_score, uint64_t *out_key, uint32_t *out_pep,
+                          int64_t *out_ncand);
+
+/* Stage (a) alone, device buffers: Correlation.hs:37-109 sequestXCorr.
+ * rows[nspec][stride] FP32 (+ optional BF16 / FP16 copies), lens[nspec]
+ * (0 for a rejected spectrum), masses[nspec] = ms2Mass (Data.hs:58-59). */
+int32_t hfx_preprocess(hfx_ctx *ctx, const hfx_search_params *p, const float *mz, const float *it,
+                       const int64_t *off, const float *pcr, const float *z, int32_t nspec,
+                       int64_t stride, float *rows, void *rows_bf16, void *rows_fp16, int32_t *lens,
+                       float *masses);
+/* Stage (b) alone, device buffers: filter.cu:75-127 findSpecCandsByMass
+ * (windows in residual-mass order, end exclusive). */
+int32_t hfx_find_windows(hfx_ctx *ctx, const hfx_search_params *p, const float *mz, const int64_t *off,
+                         const float *pcr, const float *z, const float *tol, int32_t nspec,
+                         uint32_t *begin, uint32_t *end);
+/* Stage (c) alone, device buffers: the distinct ion bins of candidates at
+ * mass-order positions pos[n] (ion_series.cu:150-232 addIons without the
+ * dense row): bins ascending, level 1/2/3 = intensity 10/25/50, capped at
+ * cap per candidate; count[i] may exceed cap. */
+int32_t hfx_ion_bins(hfx_ctx *ctx, const uint32_t *pos, const int32_t *charges, const int32_t *lens,
+                     int32_t n, int32_t cap, int32_t fastdiv, uint32_t *bins, uint8_t *levels,
+                     int32_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

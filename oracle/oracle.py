@@ -1,0 +1,216 @@
+"""ctypes bindings of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg import
+this module.  It is the checker: it restates the reference's arithmetic on
+the CPU (see hfx_oracle.h for the reference files it follows).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "libhfx_oracle.so")
+_lib = None
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("bw", C.c_float), ("custom_bw", C.c_int32), ("remove_pcr", C.c_int32), ("ppm", C.c_int32),
+        ("topn", C.c_int32), ("prec", C.c_int32), ("num_ma", C.c_int32), ("max_ma", C.c_int32),
+        ("per_type", C.c_int32), ("plain", C.c_int32), ("ma", C.c_uint8 * 16), ("ma_mass", C.c_float * 16),
+    ]
+
+
+def build():
+    r = subprocess.run(["make", "-C", HERE], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(r.stdout + r.stderr)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = C.CDLL(LIB)
+        P = C.c_void_p
+        i32, i64, f32 = C.c_int32, C.c_int64, C.c_float
+        sig = {
+            "hfxo_mass_table": (None, [i32, P, P]),
+            "hfxo_digest": (i64, [P, P, i32, P, i32, i32, f32, f32, i32, i32, i32, P, P, P, i64]),
+            "hfxo_sort_idx": (None, [P, i64, P]),
+            "hfxo_pack_ions": (None, [P, i64, P, i32, i32]),
+            "hfxo_ms2_mass": (f32, [f32, f32]),
+            "hfxo_spec_len": (i32, [P, i32, f32, f32, f32, i32]),
+            "hfxo_preprocess": (i32, [P, P, i32, f32, f32, f32, i32, i32, P, P, i32]),
+            "hfxo_windows": (None, [P, i64, P, P, i64, P, P]),
+            "hfxo_ion_bins": (i32, [P, P, C.c_uint32, C.c_uint32, f32, i32, i32, P, P, P, P, i32]),
+            "hfxo_ion_charges": (i32, [f32, i32]),
+            "hfxo_score32": (f32, [P, P, i32, P]),
+            "hfxo_score64": (C.c_double, [P, P, i32, P]),
+            "hfxo_choose": (C.c_uint32, [C.c_uint32, C.c_uint32]),
+            "hfxo_unrank_comb": (None, [P, C.c_uint32, C.c_uint32, C.c_uint32]),
+            "hfxo_mod_combos": (i32, [i32, i32, P, P, P, P, i32]),
+            "hfxo_mod_isoform": (C.c_uint32, [P, C.c_uint32, C.c_uint32, P, i32, P, C.c_uint32, i32, P, P]),
+            "hfxo_search": (i32, [P, P, P, P, P, P, i64, P, P, P, P, P, P, i32, C.POINTER(Params), i32,
+                                  P, P, P, P, P]),
+        }
+        for k, (res, args) in sig.items():
+            f = getattr(L, k)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def mass_table(mono=True, static_add=None):
+    add = np.zeros(26, np.float32) if static_add is None else np.ascontiguousarray(static_add, np.float32)
+    out = np.empty(26, np.float32)
+    lib().hfxo_mass_table(int(mono), _p(add), _p(out))
+    return out
+
+
+def digest(seq, seg, mt, rule=1, missed=2, min_mass=400.0, max_mass=7200.0, proline_rule=False, min_len=0,
+           max_len=0):
+    seq = np.ascontiguousarray(seq, np.uint8)
+    seg = np.ascontiguousarray(seg, np.uint32)
+    cap = int(len(seq) * (missed + 1) + 16)
+    r = np.empty(cap, np.float32)
+    tc = np.empty(cap, np.uint32)
+    tn = np.empty(cap, np.uint32)
+    n = lib().hfxo_digest(_p(seq), _p(seg), len(seg) - 1, _p(np.ascontiguousarray(mt, np.float32)), rule, missed,
+                          min_mass, max_mass, int(proline_rule), min_len, max_len, _p(r), _p(tc), _p(tn), cap)
+    assert n >= 0
+    return r[:n].copy(), tc[:n].copy(), tn[:n].copy()
+
+
+def sort_idx(r):
+    r = np.ascontiguousarray(r, np.float32)
+    idx = np.empty(len(r), np.uint32)
+    lib().hfxo_sort_idx(_p(r), len(r), _p(idx))
+    return idx
+
+
+def pack_ions(seq, ma=b"", quirk=False):
+    out = np.array(seq, np.uint8, copy=True)
+    mab = np.frombuffer(ma, np.uint8).copy() if ma else np.zeros(1, np.uint8)
+    lib().hfxo_pack_ions(_p(out), len(out), _p(mab), len(ma), int(quirk))
+    return out
+
+
+def ms2_mass(pcr, z):
+    return lib().hfxo_ms2_mass(float(pcr), float(z))
+
+
+def preprocess(mz, it, pcr, z, bw=1.0005079, custom_bw=False, remove_pcr=True, fp64=False):
+    mz = np.ascontiguousarray(mz, np.float32)
+    it = np.ascontiguousarray(it, np.float32)
+    L = lib().hfxo_spec_len(_p(mz), len(mz), float(pcr), float(z), float(bw), int(custom_bw))
+    if L < 0:
+        return None
+    o32 = np.empty(L, np.float32)
+    o64 = np.empty(L, np.float64) if fp64 else None
+    n = lib().hfxo_preprocess(_p(mz), _p(it), len(mz), float(pcr), float(z), float(bw), int(custom_bw),
+                              int(remove_pcr), _p(o32), _p(o64), L)
+    if n < 0:
+        return None
+    return (o32, o64) if fp64 else o32
+
+
+def windows(r_sorted, lo, hi):
+    r_sorted = np.ascontiguousarray(r_sorted, np.float32)
+    lo = np.ascontiguousarray(lo, np.float32)
+    hi = np.ascontiguousarray(hi, np.float32)
+    b = np.empty(len(lo), np.uint32)
+    e = np.empty(len(lo), np.uint32)
+    lib().hfxo_windows(_p(r_sorted), len(r_sorted), _p(lo), _p(hi), len(lo), _p(b), _p(e))
+    return b, e
+
+
+def ion_charges(z, is_mod=False):
+    return lib().hfxo_ion_charges(float(z), int(is_mod))
+
+
+def ion_bins(ions_packed, mt, tc, tn, residual, charges, length, res_add=None, modded=None, cap=65536):
+    bins = np.empty(cap, np.uint32)
+    lvl = np.empty(cap, np.uint8)
+    n = lib().hfxo_ion_bins(_p(ions_packed), _p(np.ascontiguousarray(mt, np.float32)), int(tc), int(tn),
+                            float(residual), int(charges), int(length), _p(res_add), _p(modded), _p(bins),
+                            _p(lvl), cap)
+    assert n >= 0
+    return bins[:n].copy(), lvl[:n].copy()
+
+
+def score32(bins, lvl, x):
+    return lib().hfxo_score32(_p(bins), _p(lvl), len(bins), _p(np.ascontiguousarray(x, np.float32)))
+
+
+def score64(bins, lvl, x):
+    return lib().hfxo_score64(_p(bins), _p(lvl), len(bins), _p(np.ascontiguousarray(x, np.float64)))
+
+
+def choose(n, k):
+    return lib().hfxo_choose(n, k)
+
+
+def unrank_comb(n, k, rank):
+    out = np.zeros(max(k, 1), np.uint32)
+    lib().hfxo_unrank_comb(_p(out), n, k, rank)
+    return out[:k].copy()
+
+
+def mod_combos(ma_mass, max_ma):
+    ma_mass = np.ascontiguousarray(ma_mass, np.float32)
+    cap = 1 << 16
+    counts = np.empty(cap * max(1, len(ma_mass)), np.int32)
+    sums = np.empty(cap, np.int32)
+    deltas = np.empty(cap, np.float32)
+    n = lib().hfxo_mod_combos(len(ma_mass), max_ma, _p(ma_mass), _p(counts), _p(sums), _p(deltas), cap)
+    return counts[: n * len(ma_mass)].reshape(n, len(ma_mass)).copy(), sums[:n].copy(), deltas[:n].copy()
+
+
+def mod_isoform(ions_packed, tc, tn, ma, mod_counts, rank=None, per_type=False):
+    """(isoform count, unrank row, modified flags) of one (peptide, mod)."""
+    mab = np.frombuffer(ma, np.uint8).copy()
+    mc = np.ascontiguousarray(mod_counts, np.int32)
+    if rank is None:
+        n = lib().hfxo_mod_isoform(_p(ions_packed), tc, tn, _p(mab), len(ma), _p(mc), 0xFFFFFFFF, int(per_type),
+                                   None, None)
+        return n, None, None
+    un = np.zeros(64, np.uint32)
+    md = np.zeros(max(1, tn - tc), np.uint8)
+    n = lib().hfxo_mod_isoform(_p(ions_packed), tc, tn, _p(mab), len(ma), _p(mc), rank, int(per_type), _p(un),
+                               _p(md))
+    return n, un[: int(mc.sum())].copy(), md[: tn - tc].copy()
+
+
+def search(ions_packed, mt, r, tc, tn, idx, spectra, bw=1.0005079, custom_bw=False, remove_pcr=True, ppm=False,
+           topn=10, prec=0, ma=b"", ma_mass=(), max_ma=0, per_type=False, plain=True, nthreads=0):
+    """Full search (Search.hs:98-124); returns (score, score64, key, pep, ncand)."""
+    mz, it, off, pcr, z, tol = spectra.arrays()
+    p = Params()
+    p.bw, p.custom_bw, p.remove_pcr, p.ppm = bw, int(custom_bw), int(remove_pcr), int(ppm)
+    p.topn, p.prec, p.num_ma, p.max_ma, p.per_type, p.plain = topn, prec, len(ma), max_ma, int(per_type), int(plain)
+    for i, c in enumerate(ma):
+        p.ma[i] = c
+        p.ma_mass[i] = ma_mass[i]
+    ns = len(pcr)
+    sc = np.empty((ns, topn), np.float32)
+    s64 = np.empty((ns, topn), np.float64)
+    key = np.empty((ns, topn), np.uint64)
+    pep = np.empty((ns, topn), np.uint32)
+    nc = np.empty(ns, np.int64)
+    rc = lib().hfxo_search(_p(ions_packed), _p(np.ascontiguousarray(mt, np.float32)), _p(r), _p(tc), _p(tn),
+                           _p(idx), len(r), _p(mz), _p(it), _p(off), _p(pcr), _p(z), _p(tol), ns, C.byref(p),
+                           nthreads, _p(sc), _p(s64), _p(key), _p(pep), _p(nc))
+    if rc != 0:
+        raise RuntimeError(f"oracle search status {rc}")
+    return sc, s64, key, pep, nc

@@ -1,0 +1,190 @@
+"""GPU parity tests: the CUDA path, called through the C ABI, against the
+oracle on the same seeded inputs.  Integer / index / ordering results must
+be bit-exact; FP32 scores and rows are bit-exact too because the kernels
+follow the oracle's canonical operation order."""
+import numpy as np
+import pytest
+
+from hfx_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _dev(sp):
+    d = torch.device("cuda:0")
+    return dict(mz=torch.from_numpy(sp.mz).to(d), it=torch.from_numpy(sp.it).to(d),
+                off=torch.from_numpy(sp.off).to(d), pcr=torch.from_numpy(sp.pcr).to(d),
+                z=torch.from_numpy(sp.z).to(d), tol=torch.from_numpy(sp.tol).to(d))
+
+
+def _engine(prot, digest=None):
+    import hfx_gb300
+    eng = hfx_gb300.Engine(0)
+    eng.build_db(prot.seq, prot.seg, static_add=synth.static_mods(), **(digest or synth.DIGEST))
+    return eng
+
+
+@pytest.fixture(scope="module")
+def tiny_engine(gpulib, tiny):
+    prot, sp, cfg = tiny
+    eng = _engine(prot)
+    yield eng, prot, sp
+    eng.close()
+
+
+@pytest.fixture(scope="module")
+def full_engine(gpulib):
+    prot = synth.proteins(20000, seed=1)
+    sp = synth.spectra(prot, 240, seed=101, charge_p={1: 0.05, 2: 0.5, 3: 0.35, 4: 0.10}, npeaks=(50, 400))
+    eng = _engine(prot)
+    yield eng, prot, sp
+    eng.close()
+
+
+def _oracle_db(oracle, eng, prot, ma=b""):
+    r, tc, tn, idx, mt = eng.db_export()
+    ions = oracle.pack_ions(prot.seq, ma)
+    return ions, mt, r, tc, tn, idx
+
+
+def test_preprocess_bitexact(tiny_engine, oracle):
+    import hfx_gb300
+    eng, prot, sp = tiny_engine
+    p = hfx_gb300.default_params()
+    dev = _dev(sp)
+    stride = 4096
+    n = len(sp)
+    rows = torch.empty((n, stride), dtype=torch.float32, device="cuda")
+    rbf = torch.empty((n, stride), dtype=torch.bfloat16, device="cuda")
+    rh = torch.empty((n, stride), dtype=torch.float16, device="cuda")
+    lens = torch.empty(n, dtype=torch.int32, device="cuda")
+    masses = torch.empty(n, dtype=torch.float32, device="cuda")
+    eng.preprocess(dev, p, stride, rows, rbf, rh, lens, masses)
+    rows, lens, masses = rows.cpu().numpy(), lens.cpu().numpy(), masses.cpu().numpy()
+    rbf = rbf.float().cpu().numpy()
+    rh = rh.float().cpu().numpy()
+    for i in range(n):
+        a, b = sp.off[i], sp.off[i + 1]
+        x = oracle.preprocess(sp.mz[a:b], sp.it[a:b], sp.pcr[i], sp.z[i])
+        assert lens[i] == len(x)
+        assert np.array_equal(rows[i, :len(x)].view(np.uint32), x.view(np.uint32)), i
+        assert not rows[i, len(x):].any()
+        assert np.array_equal(rbf[i, :len(x)], torch.from_numpy(x).bfloat16().float().numpy())
+        assert np.array_equal(rh[i, :len(x)], x.astype(np.float16).astype(np.float32))
+        assert masses[i] == np.float32(oracle.ms2_mass(sp.pcr[i], sp.z[i]))
+
+
+def test_windows_exact(full_engine, oracle):
+    import hfx_gb300
+    eng, prot, sp = full_engine
+    r, tc, tn, idx, mt = eng.db_export()
+    rs = r[idx]
+    for tol in (3.0, 0.5, 0.01):
+        sp.tol[:] = tol
+        dev = _dev(sp)
+        b = torch.empty(len(sp), dtype=torch.int32, device="cuda")
+        e = torch.empty(len(sp), dtype=torch.int32, device="cuda")
+        eng.find_windows(dev, hfx_gb300.default_params(), b, e)
+        m = np.array([oracle.ms2_mass(p, z) for p, z in zip(sp.pcr, sp.z)], np.float32)
+        ob, oe = oracle.windows(rs, (m - np.float32(tol)).astype(np.float32), (m + np.float32(tol)).astype(np.float32))
+        assert np.array_equal(b.cpu().numpy().astype(np.uint32), ob)
+        assert np.array_equal(e.cpu().numpy().astype(np.uint32), oe)
+    sp.tol[:] = 3.0
+
+
+@pytest.mark.parametrize("fastdiv", [False, True])
+def test_ion_bins(full_engine, oracle, fastdiv):
+    eng, prot, sp = full_engine
+    ions, mt, r, tc, tn, idx = _oracle_db(oracle, eng, prot)
+    rng = np.random.Generator(np.random.PCG64(21))
+    n = 3000
+    pos = rng.integers(0, len(r), n).astype(np.uint32)
+    pos[:50] = np.argsort(tn[idx] - tc[idx])[-50:]          # the longest peptides
+    ch = rng.integers(1, 5, n).astype(np.int32)
+    lens = rng.integers(200, 4000, n).astype(np.int32)
+    cap = 4096
+    d = torch.device("cuda")
+    bins = torch.zeros((n, cap), dtype=torch.int32, device=d)
+    lvl = torch.zeros((n, cap), dtype=torch.uint8, device=d)
+    cnt = torch.zeros(n, dtype=torch.int32, device=d)
+    eng.ion_bins(torch.from_numpy(pos.astype(np.int32)).to(d), torch.from_numpy(ch).to(d),
+                 torch.from_numpy(lens).to(d), cap, bins, lvl, cnt, fastdiv=fastdiv)
+    bins, lvl, cnt = bins.cpu().numpy(), lvl.cpu().numpy(), cnt.cpu().numpy()
+    mismatch = 0
+    for i in range(n):
+        p = idx[pos[i]]
+        ob, ol = oracle.ion_bins(ions, mt, tc[p], tn[p], r[p], int(ch[i]), int(lens[i]))
+        same = cnt[i] == len(ob) and np.array_equal(bins[i, :cnt[i]].view(np.uint32), ob) and \
+            np.array_equal(lvl[i, :cnt[i]], ol)
+        if not fastdiv:
+            assert same, i
+        mismatch += not same
+    if fastdiv:
+        # __fdividef moves bins that sit within ~2 ulp of a half-bin edge
+        print(f"fastdiv: {mismatch}/{n} candidates differ from IEEE division")
+        assert mismatch < 0.2 * n
+
+
+def _compare(res, ref, label):
+    sc, _, key, pep, nc = ref
+    assert np.array_equal(res.ncand, nc), label
+    assert np.array_equal(res.key, key), label
+    assert np.array_equal(res.score.view(np.uint32), sc.view(np.uint32)), label
+    assert np.array_equal(res.pep, pep), label
+
+
+def test_search_plain_tiny(tiny_engine, oracle):
+    import hfx_gb300
+    eng, prot, sp = tiny_engine
+    ref = oracle.search(*_oracle_db(oracle, eng, prot), sp, topn=10)
+    res = eng.search(sp, hfx_gb300.default_params(top_n=10))
+    _compare(res, ref, "tiny")
+
+
+def test_search_plain_full_subset(full_engine, oracle):
+    import hfx_gb300
+    eng, prot, sp = full_engine
+    ref = oracle.search(*_oracle_db(oracle, eng, prot), sp, topn=10)
+    res = eng.search(sp, hfx_gb300.default_params(top_n=10))
+    _compare(res, ref, "full")
+    res32 = eng.search(sp, hfx_gb300.default_params(top_n=32))
+    ref32 = oracle.search(*_oracle_db(oracle, eng, prot), sp, topn=32)
+    _compare(res32, ref32, "full top32")
+
+
+def test_search_deterministic(full_engine):
+    import hfx_gb300
+    eng, prot, sp = full_engine
+    p = hfx_gb300.default_params(top_n=10)
+    a = eng.search(sp, p)
+    b = eng.search(sp, p)
+    assert np.array_equal(a.score.view(np.uint32), b.score.view(np.uint32))
+    assert np.array_equal(a.key, b.key)
+
+
+def test_search_edge_cases(tiny_engine, oracle):
+    """Empty spectrum, empty window, charge without ions (max charge > 4
+    scores 0 in the reference's plain kernel), a one-peak spectrum."""
+    import hfx_gb300
+    eng, prot, sp = tiny_engine
+    sub = sp.subset(np.arange(6))
+    mz, it, off = [], [], [0]
+    for i in range(6):
+        a, b = sub.off[i], sub.off[i + 1]
+        if i == 0:
+            a = b                                   # empty spectrum
+        if i == 3:
+            a = b - 1                               # one peak
+        mz.append(sub.mz[a:b])
+        it.append(sub.it[a:b])
+        off.append(off[-1] + (b - a))
+    sub.mz, sub.it, sub.off = np.concatenate(mz), np.concatenate(it), np.array(off, np.int64)
+    sub.tol[1] = 1e-7                               # (almost) empty window
+    sub.z[2] = 6.0                                  # max charge 5: no ions
+    ref = oracle.search(*_oracle_db(oracle, eng, prot), sub, topn=10)
+    res = eng.search(sub, hfx_gb300.default_params(top_n=10))
+    _compare(res, ref, "edges")
+    assert res.ncand[0] == 0
+    assert (res.score[2][res.key[2] != np.iinfo(np.uint64).max] == 0).all()

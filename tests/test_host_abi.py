@@ -1,0 +1,79 @@
+"""CPU tests of the C ABI library: it loads, exports every symbol the
+public header declares, and its host-side database steps (digest, residue
+packing) match the oracle.  No device work."""
+import os
+import re
+import subprocess
+
+import numpy as np
+
+from hfx_gb300 import synth
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared(header):
+    text = open(os.path.join(ROOT, "include", header)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(hfx_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(gpulib):
+    import hfx_gb300
+    nm = subprocess.run(["nm", "-D", "--defined-only", hfx_gb300.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (hfx_[a-z0-9_]+)\b", nm))
+    for h in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        for sym in _declared(h):
+            assert sym in exported, (h, sym)
+            assert hasattr(gpulib, sym)
+    assert set(hfx_gb300.EXPORTED) <= exported
+
+
+def test_product_digest_matches_oracle(gpulib, oracle, tiny):
+    import hfx_gb300
+    prot, _, _ = tiny
+    for mono, rule, missed, pr, lo, hi in [(True, 1, 1, True, 6, 50), (True, 1, 2, False, 0, 0),
+                                           (False, 2, 0, False, 0, 0), (True, 0, 0, False, 0, 0),
+                                           (True, 13, 1, True, 3, 30)]:
+        mt = oracle.mass_table(mono, synth.static_mods())
+        a = hfx_gb300.digest(prot.seq, prot.seg, mt, rule=rule, missed=missed, proline_rule=pr, min_len=lo,
+                             max_len=hi)
+        b = oracle.digest(prot.seq, prot.seg, mt, rule=rule, missed=missed, proline_rule=pr, min_len=lo,
+                          max_len=hi)
+        for x, y in zip(a, b):
+            assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
+def test_digest_terminal_convention(gpulib, oracle):
+    """Fragment.hs:383-390: a fragment ending at a cleavage site stores the
+    index of its last residue; the last piece of a protein stores one past."""
+    import hfx_gb300
+    seq = np.frombuffer(b"AAAAKGGGGGGRCCCCCCCCCC", np.uint8)
+    seg = np.array([0, len(seq)], np.uint32)
+    mt = oracle.mass_table(True)
+    r, tc, tn = hfx_gb300.digest(seq, seg, mt, rule=1, missed=0, min_mass=0.0, max_mass=1e9)
+    assert list(zip(tc, tn)) == [(0, 4), (5, 11), (12, 22)]
+
+
+def test_product_packing_matches_reference(gpulib, golden):
+    import hfx_gb300
+    g = golden("ref_prepare_ions.npz")
+    for key in g.files:
+        if key.startswith("packed_"):
+            ma = key[len("packed_"):]
+            ma = b"" if ma == "none" else ma.encode()
+            assert np.array_equal(hfx_gb300.pack_ions(g["seq"], ma), g[key]), key
+
+
+def test_no_cpu_fallback_without_library(tmp_path):
+    import hfx_gb300
+    try:
+        hfx_gb300._lib_saved = hfx_gb300._lib
+        hfx_gb300._lib = None
+        try:
+            hfx_gb300.load_library(str(tmp_path / "missing.so"))
+            raise AssertionError("expected a loud failure")
+        except OSError:
+            pass
+    finally:
+        hfx_gb300._lib = hfx_gb300._lib_saved
