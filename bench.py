@@ -274,9 +274,9 @@ def main():
     eng.find_windows(dev, p, b_dev, e_dev)
     wb = b_dev.cpu().numpy().astype(np.int64)
     we = e_dev.cpu().numpy().astype(np.int64)
-    rows = torch.empty((ns, 4096), dtype=torch.float32, device=d)
+    rows = torch.empty((ns, 8192), dtype=torch.float32, device=d)
     lens_d = torch.empty(ns, dtype=torch.int32, device=d)
-    eng.preprocess(dev, p, 4096, rows, None, None, lens_d, None)
+    eng.preprocess(dev, p, 8192, rows, None, None, lens_d, None)
     lens = lens_d.cpu().numpy().astype(np.int64)
     del rows
     charges = np.array([_charges(z) for z in sp.z], np.int64)

@@ -8,6 +8,7 @@
 // with the per-spectrum Haskell loops replaced by device kernels.
 #include "hfx_internal.h"
 #include "search_kernels.h"
+#include "batched.h"
 #include "../../include/hfx_gpu.h"
 
 #include <algorithm>
@@ -357,6 +358,88 @@ int32_t search_plain_per_spectrum(hfx_ctx *ctx, const hfx_search_params *p, cons
     return HFX_OK;
 }
 
+int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, const SpecMeta *meta,
+                       const float *rows, const void *rows_lo, int elem_kind, int64_t stride, float *out_s,
+                       uint64_t *out_k, uint32_t *out_pep, int64_t *out_ncand) {
+    cudaError_t e;
+    const int32_t ns = b.nspec;
+    const int32_t G = p->group_size > 0 ? p->group_size : 8;
+    const int32_t chunk = p->chunk > 0 ? p->chunk : 1024;
+    if (G != 1 && G != 2 && G != 4 && G != 8) return fail(ctx, HFX_ERR_ARG, "group_size must be 1, 2, 4 or 8");
+    const int32_t K = elem_kind == 0 ? p->top_n : std::max(p->top_n, std::min(p->rescore_k > 0 ? p->rescore_k : 32,
+                                                                               kMaxTopK));
+    if (stride > (int64_t)kMaxWords * 32) return fail(ctx, HFX_ERR_UNSUPPORTED, "spectrum rows longer than 8192 bins");
+    uint32_t *wb = ctx->buf<uint32_t>("wb", ns, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    uint32_t *we = ctx->buf<uint32_t>("we", ns, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    BatchedWs ws;
+    ws.hist = ctx->buf<uint32_t>("b_hist", kBucketCount + 1, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    ws.cursor = ctx->buf<uint32_t>("b_cursor", kBucketCount, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    uint32_t *scal = ctx->buf<uint32_t>("b_scal", 8, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    ws.n_sorted = scal;
+    ws.ngroups = scal + 1;
+    ws.total_items = scal + 2;
+    ws.counter = scal + 3;
+    ws.perm = ctx->buf<int32_t>("b_perm", ns, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    ws.groups = ctx->buf<GroupInfo>("b_groups", ns, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    ws.item_off = ctx->buf<uint32_t>("b_itemoff", ns + 1, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    ws.group_of = ctx->buf<int32_t>("b_groupof", ns, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    ws.slot_of = ctx->buf<int32_t>("b_slotof", ns, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    ctx->stage_begin(HFX_STAGE_WINDOWS);
+    int rc = hfx_launch_windows(ctx->d_r.as<float>(), (uint32_t)ctx->num_pep, meta, ns, wb, we, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_windows");
+    rc = hfx_batched_plan(meta, ns, wb, we, G, chunk, ws, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "plan");
+    ctx->stage_end(HFX_STAGE_WINDOWS, 7, ns);
+    uint32_t hs[4];
+    HFX_CUDA(cudaMemcpyAsync(hs, scal, 16, cudaMemcpyDeviceToHost, ctx->stream), "D2H plan");
+    HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    const uint32_t total_items = hs[2];
+    float *ps = ctx->buf<float>("part_s", (size_t)total_items * G * K + 1, e);
+    if (e) return cuda_fail(ctx, e, "alloc parts");
+    uint64_t *pk = ctx->buf<uint64_t>("part_k", (size_t)total_items * G * K + 1, e);
+    if (e) return cuda_fail(ctx, e, "alloc parts");
+    const DevDB db = ctx->devdb();
+    ctx->stage_begin(HFX_STAGE_SCORE);
+    rc = hfx_batched_score(db, elem_kind == 0 ? (const void *)rows : rows_lo, elem_kind, stride, meta, wb, we, ws,
+                           G, chunk, K, 8, 0, p->fastdiv, ps, pk, ctx->d_err.as<uint32_t>(), ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_batched");
+    ctx->stage_end(HFX_STAGE_SCORE, 1, 0);
+    float *ks = ctx->buf<float>("kept_s", (size_t)ns * K, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    uint64_t *kk = ctx->buf<uint64_t>("kept_k", (size_t)ns * K, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    ctx->stage_begin(HFX_STAGE_TOPN);
+    rc = hfx_batched_merge(ps, pk, ws, meta, ns, G, K, K, ks, kk, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_merge_items");
+    ctx->stage_end(HFX_STAGE_TOPN, 1, ns);
+    if (elem_kind == 0) {
+        rc = hfx_finish(ks, kk, ns, p->top_n, ctx->d_idx.as<uint32_t>(), wb, we, meta, out_s, out_k, out_pep,
+                        out_ncand, ctx->stream);
+        if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_finish");
+    } else {
+        ctx->stage_begin(HFX_STAGE_RESCORE);
+        rc = hfx_rescore(db, rows, stride, meta, ks, kk, ns, K, p->top_n, p->fastdiv, out_s, out_k, out_pep,
+                         ctx->stream);
+        if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_rescore");
+        ctx->stage_end(HFX_STAGE_RESCORE, 1, (int64_t)ns * K);
+        if (out_ncand) {
+            rc = hfx_ncand(wb, we, meta, ns, out_ncand, ctx->stream);
+            if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_ncand");
+        }
+    }
+    return HFX_OK;
+}
+
 int32_t search_device(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, float *out_s, uint64_t *out_k,
                       uint32_t *out_pep, int64_t *out_ncand) {
     int32_t rc = check_params(ctx, p);
@@ -373,7 +456,13 @@ int32_t search_device(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, 
     rc = run_stage_a(ctx, p, b, stride, meta, rows, rows_bf, rows_h, p->precision == 1, p->precision == 2);
     if (rc) return rc;
     if (p->search_mods && ctx->num_mod > 0) return fail(ctx, HFX_ERR_UNSUPPORTED, "modification search not built yet");
-    rc = search_plain_per_spectrum(ctx, p, b, meta, rows, stride, out_s, out_k, out_pep, out_ncand);
+    if (p->batch_mode)
+        rc = search_batched(ctx, p, b, meta, rows, p->precision == 1 ? (const void *)rows_bf : (const void *)rows_h,
+                            p->precision, stride, out_s, out_k, out_pep, out_ncand);
+    else if (p->precision != 0)
+        return fail(ctx, HFX_ERR_UNSUPPORTED, "per-spectrum launches use FP32 rows only");
+    else
+        rc = search_plain_per_spectrum(ctx, p, b, meta, rows, stride, out_s, out_k, out_pep, out_ncand);
     if (rc) return rc;
     uint32_t herr = 0;
     HFX_CUDA(cudaMemcpyAsync(&herr, ctx->d_err.p, 4, cudaMemcpyDeviceToHost, ctx->stream), "D2H err");

@@ -54,7 +54,7 @@ def test_preprocess_bitexact(tiny_engine, oracle):
     eng, prot, sp = tiny_engine
     p = hfx_gb300.default_params()
     dev = _dev(sp)
-    stride = 4096
+    stride = 8192
     n = len(sp)
     rows = torch.empty((n, stride), dtype=torch.float32, device="cuda")
     rbf = torch.empty((n, stride), dtype=torch.bfloat16, device="cuda")
@@ -188,3 +188,32 @@ def test_search_edge_cases(tiny_engine, oracle):
     _compare(res, ref, "edges")
     assert res.ncand[0] == 0
     assert (res.score[2][res.key[2] != np.iinfo(np.uint64).max] == 0).all()
+
+
+@pytest.mark.parametrize("G", [1, 2, 4, 8])
+def test_batched_fp32_bitexact(full_engine, oracle, G):
+    import hfx_gb300
+    eng, prot, sp = full_engine
+    ref = oracle.search(*_oracle_db(oracle, eng, prot), sp, topn=10)
+    res = eng.search(sp, hfx_gb300.default_params(top_n=10, batch_mode=1, group_size=G, chunk=512))
+    _compare(res, ref, f"batched G={G}")
+
+
+@pytest.mark.parametrize("precision", [1, 2])
+def test_batched_lowp_rescore_matches_fp32(full_engine, oracle, precision):
+    """BF16 / FP16 rows pick the kept candidates, FP32 rescoring restores the
+    exact FP32 scores: the top-10 equals the FP32 oracle's."""
+    import hfx_gb300
+    eng, prot, sp = full_engine
+    ref = oracle.search(*_oracle_db(oracle, eng, prot), sp, topn=10)
+    res = eng.search(sp, hfx_gb300.default_params(top_n=10, batch_mode=1, precision=precision, rescore_k=32))
+    _compare(res, ref, f"precision {precision}")
+
+
+def test_batched_tiny_and_edges(tiny_engine, oracle):
+    import hfx_gb300
+    eng, prot, sp = tiny_engine
+    ref = oracle.search(*_oracle_db(oracle, eng, prot), sp, topn=10)
+    for prec in (0, 1):
+        res = eng.search(sp, hfx_gb300.default_params(top_n=10, batch_mode=1, precision=prec))
+        _compare(res, ref, f"tiny batched prec={prec}")
