@@ -282,7 +282,8 @@ def main():
     charges = np.array([_charges(z) for z in sp.z], np.int64)
     bpp, meanU = _bytes_per_psm(eng, bsz, wb, we, lens, charges, (tc[idx], tn[idx]), rng)
     per_launch_ms = sc_ms / max(1, sc_launch)
-    per_launch_psm = sc_units / max(1, sc_launch)
+    # every pair of the step is scored by exactly one launch of the scorer
+    per_launch_psm = psm_step * a.steps / max(1, sc_launch)
     achieved = bpp * per_launch_psm / (per_launch_ms / 1000.0) / 1e9
     peak, peak_kind = _peaks()
     launches_per_step = sum(v[1] for v in stats.values()) / a.steps
