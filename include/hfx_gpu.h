@@ -155,6 +155,36 @@ int32_t hfx_ion_bins(hfx_ctx *ctx, const uint32_t *pos, const int32_t *charges, 
                      int32_t n, int32_t cap, int32_t fastdiv, uint32_t *bins, uint8_t *levels,
                      int32_t *count);
 
+/* Allocation-free scoring of ONE spectrum.  It has no counterpart in the
+ * reference.  It is for callers that cannot call cudaMalloc: code running
+ * inside another framework's memory pool or allocator hooks, host runtimes
+ * whose only device memory is what they were handed, and latency-critical
+ * paths that must not take the allocator's locks.  It needs no context; the
+ * caller passes every input and output as a device buffer:
+ *   ions, r_sorted, tc_sorted, tn_sorted, idx_sorted[num_pep]: the
+ *     database in residual-mass order (hfx_db_export gives the host copies,
+ *     hfx_pack_ions the packed residues); mass_table26 is a HOST array;
+ *   row[len]: the spectrum's FP32 row (hfx_preprocess), len <= 8192;
+ *   charges: ion charges 1..4 (0 = none); [begin, end): the candidate window
+ *     in mass order (hfx_find_windows);
+ *   out_score / out_key / out_pep[top_n]: the top_n matches in final order,
+ *     top_n <= 32, with the keys and scores of hfx_search_* (plain matches).
+ * Its only scratch is a file-scope device array of
+ * HFX_NOALLOC_MAX_BLOCKS * 32 * 12 bytes (117 KB) that every GPU loading the
+ * library holds until exit.  The first call on a device looks up that
+ * array's device address (cudaGetSymbolAddress) and sets the kernels'
+ * shared-memory limit; make that first call before any stream capture.
+ * Every call shares the one array, so calls that overlap on the GPU (two
+ * streams, two threads) race: serialize them.  Work is issued on `stream`
+ * (a cudaStream_t; NULL = the legacy default stream) and is asynchronous.
+ * Returns HFX_ERR_ARG for sizes beyond these limits. */
+#define HFX_NOALLOC_MAX_BLOCKS 304
+int32_t hfx_score_spectrum_noalloc(const uint8_t *ions, const float *r_sorted, const uint32_t *tc_sorted,
+                                   const uint32_t *tn_sorted, const uint32_t *idx_sorted, uint32_t num_pep,
+                                   const float *mass_table26, const float *row, int32_t len, int32_t charges,
+                                   uint32_t begin, uint32_t end, int32_t top_n, int32_t fastdiv, void *stream,
+                                   float *out_score, uint64_t *out_key, uint32_t *out_pep);
+
 #ifdef __cplusplus
 }
 #endif
