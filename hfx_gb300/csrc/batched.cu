@@ -28,6 +28,18 @@ constexpr int kClasses = 10;         // (ion charges 0..4) x (narrow, wide)
 constexpr float kWideEps = 1.0f;     // windows wider than this are "wide"
 constexpr uint32_t kWaitLimit = 1u << 24;
 
+// Bins of a group tile that the scorer copies (a multiple of 8 keeps every
+// bulk copy a multiple of 16 bytes).
+__host__ __device__ __forceinline__ int32_t tile_bins(int32_t maxlen) { return (maxlen + 7) & ~7; }
+
+// Shared memory of one scorer warp: bit planes + distinct-bin list, then the
+// per-member top-K lists (scores, keys) and admission thresholds.
+__host__ __device__ __forceinline__ size_t batched_warp_bytes(int32_t words, int G, int K) {
+    const size_t a = ((size_t)3 * words * 4 + (size_t)kListCap * 2 + 15) & ~(size_t)15;
+    const size_t b = (size_t)G * K * 4 + (size_t)((G * K) & 1) * 4 + (size_t)G * K * 8 + (size_t)G * 4;
+    return (a + b + 15) & ~(size_t)15;
+}
+
 __device__ __forceinline__ int spec_class(const SpecMeta &m) {
     return m.charges_plain * 2 + (m.eps > kWideEps ? 1 : 0);
 }
@@ -159,10 +171,78 @@ __device__ __forceinline__ int32_t find_group(const uint32_t *__restrict__ item_
     return lo;
 }
 
+// Interleave each group's member rows bin-major, tile[g][bin][G]: zero
+// rows for empty slots and zeros beyond each member's length, so that the
+// scorer needs neither a per-member length test nor a per-member load.
+template <typename T> __device__ __forceinline__ T zero_of();
+template <> __device__ __forceinline__ float zero_of<float>() { return 0.0f; }
+template <> __device__ __forceinline__ __nv_bfloat16 zero_of<__nv_bfloat16>() { return __float2bfloat16_rn(0.0f); }
+template <> __device__ __forceinline__ __half zero_of<__half>() { return __float2half_rn(0.0f); }
+
+template <typename T, int G>
+struct alignas((G * sizeof(T) >= 16) ? 16 : G * sizeof(T)) TilePack {
+    T v[G];
+};
+
+template <typename T, int G>
+__global__ void k_pack_tiles(const T *__restrict__ rows, int64_t stride, const SpecMeta *__restrict__ meta,
+                             const int32_t *__restrict__ perm, const GroupInfo *__restrict__ groups,
+                             const uint32_t *__restrict__ ngroups_p, T *__restrict__ tiles) {
+    const uint32_t g = blockIdx.x;
+    if (g >= *ngroups_p) return;
+    const GroupInfo gi = groups[g];
+    __shared__ int32_t s_spec[G], s_len[G];
+    if (threadIdx.x < G) {
+        const int j = threadIdx.x;
+        const int32_t s = j < (int)gi.count ? perm[gi.pos0 + j] : -1;
+        s_spec[j] = s;
+        s_len[j] = s >= 0 ? meta[s].len : 0;
+    }
+    __syncthreads();
+    T *tile = tiles + (size_t)g * stride * G;
+    const int32_t nb = tile_bins(gi.maxlen);
+    for (int32_t b = threadIdx.x; b < nb; b += blockDim.x) {
+        TilePack<T, G> pk;
+#pragma unroll
+        for (int j = 0; j < G; ++j)
+            pk.v[j] = (s_spec[j] >= 0 && b < s_len[j]) ? rows[(size_t)s_spec[j] * stride + b] : zero_of<T>();
+        *reinterpret_cast<TilePack<T, G> *>(tile + (size_t)b * G) = pk;
+    }
+}
+
+// Warp-cooperative insert into a sorted shared-memory list (entry i at
+// lane i); returns the new K-th score (the admission threshold).
+__device__ __forceinline__ float smem_topk_insert(float *ks, uint64_t *kk, float ns, uint64_t nk, int K) {
+    const int lane = threadIdx.x & 31;
+    const float cs = lane < K ? ks[lane] : -INFINITY;
+    const uint64_t ck = lane < K ? kk[lane] : ~0ull;
+    const bool mine_better = (lane < K) && better(cs, ck, ns, nk);
+    const int pos = __popc(__ballot_sync(kFullMask, mine_better));
+    const float us = __shfl_up_sync(kFullMask, cs, 1);
+    const uint64_t uk = __shfl_up_sync(kFullMask, ck, 1);
+    float out = cs;
+    __syncwarp();
+    if (pos < K) {
+        if (lane == pos) { ks[lane] = ns; kk[lane] = nk; out = ns; }
+        else if (lane > pos && lane < K) { ks[lane] = us; kk[lane] = uk; out = us; }
+    }
+    __syncwarp();
+    return __shfl_sync(kFullMask, out, K - 1);
+}
+
+template <int G>
+__device__ __forceinline__ uint32_t slot_owner_mask() {
+    // one lane per slot among the lanes that hold the same reduced slot
+    if constexpr (G == 8) return 0x11111111u;
+    else if constexpr (G == 4) return 0x01010101u;
+    else if constexpr (G == 2) return 0x00010001u;
+    else return 0x1u;
+}
+
 template <bool FastDiv, typename T, int G>
-__global__ void __launch_bounds__(256, 1)
-k_score_batched(DevDB db, const T *__restrict__ rows, int64_t stride, const SpecMeta *__restrict__ meta,
-                const uint32_t *__restrict__ wb, const uint32_t *__restrict__ we, const int32_t *__restrict__ perm,
+__global__ void __launch_bounds__(512, 1)
+k_score_batched(DevDB db, const T *__restrict__ tiles, int64_t stride, const uint32_t *__restrict__ wb,
+                const uint32_t *__restrict__ we, const int32_t *__restrict__ perm,
                 const GroupInfo *__restrict__ groups, const uint32_t *__restrict__ item_off,
                 const uint32_t *__restrict__ ngroups_p, int32_t chunk, int32_t K, uint32_t *__restrict__ counter,
                 float *__restrict__ part_s, uint64_t *__restrict__ part_k, uint32_t *__restrict__ err) {
@@ -170,24 +250,26 @@ k_score_batched(DevDB db, const T *__restrict__ rows, int64_t stride, const Spec
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int32_t words_cap = (int32_t)((stride + 31) / 32);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
-    T *srows = reinterpret_cast<T *>(smem + 128);
-    const size_t row_bytes = (size_t)stride * sizeof(T);
-    uint32_t *planes = reinterpret_cast<uint32_t *>(smem + 128 + G * row_bytes);
-    uint16_t *lists = reinterpret_cast<uint16_t *>(planes + (size_t)nw * 3 * words_cap);
+    T *stile = reinterpret_cast<T *>(smem + 128);
+    const size_t tile_bytes = (size_t)stride * G * sizeof(T);
+    const size_t warp_bytes = batched_warp_bytes(words_cap, G, K);
+    uint8_t *wbase = smem + 128 + ((tile_bytes + 15) & ~(size_t)15) + (size_t)warp * warp_bytes;
+    uint32_t *planes = reinterpret_cast<uint32_t *>(wbase);
+    uint16_t *list = reinterpret_cast<uint16_t *>(planes + 3 * words_cap);
+    float *tk_s = reinterpret_cast<float *>(wbase + ((3 * words_cap * 4 + kListCap * 2 + 15) & ~15));
+    uint64_t *tk_k = reinterpret_cast<uint64_t *>(tk_s + G * K + ((G * K) & 1));
+    float *thr = reinterpret_cast<float *>(tk_k + G * K);
     __shared__ int32_t s_item;
-    __shared__ int32_t s_spec[G];
-    __shared__ int32_t s_len[G];
     __shared__ uint32_t s_wb[G], s_we[G];
 
     const int32_t ngroups = (int32_t)*ngroups_p;
     const uint32_t total = item_off[ngroups];
     if (threadIdx.x == 0) mbar_init(bar, 1);
-    for (int32_t i = threadIdx.x; i < nw * 3 * words_cap; i += blockDim.x) planes[i] = 0u;
+    for (int32_t i = lane; i < 3 * words_cap; i += 32) planes[i] = 0u;
     __syncthreads();
-    Planes pl{planes + (size_t)warp * 3 * words_cap, planes + (size_t)warp * 3 * words_cap + words_cap,
-              planes + (size_t)warp * 3 * words_cap + 2 * words_cap};
-    uint16_t *list = lists + (size_t)warp * kListCap;
+    const Planes pl{planes, planes + words_cap, planes + 2 * words_cap};
     const float mt_lane = db.mt[lane];
+    const int my_slot = reduce_slot_of_lane<G>(lane);
     uint32_t phase = 0;
 
     while (true) {
@@ -202,87 +284,70 @@ k_score_batched(DevDB db, const T *__restrict__ rows, int64_t stride, const Spec
         const int cnt = (int)gi.count;
         if (threadIdx.x < G) {
             const int j = threadIdx.x;
-            int32_t s = -1, len = 0;
             uint32_t b = 0, e = 0;
             if (j < cnt) {
-                s = perm[gi.pos0 + j];
-                len = meta[s].len;
+                const int32_t s = perm[gi.pos0 + j];
                 b = wb[s];
                 e = we[s];
             }
-            s_spec[j] = s;
-            s_len[j] = len;
             s_wb[j] = b;
             s_we[j] = e;
         }
-        __syncthreads();
+        for (int i = lane; i < G * K; i += 32) {
+            tk_s[i] = -INFINITY;
+            tk_k[i] = ~0ull;
+        }
+        if (lane < G) thr[lane] = -INFINITY;
+        const int32_t nb = tile_bins(gi.maxlen);
         if (threadIdx.x == 0) {
             fence_proxy_async();
-            mbar_arrive_expect_tx(bar, (uint32_t)(cnt * row_bytes));
-            for (int j = 0; j < cnt; ++j)
-                bulk_g2s(reinterpret_cast<uint8_t *>(srows) + j * row_bytes, rows + (size_t)s_spec[j] * stride,
-                         (uint32_t)row_bytes, bar);
+            const uint32_t bytes = (uint32_t)((size_t)nb * G * sizeof(T));
+            mbar_arrive_expect_tx(bar, bytes);
+            bulk_g2s(stile, tiles + (size_t)g * stride * G, bytes, bar);
         }
+        __syncthreads();
         if (!mbar_wait(bar, phase, kWaitLimit)) {
             if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
             return;
         }
         phase ^= 1u;
-        SpecSet<T, G> ss;
-#pragma unroll
-        for (int j = 0; j < G; ++j) {
-            ss.row[j] = srows + (size_t)j * stride;
-            ss.len[j] = s_len[j];
-        }
-        WarpTopK tk[G];
-        float thr[G];
-#pragma unroll
-        for (int j = 0; j < G; ++j) {
-            tk[j].init();
-            thr[j] = -INFINITY;
-        }
-        const int32_t nbins = gi.maxlen;
-        const int32_t words = (nbins + 31) / 32;
+        const uint32_t my_b = lane < G ? s_wb[lane] : 0u, my_e = lane < G ? s_we[lane] : 0u;
+        const TileDot<T, G> dot{stile};
         for (uint32_t p = p0 + warp; p < p1; p += nw) {
-            uint32_t act = 0;
-#pragma unroll
-            for (int j = 0; j < G; ++j)
-                if (j < cnt && s_wb[j] <= p && p < s_we[j]) act |= 1u << j;
+            const uint32_t act = __ballot_sync(kFullMask, lane < G && my_b <= p && p < my_e) & ((1u << G) - 1u);
             if (!act) continue;
-            ss.active = act;
-            build_planes<FastDiv>(pl, db.ions, db.tc_sorted[p], db.tn_sorted[p], db.r_sorted[p], (int)gi.charges,
-                                  nbins, mt_lane, NoMods{});
+            const WordRange wr = build_planes<FastDiv>(pl, db.ions, db.tc_sorted[p], db.tn_sorted[p],
+                                                       db.r_sorted[p], (int)gi.charges, gi.maxlen, mt_lane,
+                                                       NoMods{});
             float acc[G];
-            planes_dot<T, G>(pl, list, words, ss, acc);
-#pragma unroll
-            for (int j = 0; j < G; ++j) {
-                if (((act >> j) & 1u) && acc[j] >= thr[j]) {
-                    tk[j].insert(acc[j], (uint64_t)p, K);
-                    thr[j] = __shfl_sync(kFullMask, tk[j].s, K - 1);
-                }
+            planes_accumulate<G>(pl, list, wr, dot, acc);
+            const float sc = reduce_scatter<G>(acc);
+            const bool want = ((act >> my_slot) & 1u) && sc >= thr[my_slot];
+            uint32_t ins = __ballot_sync(kFullMask, want) & slot_owner_mask<G>();
+            while (ins) {
+                const int src = __ffs(ins) - 1;
+                ins &= ins - 1u;
+                const int j = reduce_slot_of_lane<G>(src);
+                const float s = __shfl_sync(kFullMask, sc, src);
+                const float t = smem_topk_insert(tk_s + j * K, tk_k + j * K, s, (uint64_t)p, K);
+                if (lane == 0) thr[j] = t;
+                __syncwarp();
             }
         }
         __syncthreads();
-        // merge the warps' lists per member; planes/lists are reused as scratch
-        float *sm_s = reinterpret_cast<float *>(planes);
-        uint64_t *sm_k = reinterpret_cast<uint64_t *>(planes) + (size_t)nw * G * K;
-#pragma unroll
-        for (int j = 0; j < G; ++j) {
-            if (lane < K) {
-                sm_s[(warp * G + j) * K + lane] = tk[j].s;
-                sm_k[(warp * G + j) * K + lane] = tk[j].k;
-            }
-        }
-        __syncthreads();
+        // merge the warps' lists of every member
         for (int j = warp; j < cnt; j += nw) {
             WarpTopK m;
             m.init();
             for (int w = 0; w < nw; ++w) {
-                for (int t = 0; t < K; ++t) {
-                    const uint64_t kk = sm_k[(w * G + j) * K + t];
-                    if (kk == ~0ull) break;
-                    m.insert(sm_s[(w * G + j) * K + t], kk, K);
-                }
+                const uint8_t *ob = smem + 128 + ((tile_bytes + 15) & ~(size_t)15) + (size_t)w * warp_bytes;
+                const float *os = reinterpret_cast<const float *>(ob + ((3 * words_cap * 4 + kListCap * 2 + 15) & ~15));
+                const uint64_t *ok = reinterpret_cast<const uint64_t *>(os + G * K + ((G * K) & 1));
+                const float vs = lane < K ? os[j * K + lane] : -INFINITY;
+                const uint64_t vk = lane < K ? ok[j * K + lane] : ~0ull;
+                const int nvalid = __popc(__ballot_sync(kFullMask, vk != ~0ull));
+                for (int t = 0; t < nvalid; ++t)
+                    m.insert(__shfl_sync(kFullMask, vs, t), __shfl_sync(kFullMask, vk, t), K);
             }
             if (lane < K) {
                 const size_t o = ((size_t)item * G + j) * K + lane;
@@ -290,9 +355,6 @@ k_score_batched(DevDB db, const T *__restrict__ rows, int64_t stride, const Spec
                 part_k[o] = m.k;
             }
         }
-        __syncthreads();
-        // restore zeroed planes for the next item
-        for (int32_t i = threadIdx.x; i < nw * 3 * words_cap; i += blockDim.x) planes[i] = 0u;
         __syncthreads();
     }
 }
@@ -361,10 +423,10 @@ __global__ void __launch_bounds__(256) k_rescore(DevDB db, const float *__restri
         float sc = -INFINITY;
         if (kk != ~0ull) {
             const uint32_t p = (uint32_t)kk;
-            build_planes<FastDiv>(pl, db.ions, db.tc_sorted[p], db.tn_sorted[p], db.r_sorted[p], m.charges_plain,
-                                  m.len, mt_lane, NoMods{});
+            const WordRange wr = build_planes<FastDiv>(pl, db.ions, db.tc_sorted[p], db.tn_sorted[p],
+                                                       db.r_sorted[p], m.charges_plain, m.len, mt_lane, NoMods{});
             float acc[1];
-            planes_dot<float, 1>(pl, list, (m.len + 31) / 32, ss, acc);
+            planes_dot<float, 1>(pl, list, wr, ss, acc);
             sc = acc[0];
         }
         if (lane == 0) {
@@ -417,9 +479,8 @@ using namespace hfx;
 
 size_t hfx_batched_smem(int64_t stride, int elem_bytes, int G, int nw, int K) {
     const int32_t words = (int32_t)((stride + 31) / 32);
-    const size_t planes = (size_t)nw * 3 * words * 4 + (size_t)nw * kListCap * 2;
-    const size_t merge = (size_t)nw * G * K * 16;
-    return 128 + (size_t)G * stride * elem_bytes + (planes > merge ? planes : merge);
+    const size_t tile = ((size_t)stride * G * elem_bytes + 15) & ~(size_t)15;
+    return 128 + tile + (size_t)nw * batched_warp_bytes(words, G, K);
 }
 
 int hfx_batched_plan(const SpecMeta *meta, int32_t nspec, const uint32_t *wb, const uint32_t *we, int32_t G,
@@ -441,60 +502,73 @@ int hfx_batched_plan(const SpecMeta *meta, int32_t nspec, const uint32_t *wb, co
 
 template <bool F, typename T, int G>
 static int launch_batched_t(const DevDB &db, const T *rows, int64_t stride, const SpecMeta *meta, const uint32_t *wb,
-                            const uint32_t *we, const BatchedWs &ws, int32_t chunk, int32_t K, int nw, int grid,
-                            float *part_s, uint64_t *part_k, uint32_t *err, cudaStream_t st) {
+                            const uint32_t *we, const BatchedWs &ws, void *tiles, uint32_t ngroups, int32_t chunk,
+                            int32_t K, int nw, int grid, float *part_s, uint64_t *part_k, uint32_t *err,
+                            cudaStream_t st) {
+    if (ngroups > 0)
+        k_pack_tiles<T, G><<<ngroups, 256, 0, st>>>(rows, stride, meta, ws.perm, ws.groups, ws.ngroups, (T *)tiles);
+    int dev = 0, sms = 0, smem_max = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const int32_t words = (int32_t)((stride + 31) / 32);
+    if (nw <= 0) {
+        const size_t fixed = hfx_batched_smem(stride, sizeof(T), G, 0, K);
+        const size_t per = batched_warp_bytes(words, G, K);
+        nw = (int)std::min<size_t>(16, fixed < (size_t)smem_max ? ((size_t)smem_max - fixed) / per : 0);
+        if (nw < 1) return (int)cudaErrorInvalidValue;
+    }
     const size_t smem = hfx_batched_smem(stride, sizeof(T), G, nw, K);
     auto fn = k_score_batched<F, T, G>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
     if (grid <= 0) {
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        int per = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, nw * 32, smem);
         grid = sms * (per > 0 ? per : 1);
     }
-    fn<<<grid, nw * 32, smem, st>>>(db, rows, stride, meta, wb, we, ws.perm, ws.groups, ws.item_off, ws.ngroups,
-                                    chunk, K, ws.counter, part_s, part_k, err);
+    fn<<<grid, nw * 32, smem, st>>>(db, (const T *)tiles, stride, wb, we, ws.perm, ws.groups, ws.item_off,
+                                    ws.ngroups, chunk, K, ws.counter, part_s, part_k, err);
     return (int)cudaGetLastError();
 }
 
 template <bool F, typename T>
 static int launch_batched_g(int G, const DevDB &db, const T *rows, int64_t stride, const SpecMeta *meta,
-                            const uint32_t *wb, const uint32_t *we, const BatchedWs &ws, int32_t chunk, int32_t K,
-                            int nw, int grid, float *ps, uint64_t *pk, uint32_t *err, cudaStream_t st) {
+                            const uint32_t *wb, const uint32_t *we, const BatchedWs &ws, void *tiles, uint32_t ng,
+                            int32_t chunk, int32_t K, int nw, int grid, float *ps, uint64_t *pk, uint32_t *err,
+                            cudaStream_t st) {
     switch (G) {
-    case 1: return launch_batched_t<F, T, 1>(db, rows, stride, meta, wb, we, ws, chunk, K, nw, grid, ps, pk, err, st);
-    case 2: return launch_batched_t<F, T, 2>(db, rows, stride, meta, wb, we, ws, chunk, K, nw, grid, ps, pk, err, st);
-    case 4: return launch_batched_t<F, T, 4>(db, rows, stride, meta, wb, we, ws, chunk, K, nw, grid, ps, pk, err, st);
-    case 8: return launch_batched_t<F, T, 8>(db, rows, stride, meta, wb, we, ws, chunk, K, nw, grid, ps, pk, err, st);
+    case 1: return launch_batched_t<F, T, 1>(db, rows, stride, meta, wb, we, ws, tiles, ng, chunk, K, nw, grid, ps, pk, err, st);
+    case 2: return launch_batched_t<F, T, 2>(db, rows, stride, meta, wb, we, ws, tiles, ng, chunk, K, nw, grid, ps, pk, err, st);
+    case 4: return launch_batched_t<F, T, 4>(db, rows, stride, meta, wb, we, ws, tiles, ng, chunk, K, nw, grid, ps, pk, err, st);
+    case 8: return launch_batched_t<F, T, 8>(db, rows, stride, meta, wb, we, ws, tiles, ng, chunk, K, nw, grid, ps, pk, err, st);
     default: return (int)cudaErrorInvalidValue;
     }
 }
 
 int hfx_batched_score(const DevDB &db, const void *rows, int elem_kind, int64_t stride, const SpecMeta *meta,
-                      const uint32_t *wb, const uint32_t *we, const BatchedWs &ws, int32_t G, int32_t chunk,
-                      int32_t K, int nw, int grid, int fastdiv, float *part_s, uint64_t *part_k, uint32_t *err,
-                      cudaStream_t st) {
+                      const uint32_t *wb, const uint32_t *we, const BatchedWs &ws, void *tiles, uint32_t ngroups,
+                      int32_t G, int32_t chunk, int32_t K, int nw, int grid, int fastdiv, float *part_s,
+                      uint64_t *part_k, uint32_t *err, cudaStream_t st) {
     cudaMemsetAsync(ws.counter, 0, 4, st);
     if (elem_kind == 0) {
         const float *r = (const float *)rows;
-        return fastdiv ? launch_batched_g<true, float>(G, db, r, stride, meta, wb, we, ws, chunk, K, nw, grid, part_s,
-                                                       part_k, err, st)
-                       : launch_batched_g<false, float>(G, db, r, stride, meta, wb, we, ws, chunk, K, nw, grid,
-                                                        part_s, part_k, err, st);
+        return fastdiv ? launch_batched_g<true, float>(G, db, r, stride, meta, wb, we, ws, tiles, ngroups, chunk, K,
+                                                       nw, grid, part_s, part_k, err, st)
+                       : launch_batched_g<false, float>(G, db, r, stride, meta, wb, we, ws, tiles, ngroups, chunk, K,
+                                                        nw, grid, part_s, part_k, err, st);
     } else if (elem_kind == 1) {
         const __nv_bfloat16 *r = (const __nv_bfloat16 *)rows;
-        return fastdiv ? launch_batched_g<true, __nv_bfloat16>(G, db, r, stride, meta, wb, we, ws, chunk, K, nw, grid,
-                                                               part_s, part_k, err, st)
-                       : launch_batched_g<false, __nv_bfloat16>(G, db, r, stride, meta, wb, we, ws, chunk, K, nw,
-                                                                grid, part_s, part_k, err, st);
+        return fastdiv ? launch_batched_g<true, __nv_bfloat16>(G, db, r, stride, meta, wb, we, ws, tiles, ngroups,
+                                                               chunk, K, nw, grid, part_s, part_k, err, st)
+                       : launch_batched_g<false, __nv_bfloat16>(G, db, r, stride, meta, wb, we, ws, tiles, ngroups,
+                                                                chunk, K, nw, grid, part_s, part_k, err, st);
     } else {
         const __half *r = (const __half *)rows;
-        return fastdiv ? launch_batched_g<true, __half>(G, db, r, stride, meta, wb, we, ws, chunk, K, nw, grid,
-                                                        part_s, part_k, err, st)
-                       : launch_batched_g<false, __half>(G, db, r, stride, meta, wb, we, ws, chunk, K, nw, grid,
-                                                         part_s, part_k, err, st);
+        return fastdiv ? launch_batched_g<true, __half>(G, db, r, stride, meta, wb, we, ws, tiles, ngroups, chunk, K,
+                                                        nw, grid, part_s, part_k, err, st)
+                       : launch_batched_g<false, __half>(G, db, r, stride, meta, wb, we, ws, tiles, ngroups, chunk,
+                                                         K, nw, grid, part_s, part_k, err, st);
     }
 }
 

@@ -31,8 +31,6 @@ constexpr float kBinMono = 1.0005079f;
 
 constexpr uint32_t kFullMask = 0xFFFFFFFFu;
 
-__device__ __forceinline__ float div_ieee(float a, float b) { return __fdiv_rn(a, b); }
-
 // ion_series.cu:59-69: ionMZ and binMZ.  IEEE division unless FastDiv, which
 // calls __fdividef exactly where the reference did.
 template <bool FastDiv>
@@ -41,27 +39,46 @@ __device__ __forceinline__ float dev_div(float a, float b) {
     else return __fdiv_rn(a, b);
 }
 
+// The IEEE quotient a / c for an ion charge c in 1..4: the powers of two are
+// exact scalings, only c = 3 needs a division.
+template <bool FastDiv>
+__device__ __forceinline__ float div_charge(float a, int c) {
+    if constexpr (FastDiv) return __fdividef(a, (float)c);
+    if (c == 3) return __fdiv_rn(a, 3.0f);
+    return __fmul_rn(a, c == 1 ? 1.0f : (c == 2 ? 0.5f : 0.25f));
+}
+
 // float -> uint32 conversion (saturating, NaN -> 0) reinterpreted as int32.
 __device__ __forceinline__ int32_t sat_bin(float r) {
     return (int32_t)__float2uint_rz(r);
 }
 
+// rint(fl(mz / 1.0005079)).  A multiply by the rounded reciprocal lies within
+// 2^-22 relative of the IEEE quotient, i.e. within 2^-8 for |q| < 2^14; when
+// it is farther than 1/128 from a half-integer both round to the same
+// integer, otherwise the IEEE quotient itself is computed.  Exact.
+constexpr float kInvBinMono = 1.0f / 1.0005079f;
 template <bool FastDiv>
 __device__ __forceinline__ int32_t bin_of(float mz) {
-    return sat_bin(rintf(dev_div<FastDiv>(mz, kBinMono)));
+    if constexpr (FastDiv) return sat_bin(rintf(__fdividef(mz, kBinMono)));
+    const float q = __fmul_rn(mz, kInvBinMono);
+    const float f = __fsub_rn(q, floorf(q));
+    if (fabsf(q) < 16384.0f && fabsf(__fsub_rn(f, 0.5f)) > 0.0078125f) return sat_bin(rintf(q));
+    return sat_bin(rintf(__fdiv_rn(mz, kBinMono)));
 }
 
 struct ChargeConst {
-    float cf, hc, dh2o, dnh3;
+    int c;
+    float hc, dh2o, dnh3;
 };
 
 template <bool FastDiv>
 __device__ __forceinline__ ChargeConst charge_const(int c) {
     ChargeConst k;
-    k.cf = (float)c;
-    k.hc = __fmul_rn(kH, k.cf);
-    k.dh2o = dev_div<FastDiv>(kH2O, k.cf);
-    k.dnh3 = dev_div<FastDiv>(kNH3, k.cf);
+    k.c = c;
+    k.hc = __fmul_rn(kH, (float)c);
+    k.dh2o = div_charge<FastDiv>(kH2O, c);
+    k.dnh3 = div_charge<FastDiv>(kNH3, c);
     return k;
 }
 
@@ -75,37 +92,47 @@ __device__ __forceinline__ void set_bit(uint32_t *p, int32_t x) {
     atomicOr(&p[x >> 5], 1u << (x & 31));
 }
 
+// Range of bins a lane has set, for the compaction pass.
+struct BinRange {
+    int32_t lo = 0x7FFFFFFF, hi = -1;
+    __device__ __forceinline__ void add(int32_t a, int32_t b) {
+        lo = min(lo, a);
+        hi = max(hi, b);
+    }
+};
+
 // x-1, x, x+1 at weight 25/50/25 (ion_series.cu:92-94, 109-111).
-__device__ __forceinline__ void set_triplet(const Planes &pl, int32_t x, int32_t nbins) {
+__device__ __forceinline__ void set_triplet(const Planes &pl, int32_t x, int32_t nbins, BinRange &br) {
     if (x >= 1 && x + 1 < nbins && (x & 31) != 0 && (x & 31) != 31) {
         atomicOr(&pl.H[x >> 5], 7u << ((x - 1) & 31));
         atomicOr(&pl.T[x >> 5], 1u << (x & 31));
+        br.add(x - 1, x + 1);
         return;
     }
-    if (0 <= x - 1 && x - 1 < nbins) set_bit(pl.H, x - 1);
-    if (0 <= x + 1 && x + 1 < nbins) set_bit(pl.H, x + 1);
-    if (0 <= x && x < nbins) { set_bit(pl.H, x); set_bit(pl.T, x); }
+    if (0 <= x - 1 && x - 1 < nbins) { set_bit(pl.H, x - 1); br.add(x - 1, x - 1); }
+    if (0 <= x + 1 && x + 1 < nbins) { set_bit(pl.H, x + 1); br.add(x + 1, x + 1); }
+    if (0 <= x && x < nbins) { set_bit(pl.H, x); set_bit(pl.T, x); br.add(x, x); }
 }
 
-__device__ __forceinline__ void set_single(const Planes &pl, int32_t x, int32_t nbins) {
-    if (0 <= x && x < nbins) set_bit(pl.A, x);
+__device__ __forceinline__ void set_single(const Planes &pl, int32_t x, int32_t nbins, BinRange &br) {
+    if (0 <= x && x < nbins) { set_bit(pl.A, x); br.add(x, x); }
 }
 
 // The ten ions of one (b, y, charge), ion_series.cu:78-123.
 template <bool FastDiv>
-__device__ __forceinline__ void emit_ions(const Planes &pl, float b, float y,
-                                          const ChargeConst &k, int32_t nbins) {
+__device__ __forceinline__ void emit_ions(const Planes &pl, float b, float y, const ChargeConst &k,
+                                          int32_t nbins, BinRange &br) {
     // A ion
-    set_single(pl, bin_of<FastDiv>(dev_div<FastDiv>(__fadd_rn(__fsub_rn(b, kCO), k.hc), k.cf)), nbins);
+    set_single(pl, bin_of<FastDiv>(div_charge<FastDiv>(__fadd_rn(__fsub_rn(b, kCO), k.hc), k.c)), nbins, br);
     // B ions
-    float m = dev_div<FastDiv>(__fadd_rn(b, k.hc), k.cf);
-    set_triplet(pl, bin_of<FastDiv>(m), nbins);
-    set_single(pl, bin_of<FastDiv>(__fsub_rn(m, k.dh2o)), nbins);
-    set_single(pl, bin_of<FastDiv>(__fsub_rn(m, k.dnh3)), nbins);
+    float m = div_charge<FastDiv>(__fadd_rn(b, k.hc), k.c);
+    set_triplet(pl, bin_of<FastDiv>(m), nbins, br);
+    set_single(pl, bin_of<FastDiv>(__fsub_rn(m, k.dh2o)), nbins, br);
+    set_single(pl, bin_of<FastDiv>(__fsub_rn(m, k.dnh3)), nbins, br);
     // Y ions
-    m = dev_div<FastDiv>(__fadd_rn(__fadd_rn(y, kH2O), k.hc), k.cf);
-    set_triplet(pl, bin_of<FastDiv>(m), nbins);
-    set_single(pl, bin_of<FastDiv>(__fsub_rn(m, k.dnh3)), nbins);
+    m = div_charge<FastDiv>(__fadd_rn(__fadd_rn(y, kH2O), k.hc), k.c);
+    set_triplet(pl, bin_of<FastDiv>(m), nbins, br);
+    set_single(pl, bin_of<FastDiv>(__fsub_rn(m, k.dnh3)), nbins, br);
 }
 
 // Mass of one packed residue byte (utils.h:92-101; an out-of-range texture
@@ -122,15 +149,22 @@ struct NoMods {
     __device__ __forceinline__ float add(uint32_t /*byte*/) const { return 0.0f; }
 };
 
+// Words [lo, hi) of the bit planes that hold set bits.
+struct WordRange {
+    int32_t lo, hi;
+};
+
 // Build the ion bit planes of one candidate.  Residues [tc, tn) of `ions`,
-// `charges` ion charges (0 = none), bins >= nbins dropped.
+// `charges` ion charges (0 = none), bins >= nbins dropped.  Returns the
+// range of plane words that may hold set bits (warp-uniform).
 template <bool FastDiv, typename Mods>
-__device__ __forceinline__ void build_planes(const Planes &pl, const uint8_t *__restrict__ ions,
-                                             uint32_t tc, uint32_t tn, float residual,
-                                             int charges, int32_t nbins, float mt_lane,
-                                             const Mods &mods) {
+__device__ __forceinline__ WordRange build_planes(const Planes &pl, const uint8_t *__restrict__ ions,
+                                                  uint32_t tc, uint32_t tn, float residual,
+                                                  int charges, int32_t nbins, float mt_lane,
+                                                  const Mods &mods) {
     const int lane = threadIdx.x & 31;
-    if (charges <= 0) return;
+    BinRange br;
+    if (charges <= 0) return WordRange{0, 0};
     float carry = 0.0f;
     for (uint32_t base = tc; base < tn; base += 32) {
         const int cnt = (int)min(32u, tn - base);
@@ -158,11 +192,15 @@ __device__ __forceinline__ void build_planes(const Planes &pl, const uint8_t *__
             const float yk = __shfl_sync(kFullMask, y, k & 31);
             if (it < items) {
                 const ChargeConst kc = charge_const<FastDiv>(cm1 + 1);
-                emit_ions<FastDiv>(pl, bk, yk, kc, nbins);
+                emit_ions<FastDiv>(pl, bk, yk, kc, nbins, br);
             }
         }
     }
     __syncwarp();
+    const int32_t lo = __reduce_min_sync(kFullMask, br.lo);
+    const int32_t hi = __reduce_max_sync(kFullMask, br.hi);
+    if (hi < 0) return WordRange{0, 0};
+    return WordRange{lo >> 5, (hi >> 5) + 1};
 }
 
 // Warp-wide inclusive scan of an int.
@@ -197,39 +235,123 @@ struct SpecSet {
     uint32_t active;     // bit g set: score this candidate against spectrum g
 };
 
-// Accumulate list entries [0, n) into acc[] (entry i by lane i%32).
+// Accumulate list entries [0, n) into acc[] (entry i by lane i%32): rows
+// given separately, with a length and an active flag per spectrum.
 template <typename T, int G>
-__device__ __forceinline__ void dot_list(const uint16_t *list, int n, const SpecSet<T, G> &ss,
-                                         float (&acc)[G]) {
-    const int lane = threadIdx.x & 31;
-    for (int i = lane; i < n; i += 32) {
-        const uint32_t e = list[i];
-        const uint32_t bin = e >> 2;
-        const float w = level_weight(e & 3u);
+struct RowDot {
+    const SpecSet<T, G> &ss;
+    __device__ __forceinline__ void operator()(const uint16_t *list, int n, float (&acc)[G]) const {
+        const int lane = threadIdx.x & 31;
+        for (int i = lane; i < n; i += 32) {
+            const uint32_t e = list[i];
+            const uint32_t bin = e >> 2;
+            const float w = level_weight(e & 3u);
 #pragma unroll
-        for (int g = 0; g < G; ++g) {
-            if (((ss.active >> g) & 1u) && (int32_t)bin < ss.len[g])
-                acc[g] = __fmaf_rn(w, load_x<T>(ss.row[g], bin), acc[g]);
+            for (int g = 0; g < G; ++g) {
+                if (((ss.active >> g) & 1u) && (int32_t)bin < ss.len[g])
+                    acc[g] = __fmaf_rn(w, load_x<T>(ss.row[g], bin), acc[g]);
+            }
         }
     }
-}
+};
 
-// Compact the planes (clearing them) into the sorted distinct-bin list and
-// accumulate the gather-dot for every active spectrum.  words = planes'
-// used word count (multiple of 32 not required).
+// The same over a tile of G zero-padded rows interleaved bin-major
+// (tile[bin*G + g]): one vector load per entry feeds all G spectra.  Rows
+// are zero beyond their length and fmaf(w, +0, acc) == acc (acc is never
+// -0), so no per-spectrum length test is needed.
+template <typename T, int G> struct TileLoad {
+    __device__ __forceinline__ static void load(const T *t, uint32_t bin, float (&x)[G]) {
+#pragma unroll
+        for (int g = 0; g < G; ++g) x[g] = load_x<T>(t, bin * G + g);
+    }
+};
+template <> struct TileLoad<__nv_bfloat16, 8> {
+    __device__ __forceinline__ static void load(const __nv_bfloat16 *t, uint32_t bin, float (&x)[8]) {
+        const uint4 v = *reinterpret_cast<const uint4 *>(t + (size_t)bin * 8);
+        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            x[2 * i] = __uint_as_float(w[i] << 16);
+            x[2 * i + 1] = __uint_as_float(w[i] & 0xFFFF0000u);
+        }
+    }
+};
+template <> struct TileLoad<__nv_bfloat16, 4> {
+    __device__ __forceinline__ static void load(const __nv_bfloat16 *t, uint32_t bin, float (&x)[4]) {
+        const uint2 v = *reinterpret_cast<const uint2 *>(t + (size_t)bin * 4);
+        x[0] = __uint_as_float(v.x << 16);
+        x[1] = __uint_as_float(v.x & 0xFFFF0000u);
+        x[2] = __uint_as_float(v.y << 16);
+        x[3] = __uint_as_float(v.y & 0xFFFF0000u);
+    }
+};
+template <> struct TileLoad<__half, 8> {
+    __device__ __forceinline__ static void load(const __half *t, uint32_t bin, float (&x)[8]) {
+        const uint4 v = *reinterpret_cast<const uint4 *>(t + (size_t)bin * 8);
+        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const __half2 h = *reinterpret_cast<const __half2 *>(&w[i]);
+            const float2 f = __half22float2(h);
+            x[2 * i] = f.x;
+            x[2 * i + 1] = f.y;
+        }
+    }
+};
+template <> struct TileLoad<__half, 4> {
+    __device__ __forceinline__ static void load(const __half *t, uint32_t bin, float (&x)[4]) {
+        const uint2 v = *reinterpret_cast<const uint2 *>(t + (size_t)bin * 4);
+        const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&v.x));
+        const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&v.y));
+        x[0] = a.x; x[1] = a.y; x[2] = b.x; x[3] = b.y;
+    }
+};
+template <> struct TileLoad<float, 4> {
+    __device__ __forceinline__ static void load(const float *t, uint32_t bin, float (&x)[4]) {
+        const float4 v = *reinterpret_cast<const float4 *>(t + (size_t)bin * 4);
+        x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+    }
+};
+template <> struct TileLoad<float, 8> {
+    __device__ __forceinline__ static void load(const float *t, uint32_t bin, float (&x)[8]) {
+        const float4 a = *reinterpret_cast<const float4 *>(t + (size_t)bin * 8);
+        const float4 b = *reinterpret_cast<const float4 *>(t + (size_t)bin * 8 + 4);
+        x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w;
+        x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
+    }
+};
+
 template <typename T, int G>
-__device__ __forceinline__ void planes_dot(const Planes &pl, uint16_t *list, int words,
-                                           const SpecSet<T, G> &ss, float (&acc)[G],
-                                           int *n_distinct = nullptr) {
+struct TileDot {
+    const T *tile;
+    __device__ __forceinline__ void operator()(const uint16_t *list, int n, float (&acc)[G]) const {
+        const int lane = threadIdx.x & 31;
+        for (int i = lane; i < n; i += 32) {
+            const uint32_t e = list[i];
+            const float w = level_weight(e & 3u);
+            float x[G];
+            TileLoad<T, G>::load(tile, e >> 2, x);
+#pragma unroll
+            for (int g = 0; g < G; ++g) acc[g] = __fmaf_rn(w, x[g], acc[g]);
+        }
+    }
+};
+
+// Compact plane words [wr.lo, wr.hi) (clearing them) into the ascending list
+// of distinct bins and feed it to `dot` in lane order (entry i -> lane i%32).
+// acc[] holds each lane's partial sums afterwards (no cross-lane reduction).
+template <int G, typename Dot>
+__device__ __forceinline__ int planes_accumulate(const Planes &pl, uint16_t *list, WordRange wr, const Dot &dot,
+                                                 float (&acc)[G]) {
     const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int g = 0; g < G; ++g) acc[g] = 0.0f;
     int nbuf = 0;
     int ntot = 0;
-    for (int w0 = 0; w0 < words; w0 += 32) {
+    for (int w0 = wr.lo; w0 < wr.hi; w0 += 32) {
         const int w = w0 + lane;
         uint32_t a = 0, h = 0, t = 0;
-        if (w < words) {
+        if (w < wr.hi) {
             h = pl.H[w];
             t = pl.T[w];
             a = pl.A[w] | h;
@@ -243,7 +365,7 @@ __device__ __forceinline__ void planes_dot(const Planes &pl, uint16_t *list, int
         if (nbuf + total > kListCap) {
             // flush whole multiples of 32 so that lane = global rank % 32 holds
             const int full = nbuf & ~31;
-            dot_list<T, G>(list, full, ss, acc);
+            dot(list, full, acc);
             __syncwarp();
             const int rem = nbuf - full;
             uint16_t keep = 0;
@@ -264,15 +386,74 @@ __device__ __forceinline__ void planes_dot(const Planes &pl, uint16_t *list, int
         ntot += total;
         __syncwarp();
     }
-    dot_list<T, G>(list, nbuf, ss, acc);
+    dot(list, nbuf, acc);
     __syncwarp();
+    return ntot;
+}
+
+// XOR butterfly (16, 8, 4, 2, 1) of every accumulator: all lanes end with the
+// canonical sums.
+template <int G>
+__device__ __forceinline__ void butterfly_all(float (&acc)[G]) {
 #pragma unroll
     for (int g = 0; g < G; ++g) {
 #pragma unroll
         for (int off = 16; off >= 1; off >>= 1)
             acc[g] = __fadd_rn(acc[g], __shfl_xor_sync(kFullMask, acc[g], off));
     }
-    if (n_distinct) *n_distinct = ntot;
+}
+
+// The same sums as butterfly_all, as a reduce-scatter: at offsets 16, 8, 4
+// each lane keeps half of its accumulators and receives its partner's copy
+// of them, so every addition pairs the same operands as the full butterfly.
+// Returns the sum of accumulator slot_of_lane(lane); lanes differing only in
+// bits 0-1 (G = 8), 0-2 (G = 4), 0-3 (G = 2) hold the same slot.
+template <int G>
+__device__ __forceinline__ int reduce_slot_of_lane(int lane) {
+    if constexpr (G == 8) return ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
+    else if constexpr (G == 4) return ((lane >> 4) & 1) * 2 + ((lane >> 3) & 1);
+    else if constexpr (G == 2) return (lane >> 4) & 1;
+    else return 0;
+}
+template <int G>
+__device__ __forceinline__ float reduce_scatter(float (&acc)[G]) {
+    const int lane = threadIdx.x & 31;
+    float v[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) v[g] = acc[g];
+    int n = G;
+    int off = 16;
+#pragma unroll
+    for (int step = 0; step < 3; ++step) {
+        if (n == 1) break;
+        const int half = n / 2;
+        const bool hi = (lane & off) != 0;
+#pragma unroll
+        for (int k = 0; k < G / 2; ++k) {
+            if (k < half) {
+                const float send = hi ? v[k] : v[half + k];
+                const float keep = hi ? v[half + k] : v[k];
+                v[k] = __fadd_rn(keep, __shfl_xor_sync(kFullMask, send, off));
+            }
+        }
+        n = half;
+        off >>= 1;
+    }
+    float s = v[0];
+    for (; off >= 1; off >>= 1) s = __fadd_rn(s, __shfl_xor_sync(kFullMask, s, off));
+    return s;
+}
+
+// Compact the planes (clearing them) into the sorted distinct-bin list and
+// accumulate the gather-dot for every active spectrum; every lane ends with
+// the canonical sums.
+template <typename T, int G>
+__device__ __forceinline__ void planes_dot(const Planes &pl, uint16_t *list, WordRange wr,
+                                           const SpecSet<T, G> &ss, float (&acc)[G],
+                                           int *n_distinct = nullptr) {
+    const int nt = planes_accumulate<G>(pl, list, wr, RowDot<T, G>{ss}, acc);
+    butterfly_all<G>(acc);
+    if (n_distinct) *n_distinct = nt;
 }
 
 // ---------------------------------------------------------------- top-K ---

@@ -363,7 +363,8 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
                        uint64_t *out_k, uint32_t *out_pep, int64_t *out_ncand) {
     cudaError_t e;
     const int32_t ns = b.nspec;
-    const int32_t G = p->group_size > 0 ? p->group_size : 8;
+    // one 16-byte tile load per bin: 8 BF16/FP16 or 4 FP32 spectra per group
+    const int32_t G = p->group_size > 0 ? p->group_size : (elem_kind == 0 ? 4 : 8);
     const int32_t chunk = p->chunk > 0 ? p->chunk : 1024;
     if (G != 1 && G != 2 && G != 4 && G != 8) return fail(ctx, HFX_ERR_ARG, "group_size must be 1, 2, 4 or 8");
     const int32_t K = elem_kind == 0 ? p->top_n : std::max(p->top_n, std::min(p->rescore_k > 0 ? p->rescore_k : 32,
@@ -403,7 +404,11 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     uint32_t hs[4];
     HFX_CUDA(cudaMemcpyAsync(hs, scal, 16, cudaMemcpyDeviceToHost, ctx->stream), "D2H plan");
     HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    const uint32_t ngroups = hs[1];
     const uint32_t total_items = hs[2];
+    const size_t esz = elem_kind == 0 ? 4 : 2;
+    void *tiles = ctx->buf<uint8_t>("tiles", (size_t)ngroups * stride * G * esz + 64, e);
+    if (e) return cuda_fail(ctx, e, "alloc tiles");
     float *ps = ctx->buf<float>("part_s", (size_t)total_items * G * K + 1, e);
     if (e) return cuda_fail(ctx, e, "alloc parts");
     uint64_t *pk = ctx->buf<uint64_t>("part_k", (size_t)total_items * G * K + 1, e);
@@ -411,7 +416,8 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     const DevDB db = ctx->devdb();
     ctx->stage_begin(HFX_STAGE_SCORE);
     rc = hfx_batched_score(db, elem_kind == 0 ? (const void *)rows : rows_lo, elem_kind, stride, meta, wb, we, ws,
-                           G, chunk, K, 8, 0, p->fastdiv, ps, pk, ctx->d_err.as<uint32_t>(), ctx->stream);
+                           tiles, ngroups, G, chunk, K, 0, 0, p->fastdiv, ps, pk, ctx->d_err.as<uint32_t>(),
+                           ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_batched");
     ctx->stage_end(HFX_STAGE_SCORE, 1, 0);
     float *ks = ctx->buf<float>("kept_s", (size_t)ns * K, e);

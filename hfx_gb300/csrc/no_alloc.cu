@@ -57,10 +57,10 @@ __global__ void __launch_bounds__(256) k_score_spectrum_na(DevDB db, const float
     ss.len[0] = len;
     ss.active = 1u;
     for (uint32_t p = begin + blockIdx.x * nw + warp; p < end; p += gridDim.x * nw) {
-        build_planes<FastDiv>(pl, db.ions, db.tc_sorted[p], db.tn_sorted[p], db.r_sorted[p], charges, len,
-                              mt_lane, NoMods{});
+        const WordRange wr = build_planes<FastDiv>(pl, db.ions, db.tc_sorted[p], db.tn_sorted[p],
+                                                   db.r_sorted[p], charges, len, mt_lane, NoMods{});
         float acc[1];
-        planes_dot<float, 1>(pl, list, words, ss, acc);
+        planes_dot<float, 1>(pl, list, wr, ss, acc);
         tk.insert(acc[0], (uint64_t)p, K);
     }
     __syncthreads();

@@ -87,9 +87,9 @@ __global__ void __launch_bounds__(256) k_score_spectrum(DevDB db, const float *_
     for (uint32_t p = begin + blockIdx.x * nw + warp; p < end; p += gridDim.x * nw) {
         const uint32_t tc = db.tc_sorted[p], tn = db.tn_sorted[p];
         const float r = db.r_sorted[p];
-        build_planes<FastDiv>(pl, db.ions, tc, tn, r, charges, len, mt_lane, NoMods{});
+        const WordRange wr = build_planes<FastDiv>(pl, db.ions, tc, tn, r, charges, len, mt_lane, NoMods{});
         float acc[1];
-        planes_dot<float, 1>(pl, list, words, ss, acc);
+        planes_dot<float, 1>(pl, list, wr, ss, acc);
         tk.insert(acc[0], (uint64_t)p, K);
     }
     __syncthreads();
