@@ -50,6 +50,8 @@ def _args():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--out", default="")
+    ap.add_argument("--group-size", type=int, default=0, help="spectra per batched work item (0 = default)")
+    ap.add_argument("--chunk", type=int, default=0, help="candidates per batched work item (0 = default)")
     return ap.parse_args()
 
 
@@ -205,7 +207,7 @@ def main():
     prec = a.precision if a.precision >= 0 else 0
     mode = a.batch_mode if a.batch_mode >= 0 else 0
     p = hfx_gb300.default_params(top_n=cfg["top_n"], bin_width=cfg["bin_width"], precision=prec, batch_mode=mode,
-                                 rescore_k=32 if prec else 0)
+                                 rescore_k=32 if prec else 0, group_size=a.group_size, chunk=a.chunk)
     d = torch.device("cuda", local)
     dev = dict(mz=torch.from_numpy(sp.mz).to(d), it=torch.from_numpy(sp.it).to(d),
                off=torch.from_numpy(sp.off).to(d), pcr=torch.from_numpy(sp.pcr).to(d),
@@ -238,6 +240,7 @@ def main():
     torch.cuda.synchronize()
     clocks = clk.stop()
     stats = eng.stage_stats(reset=True)
+    work = {k: v // a.steps for k, v in eng.counters(reset=True).items()}
     eng.set_profiling(False)
     if world > 1:
         t = torch.tensor([total_ms], device=d)
@@ -295,7 +298,8 @@ def main():
                    "psm_per_step": psm_step, "precision": ["fp32", "bf16+fp32 rescore", "fp16+fp32 rescore"][prec],
                    "batch_mode": ["per-spectrum launches", "persistent batched"][mode],
                    "l2": "flushed between timed steps (512 MB write)",
-                   "stage_ms_per_step": {k: v[0] / a.steps for k, v in stats.items() if v[1]}},
+                   "stage_ms_per_step": {k: v[0] / a.steps for k, v in stats.items() if v[1]},
+                   "work_per_step": work},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches_per_step),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

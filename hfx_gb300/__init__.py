@@ -31,9 +31,9 @@ EXPORTED = [
     "hfx_last_error", "hfx_build_db", "hfx_upload_db", "hfx_db_info", "hfx_db_export",
     "hfx_set_mods", "hfx_mod_table", "hfx_search_host", "hfx_search_device",
     "hfx_preprocess", "hfx_find_windows", "hfx_ion_bins", "hfx_digest", "hfx_pack_ions",
-    "hfx_set_profiling", "hfx_stage_stats",
+    "hfx_set_profiling", "hfx_stage_stats", "hfx_search_counters",
 ]
-STAGES = ["layout", "preprocess", "windows", "score", "topn", "rescore", "mods", "spare"]
+STAGES = ["layout", "preprocess", "windows", "score", "topn", "rescore", "mods", "lists"]
 
 
 class HfxError(RuntimeError):
@@ -96,6 +96,7 @@ def load_library(path: str = LIB_PATH):
         "hfx_pack_ions": (i32, [P, u64, P, i32, P]),
         "hfx_set_profiling": (i32, [P, i32]),
         "hfx_stage_stats": (i32, [P, P, P, P, i32]),
+        "hfx_search_counters": (i32, [P, P, i32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -199,6 +200,13 @@ class Engine:
         nu = np.zeros(8, np.int64)
         self._check(self.lib.hfx_stage_stats(self.h, _ptr(ms), _ptr(nl), _ptr(nu), int(reset)))
         return {STAGES[i]: (float(ms[i]), int(nl[i]), int(nu[i])) for i in range(8)}
+
+    def counters(self, reset: bool = True):
+        """Work counters of the batched list path (see hfx_search_counters)."""
+        c = np.zeros(8, np.uint64)
+        self._check(self.lib.hfx_search_counters(self.h, _ptr(c), int(reset)))
+        names = ["lists", "list_entries", "candidates", "entries_streamed", "pairs"]
+        return {n: int(c[i]) for i, n in enumerate(names)}
 
     def set_stream(self, stream_ptr: int):
         self._check(self.lib.hfx_set_stream(self.h, stream_ptr))

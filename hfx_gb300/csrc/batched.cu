@@ -20,24 +20,22 @@
 #include "hfx_internal.h"
 #include "device_common.cuh"
 #include "batched.h"
+#include "batched_common.cuh"
 
 namespace hfx {
 
 constexpr int kMassBuckets = 8192;   // 1 Da buckets of residual mass
 constexpr int kClasses = 10;         // (ion charges 0..4) x (narrow, wide)
 constexpr float kWideEps = 1.0f;     // windows wider than this are "wide"
-constexpr uint32_t kWaitLimit = 1u << 24;
 
-// Bins of a group tile that the scorer copies (a multiple of 8 keeps every
-// bulk copy a multiple of 16 bytes).
-__host__ __device__ __forceinline__ int32_t tile_bins(int32_t maxlen) { return (maxlen + 7) & ~7; }
-
-// Shared memory of one scorer warp: bit planes + distinct-bin list, then the
-// per-member top-K lists (scores, keys) and admission thresholds.
-__host__ __device__ __forceinline__ size_t batched_warp_bytes(int32_t words, int G, int K) {
-    const size_t a = ((size_t)3 * words * 4 + (size_t)kListCap * 2 + 15) & ~(size_t)15;
-    const size_t b = (size_t)G * K * 4 + (size_t)((G * K) & 1) * 4 + (size_t)G * K * 8 + (size_t)G * 4;
-    return (a + b + 15) & ~(size_t)15;
+// Shared memory of one scorer warp: bit planes + distinct-bin list.
+__host__ __device__ __forceinline__ size_t batched_warp_bytes(int32_t words) {
+    return ((size_t)3 * words * 4 + (size_t)kListCap * 2 + 15) & ~(size_t)15;
+}
+// CTA-wide top-K lists: scores (padded to 8 bytes), keys, thresholds, locks.
+__host__ __device__ __forceinline__ size_t batched_cta_bytes(int G, int K) {
+    const size_t b = (size_t)((G * K + 1) & ~1) * 4 + (size_t)G * K * 8 + (size_t)G * 4 + (size_t)G * 4;
+    return (b + 15) & ~(size_t)15;
 }
 
 __device__ __forceinline__ int spec_class(const SpecMeta &m) {
@@ -161,86 +159,8 @@ __global__ void k_groups(const uint32_t *__restrict__ bucket_off, const uint32_t
     nchunks[g] = (gi.hi - gi.lo + (uint32_t)chunk - 1) / (uint32_t)chunk;
 }
 
-__device__ __forceinline__ int32_t find_group(const uint32_t *__restrict__ item_off, int32_t ngroups, uint32_t item) {
-    // last g with item_off[g] <= item
-    int32_t lo = 0, hi = ngroups;
-    while (hi - lo > 1) {
-        const int32_t mid = (lo + hi) >> 1;
-        if (item_off[mid] <= item) lo = mid; else hi = mid;
-    }
-    return lo;
-}
-
-// Interleave each group's member rows bin-major, tile[g][bin][G]: zero
-// rows for empty slots and zeros beyond each member's length, so that the
-// scorer needs neither a per-member length test nor a per-member load.
-template <typename T> __device__ __forceinline__ T zero_of();
-template <> __device__ __forceinline__ float zero_of<float>() { return 0.0f; }
-template <> __device__ __forceinline__ __nv_bfloat16 zero_of<__nv_bfloat16>() { return __float2bfloat16_rn(0.0f); }
-template <> __device__ __forceinline__ __half zero_of<__half>() { return __float2half_rn(0.0f); }
-
-template <typename T, int G>
-struct alignas((G * sizeof(T) >= 16) ? 16 : G * sizeof(T)) TilePack {
-    T v[G];
-};
-
-template <typename T, int G>
-__global__ void k_pack_tiles(const T *__restrict__ rows, int64_t stride, const SpecMeta *__restrict__ meta,
-                             const int32_t *__restrict__ perm, const GroupInfo *__restrict__ groups,
-                             const uint32_t *__restrict__ ngroups_p, T *__restrict__ tiles) {
-    const uint32_t g = blockIdx.x;
-    if (g >= *ngroups_p) return;
-    const GroupInfo gi = groups[g];
-    __shared__ int32_t s_spec[G], s_len[G];
-    if (threadIdx.x < G) {
-        const int j = threadIdx.x;
-        const int32_t s = j < (int)gi.count ? perm[gi.pos0 + j] : -1;
-        s_spec[j] = s;
-        s_len[j] = s >= 0 ? meta[s].len : 0;
-    }
-    __syncthreads();
-    T *tile = tiles + (size_t)g * stride * G;
-    const int32_t nb = tile_bins(gi.maxlen);
-    for (int32_t b = threadIdx.x; b < nb; b += blockDim.x) {
-        TilePack<T, G> pk;
-#pragma unroll
-        for (int j = 0; j < G; ++j)
-            pk.v[j] = (s_spec[j] >= 0 && b < s_len[j]) ? rows[(size_t)s_spec[j] * stride + b] : zero_of<T>();
-        *reinterpret_cast<TilePack<T, G> *>(tile + (size_t)b * G) = pk;
-    }
-}
-
-// Warp-cooperative insert into a sorted shared-memory list (entry i at
-// lane i); returns the new K-th score (the admission threshold).
-__device__ __forceinline__ float smem_topk_insert(float *ks, uint64_t *kk, float ns, uint64_t nk, int K) {
-    const int lane = threadIdx.x & 31;
-    const float cs = lane < K ? ks[lane] : -INFINITY;
-    const uint64_t ck = lane < K ? kk[lane] : ~0ull;
-    const bool mine_better = (lane < K) && better(cs, ck, ns, nk);
-    const int pos = __popc(__ballot_sync(kFullMask, mine_better));
-    const float us = __shfl_up_sync(kFullMask, cs, 1);
-    const uint64_t uk = __shfl_up_sync(kFullMask, ck, 1);
-    float out = cs;
-    __syncwarp();
-    if (pos < K) {
-        if (lane == pos) { ks[lane] = ns; kk[lane] = nk; out = ns; }
-        else if (lane > pos && lane < K) { ks[lane] = us; kk[lane] = uk; out = us; }
-    }
-    __syncwarp();
-    return __shfl_sync(kFullMask, out, K - 1);
-}
-
-template <int G>
-__device__ __forceinline__ uint32_t slot_owner_mask() {
-    // one lane per slot among the lanes that hold the same reduced slot
-    if constexpr (G == 8) return 0x11111111u;
-    else if constexpr (G == 4) return 0x01010101u;
-    else if constexpr (G == 2) return 0x00010001u;
-    else return 0x1u;
-}
-
 template <bool FastDiv, typename T, int G>
-__global__ void __launch_bounds__(512, 1)
+__global__ void __launch_bounds__(768, 1)
 k_score_batched(DevDB db, const T *__restrict__ tiles, int64_t stride, const uint32_t *__restrict__ wb,
                 const uint32_t *__restrict__ we, const int32_t *__restrict__ perm,
                 const GroupInfo *__restrict__ groups, const uint32_t *__restrict__ item_off,
@@ -251,15 +171,17 @@ k_score_batched(DevDB db, const T *__restrict__ tiles, int64_t stride, const uin
     const int32_t words_cap = (int32_t)((stride + 31) / 32);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     T *stile = reinterpret_cast<T *>(smem + 128);
-    const size_t tile_bytes = (size_t)stride * G * sizeof(T);
-    const size_t warp_bytes = batched_warp_bytes(words_cap, G, K);
-    uint8_t *wbase = smem + 128 + ((tile_bytes + 15) & ~(size_t)15) + (size_t)warp * warp_bytes;
+    const size_t tile_bytes = ((size_t)stride * G * sizeof(T) + 15) & ~(size_t)15;
+    // CTA-wide top-K per member spectrum: scores, keys, admission thresholds, locks
+    float *tk_s = reinterpret_cast<float *>(smem + 128 + tile_bytes);
+    uint64_t *tk_k = reinterpret_cast<uint64_t *>(tk_s + ((G * K + 1) & ~1));
+    float *thr = reinterpret_cast<float *>(tk_k + G * K);
+    uint32_t *locks = reinterpret_cast<uint32_t *>(thr + G);
+    uint8_t *wbase = smem + 128 + tile_bytes + batched_cta_bytes(G, K) + (size_t)warp * batched_warp_bytes(words_cap);
     uint32_t *planes = reinterpret_cast<uint32_t *>(wbase);
     uint16_t *list = reinterpret_cast<uint16_t *>(planes + 3 * words_cap);
-    float *tk_s = reinterpret_cast<float *>(wbase + ((3 * words_cap * 4 + kListCap * 2 + 15) & ~15));
-    uint64_t *tk_k = reinterpret_cast<uint64_t *>(tk_s + G * K + ((G * K) & 1));
-    float *thr = reinterpret_cast<float *>(tk_k + G * K);
     __shared__ int32_t s_item;
+    __shared__ uint32_t s_next;
     __shared__ uint32_t s_wb[G], s_we[G];
 
     const int32_t ngroups = (int32_t)*ngroups_p;
@@ -293,11 +215,15 @@ k_score_batched(DevDB db, const T *__restrict__ tiles, int64_t stride, const uin
             s_wb[j] = b;
             s_we[j] = e;
         }
-        for (int i = lane; i < G * K; i += 32) {
+        for (int i = threadIdx.x; i < G * K; i += blockDim.x) {
             tk_s[i] = -INFINITY;
             tk_k[i] = ~0ull;
         }
-        if (lane < G) thr[lane] = -INFINITY;
+        if (threadIdx.x < G) {
+            thr[threadIdx.x] = -INFINITY;
+            locks[threadIdx.x] = 0u;
+        }
+        if (threadIdx.x == 0) s_next = p0;
         const int32_t nb = tile_bins(gi.maxlen);
         if (threadIdx.x == 0) {
             fence_proxy_async();
@@ -313,7 +239,12 @@ k_score_batched(DevDB db, const T *__restrict__ tiles, int64_t stride, const uin
         phase ^= 1u;
         const uint32_t my_b = lane < G ? s_wb[lane] : 0u, my_e = lane < G ? s_we[lane] : 0u;
         const TileDot<T, G> dot{stile};
-        for (uint32_t p = p0 + warp; p < p1; p += nw) {
+        while (true) {
+            // candidates are handed out one at a time so that warps finish together
+            uint32_t p = 0;
+            if (lane == 0) p = atomicAdd(&s_next, 1u);
+            p = __shfl_sync(kFullMask, p, 0);
+            if (p >= p1) break;
             const uint32_t act = __ballot_sync(kFullMask, lane < G && my_b <= p && p < my_e) & ((1u << G) - 1u);
             if (!act) continue;
             const WordRange wr = build_planes<FastDiv>(pl, db.ions, db.tc_sorted[p], db.tn_sorted[p],
@@ -329,31 +260,33 @@ k_score_batched(DevDB db, const T *__restrict__ tiles, int64_t stride, const uin
                 ins &= ins - 1u;
                 const int j = reduce_slot_of_lane<G>(src);
                 const float s = __shfl_sync(kFullMask, sc, src);
+                // the CTA's list of member j is updated under a short lock;
+                // the wait is bounded and reported, never endless
+                uint32_t ok = 1u;
+                if (lane == 0) {
+                    uint32_t n = 0;
+                    while (atomicCAS(&locks[j], 0u, 1u) != 0u) {
+                        if (++n > kLockLimit) { ok = 0u; break; }
+                    }
+                }
+                ok = __shfl_sync(kFullMask, ok, 0);
+                if (!ok) {
+                    if (lane == 0) atomicOr(err, kErrTimeout);
+                    continue;
+                }
+                __threadfence_block();
                 const float t = smem_topk_insert(tk_s + j * K, tk_k + j * K, s, (uint64_t)p, K);
                 if (lane == 0) thr[j] = t;
+                __threadfence_block();
                 __syncwarp();
+                if (lane == 0) atomicExch(&locks[j], 0u);
             }
         }
         __syncthreads();
-        // merge the warps' lists of every member
-        for (int j = warp; j < cnt; j += nw) {
-            WarpTopK m;
-            m.init();
-            for (int w = 0; w < nw; ++w) {
-                const uint8_t *ob = smem + 128 + ((tile_bytes + 15) & ~(size_t)15) + (size_t)w * warp_bytes;
-                const float *os = reinterpret_cast<const float *>(ob + ((3 * words_cap * 4 + kListCap * 2 + 15) & ~15));
-                const uint64_t *ok = reinterpret_cast<const uint64_t *>(os + G * K + ((G * K) & 1));
-                const float vs = lane < K ? os[j * K + lane] : -INFINITY;
-                const uint64_t vk = lane < K ? ok[j * K + lane] : ~0ull;
-                const int nvalid = __popc(__ballot_sync(kFullMask, vk != ~0ull));
-                for (int t = 0; t < nvalid; ++t)
-                    m.insert(__shfl_sync(kFullMask, vs, t), __shfl_sync(kFullMask, vk, t), K);
-            }
-            if (lane < K) {
-                const size_t o = ((size_t)item * G + j) * K + lane;
-                part_s[o] = m.s;
-                part_k[o] = m.k;
-            }
+        for (int i = threadIdx.x; i < cnt * K; i += blockDim.x) {
+            const size_t o = (size_t)item * G * K + i;
+            part_s[o] = tk_s[i];
+            part_k[o] = tk_k[i];
         }
         __syncthreads();
     }
@@ -480,7 +413,7 @@ using namespace hfx;
 size_t hfx_batched_smem(int64_t stride, int elem_bytes, int G, int nw, int K) {
     const int32_t words = (int32_t)((stride + 31) / 32);
     const size_t tile = ((size_t)stride * G * elem_bytes + 15) & ~(size_t)15;
-    return 128 + tile + (size_t)nw * batched_warp_bytes(words, G, K);
+    return 128 + tile + batched_cta_bytes(G, K) + (size_t)nw * batched_warp_bytes(words);
 }
 
 int hfx_batched_plan(const SpecMeta *meta, int32_t nspec, const uint32_t *wb, const uint32_t *we, int32_t G,
@@ -505,8 +438,7 @@ static int launch_batched_t(const DevDB &db, const T *rows, int64_t stride, cons
                             const uint32_t *we, const BatchedWs &ws, void *tiles, uint32_t ngroups, int32_t chunk,
                             int32_t K, int nw, int grid, float *part_s, uint64_t *part_k, uint32_t *err,
                             cudaStream_t st) {
-    if (ngroups > 0)
-        k_pack_tiles<T, G><<<ngroups, 256, 0, st>>>(rows, stride, meta, ws.perm, ws.groups, ws.ngroups, (T *)tiles);
+    if (ngroups > 0) hfx_pack_tiles_launch<T, G>(rows, stride, meta, ws, (T *)tiles, ngroups, st);
     int dev = 0, sms = 0, smem_max = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -514,8 +446,8 @@ static int launch_batched_t(const DevDB &db, const T *rows, int64_t stride, cons
     const int32_t words = (int32_t)((stride + 31) / 32);
     if (nw <= 0) {
         const size_t fixed = hfx_batched_smem(stride, sizeof(T), G, 0, K);
-        const size_t per = batched_warp_bytes(words, G, K);
-        nw = (int)std::min<size_t>(16, fixed < (size_t)smem_max ? ((size_t)smem_max - fixed) / per : 0);
+        const size_t per = batched_warp_bytes(words);
+        nw = (int)std::min<size_t>(24, fixed < (size_t)smem_max ? ((size_t)smem_max - fixed) / per : 0);
         if (nw < 1) return (int)cudaErrorInvalidValue;
     }
     const size_t smem = hfx_batched_smem(stride, sizeof(T), G, nw, K);

@@ -154,6 +154,12 @@ struct WordRange {
     int32_t lo, hi;
 };
 
+template <bool FastDiv, typename Mods>
+__device__ __forceinline__ WordRange build_planes_range(const Planes &pl, const uint8_t *__restrict__ ions,
+                                                        uint32_t tc, uint32_t tn, float residual, int c_first,
+                                                        int c_last, int32_t nbins, float mt_lane,
+                                                        const Mods &mods);
+
 // Build the ion bit planes of one candidate.  Residues [tc, tn) of `ions`,
 // `charges` ion charges (0 = none), bins >= nbins dropped.  Returns the
 // range of plane words that may hold set bits (warp-uniform).
@@ -162,9 +168,20 @@ __device__ __forceinline__ WordRange build_planes(const Planes &pl, const uint8_
                                                   uint32_t tc, uint32_t tn, float residual,
                                                   int charges, int32_t nbins, float mt_lane,
                                                   const Mods &mods) {
+    return build_planes_range<FastDiv>(pl, ions, tc, tn, residual, 1, charges, nbins, mt_lane, mods);
+}
+
+// The same for ion charges c_first..c_last only (bits accumulate in the
+// planes, so successive calls build the cumulative charge levels).
+template <bool FastDiv, typename Mods>
+__device__ __forceinline__ WordRange build_planes_range(const Planes &pl, const uint8_t *__restrict__ ions,
+                                                        uint32_t tc, uint32_t tn, float residual, int c_first,
+                                                        int c_last, int32_t nbins, float mt_lane,
+                                                        const Mods &mods) {
     const int lane = threadIdx.x & 31;
     BinRange br;
-    if (charges <= 0) return WordRange{0, 0};
+    const int charges = c_last - c_first + 1;
+    if (c_last <= 0 || charges <= 0) return WordRange{0, 0};
     float carry = 0.0f;
     for (uint32_t base = tc; base < tn; base += 32) {
         const int cnt = (int)min(32u, tn - base);
@@ -191,7 +208,7 @@ __device__ __forceinline__ WordRange build_planes(const Planes &pl, const uint8_
             const float bk = __shfl_sync(kFullMask, v, k & 31);
             const float yk = __shfl_sync(kFullMask, y, k & 31);
             if (it < items) {
-                const ChargeConst kc = charge_const<FastDiv>(cm1 + 1);
+                const ChargeConst kc = charge_const<FastDiv>(c_first + cm1);
                 emit_ions<FastDiv>(pl, bk, yk, kc, nbins, br);
             }
         }

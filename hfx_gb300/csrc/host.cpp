@@ -9,6 +9,7 @@
 #include "hfx_internal.h"
 #include "search_kernels.h"
 #include "batched.h"
+#include "lists.h"
 #include "../../include/hfx_gpu.h"
 
 #include <algorithm>
@@ -75,6 +76,9 @@ struct hfx_ctx {
     std::string err;
     // database (residual-mass order on the device)
     uint64_t num_ions = 0, num_pep = 0;
+    uint64_t ladder_residues = 0;  // sum over fragments of (tn - tc)
+    DBuf d_lstart;                 // per mass-order position: 10 * prefix sum of (tn - tc)
+    unsigned long long counters[8] = {0};
     float mt[26] = {0};
     std::vector<uint8_t> h_ascii;
     std::vector<float> h_r;        // fragment order
@@ -179,11 +183,17 @@ int32_t upload_db(hfx_ctx *ctx) {
                      [&](uint32_t a, uint32_t b) { return ctx->h_r[a] < ctx->h_r[b]; });
     std::vector<float> rs(np);
     std::vector<uint32_t> tcs(np), tns(np);
+    ctx->ladder_residues = 0;
+    std::vector<uint32_t> lstart(np);
     for (uint64_t i = 0; i < np; ++i) {
         rs[i] = ctx->h_r[ctx->h_idx[i]];
         tcs[i] = ctx->h_tc[ctx->h_idx[i]];
         tns[i] = ctx->h_tn[ctx->h_idx[i]];
         if (tns[i] < tcs[i] || tns[i] > ctx->num_ions) return fail(ctx, HFX_ERR_ARG, "fragment outside the residues");
+        if (10ull * ctx->ladder_residues > 0xFFFFFFFFull)
+            return fail(ctx, HFX_ERR_UNSUPPORTED, "ion-list offsets exceed 32 bits");
+        lstart[i] = (uint32_t)(10ull * ctx->ladder_residues);
+        ctx->ladder_residues += tns[i] - tcs[i];
     }
     std::vector<uint8_t> packed;
     pack_ions(ctx->h_ascii, ctx->ma, ctx->num_ma, packed);
@@ -198,6 +208,8 @@ int32_t upload_db(hfx_ctx *ctx) {
     HFX_CUDA(cudaMemcpy(ctx->d_tc.p, tcs.data(), np * 4, cudaMemcpyHostToDevice), "H2D tc");
     HFX_CUDA(cudaMemcpy(ctx->d_tn.p, tns.data(), np * 4, cudaMemcpyHostToDevice), "H2D tn");
     HFX_CUDA(cudaMemcpy(ctx->d_idx.p, ctx->h_idx.data(), np * 4, cudaMemcpyHostToDevice), "H2D idx");
+    HFX_CUDA(ctx->d_lstart.ensure(np * 4 + 16), "alloc lstart");
+    HFX_CUDA(cudaMemcpy(ctx->d_lstart.p, lstart.data(), np * 4, cudaMemcpyHostToDevice), "H2D lstart");
     return HFX_OK;
 }
 
@@ -414,12 +426,56 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     uint64_t *pk = ctx->buf<uint64_t>("part_k", (size_t)total_items * G * K + 1, e);
     if (e) return cuda_fail(ctx, e, "alloc parts");
     const DevDB db = ctx->devdb();
-    ctx->stage_begin(HFX_STAGE_SCORE);
-    rc = hfx_batched_score(db, elem_kind == 0 ? (const void *)rows : rows_lo, elem_kind, stride, meta, wb, we, ws,
-                           tiles, ngroups, G, chunk, K, 0, 0, p->fastdiv, ps, pk, ctx->d_err.as<uint32_t>(),
-                           ctx->stream);
-    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_batched");
-    ctx->stage_end(HFX_STAGE_SCORE, 1, 0);
+    const void *src_rows = elem_kind == 0 ? (const void *)rows : rows_lo;
+    if (p->batch_mode == 2) {
+        // fused: every work item rebuilds its candidates' ion lists
+        ctx->stage_begin(HFX_STAGE_SCORE);
+        rc = hfx_batched_score(db, src_rows, elem_kind, stride, meta, wb, we, ws, tiles, ngroups, G, chunk, K, 0, 0,
+                               p->fastdiv, ps, pk, ctx->d_err.as<uint32_t>(), ctx->stream);
+        if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_batched");
+        ctx->stage_end(HFX_STAGE_SCORE, 2, 0);
+    } else {
+        // lists: one ion list per needed (peptide, charge level), then scoring
+        const int64_t npep1 = (int64_t)ctx->num_pep + 1;
+        int32_t *diff = ctx->buf<int32_t>("l_diff", (size_t)kLevels * npep1, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        int32_t *cover = ctx->buf<int32_t>("l_cover", (size_t)kLevels * npep1, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        int32_t *partial = ctx->buf<int32_t>("l_partial", hfx_scan_partials_needed(kLevels * npep1), e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        uint16_t *llen = ctx->buf<uint16_t>("l_len", (size_t)kLevels * ctx->num_pep, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        // static slots: 10 ions per prefix and charge, levels 1..4 (1+2+3+4)
+        const uint64_t total10 = 10ull * ctx->ladder_residues;
+        uint16_t *lists = ctx->buf<uint16_t>("l_lists", total10 * 10 + 64, e);
+        if (e) return cuda_fail(ctx, e, "alloc lists");
+        unsigned long long *stats = nullptr;
+        if (ctx->profile) {
+            stats = ctx->buf<unsigned long long>("l_stats", 8, e);
+            if (e) return cuda_fail(ctx, e, "alloc");
+            HFX_CUDA(cudaMemsetAsync(stats, 0, 64, ctx->stream), "memset");
+        }
+        ctx->stage_begin(HFX_STAGE_LISTS);
+        rc = hfx_lists_mark(meta, wb, we, ns, npep1, diff, ctx->stream);
+        if (!rc) rc = hfx_scan_inclusive(diff, kLevels * npep1, cover, partial, ctx->stream);
+        if (!rc)
+            rc = hfx_lists_generate(db, cover, npep1, kMaxWords * 32, ctx->d_lstart.as<uint32_t>(), total10, lists,
+                                    llen, p->fastdiv, stats, ctx->d_err.as<uint32_t>(), ctx->stream);
+        if (rc) return cuda_fail(ctx, (cudaError_t)rc, "ion lists");
+        ctx->stage_end(HFX_STAGE_LISTS, 5, 0);
+        ctx->stage_begin(HFX_STAGE_SCORE);
+        rc = hfx_lists_score(lists, ctx->d_lstart.as<uint32_t>(), total10, llen, (uint32_t)ctx->num_pep, src_rows,
+                             elem_kind, stride, meta, wb, we, ws, tiles, ngroups, G, chunk, K, 0, ps, pk, stats,
+                             ctx->d_err.as<uint32_t>(), ctx->stream);
+        if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_lists");
+        ctx->stage_end(HFX_STAGE_SCORE, 2, 0);
+        if (stats) {
+            unsigned long long h[8];
+            HFX_CUDA(cudaMemcpyAsync(h, stats, 64, cudaMemcpyDeviceToHost, ctx->stream), "D2H stats");
+            HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+            for (int i = 0; i < 8; ++i) ctx->counters[i] += h[i];
+        }
+    }
     float *ks = ctx->buf<float>("kept_s", (size_t)ns * K, e);
     if (e) return cuda_fail(ctx, e, "alloc");
     uint64_t *kk = ctx->buf<uint64_t>("kept_k", (size_t)ns * K, e);
@@ -527,6 +583,7 @@ int32_t hfx_ctx_destroy(hfx_ctx *ctx) {
     ctx->d_tc.release();
     ctx->d_tn.release();
     ctx->d_idx.release();
+    ctx->d_lstart.release();
     ctx->d_mod_counts.release();
     ctx->d_mod_delta.release();
     ctx->d_err.release();
@@ -551,6 +608,15 @@ const char *hfx_last_error(const hfx_ctx *ctx) { return ctx ? ctx->err.c_str() :
 int32_t hfx_set_profiling(hfx_ctx *ctx, int32_t on) {
     if (!ctx) return HFX_ERR_ARG;
     ctx->profile = on != 0;
+    return HFX_OK;
+}
+
+int32_t hfx_search_counters(hfx_ctx *ctx, uint64_t *out8, int32_t reset) {
+    if (!ctx || !out8) return HFX_ERR_ARG;
+    for (int i = 0; i < 8; ++i) {
+        out8[i] = ctx->counters[i];
+        if (reset) ctx->counters[i] = 0;
+    }
     return HFX_OK;
 }
 

@@ -1,0 +1,489 @@
+// List-based batched scoring (the default batched path for unmodified
+// candidates).
+//
+// Within one search step every candidate peptide is scored against many
+// spectra (the +-tolerance windows of neighbouring spectra overlap).  So the
+// step first builds, ONCE per (peptide, ion-charge level) that some spectrum
+// of the batch needs, the ascending list of distinct ion bins with their
+// intensity levels (ion_series.cu:78-123 with the max-dedupe of
+// ion_series.cu:71-75), and stores it in HBM.  The scorer then streams a
+// candidate's list -- entry i read by lane i % 32, which is exactly the
+// canonical accumulation order -- and gathers the group tile in shared
+// memory.  Nothing is reused across steps: the lists are rebuilt by every
+// search.
+//
+// Which (peptide, level) pairs are needed: every spectrum adds its window
+// [begin, end) to a difference array of its level; a prefix sum marks the
+// covered peptides.
+#include "hfx_internal.h"
+#include "device_common.cuh"
+#include "batched.h"
+#include "lists.h"
+#include "batched_common.cuh"
+
+namespace hfx {
+
+constexpr int kScanTile = 4096;
+
+// ---- multi-block inclusive scan of int32 (reduce, scan partials, apply) ----
+__global__ void k_scan_reduce(const int32_t *__restrict__ a, int64_t n, int32_t *__restrict__ partial) {
+    __shared__ int32_t red[32];
+    const int64_t base = (int64_t)blockIdx.x * kScanTile;
+    int32_t s = 0;
+    for (int i = threadIdx.x; i < kScanTile; i += blockDim.x)
+        if (base + i < n) s += a[base + i];
+    s = __reduce_add_sync(kFullMask, s);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int32_t v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0;
+        v = __reduce_add_sync(kFullMask, v);
+        if (threadIdx.x == 0) partial[blockIdx.x] = v;
+    }
+}
+
+__global__ void k_scan_partials(int32_t *__restrict__ partial, int32_t nb) {
+    // single CTA, exclusive scan in place
+    __shared__ int32_t ws[32];
+    __shared__ int32_t carry;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int32_t b0 = 0; b0 < nb; b0 += blockDim.x) {
+        const int32_t i = b0 + threadIdx.x;
+        const int32_t v = i < nb ? partial[i] : 0;
+        const int32_t x = warp_incl_scan(v);
+        if (lane == 31) ws[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            int32_t w = lane < (int)(blockDim.x >> 5) ? ws[lane] : 0;
+            w = warp_incl_scan(w);
+            ws[lane] = w;
+        }
+        __syncthreads();
+        const int32_t before = carry + (warp ? ws[warp - 1] : 0);
+        if (i < nb) partial[i] = before + x - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = before + x;
+        __syncthreads();
+    }
+}
+
+// Inclusive scan of one tile with its block offset: out[i] = sum a[0..i].
+__global__ void k_scan_apply(const int32_t *__restrict__ a, int64_t n, const int32_t *__restrict__ partial,
+                             int32_t *__restrict__ out) {
+    __shared__ int32_t ws[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t base = (int64_t)blockIdx.x * kScanTile;
+    const int per = kScanTile / blockDim.x;  // consecutive elements per thread
+    int32_t loc[16];
+    int32_t s = 0;
+    for (int k = 0; k < per; ++k) {
+        const int64_t i = base + (int64_t)threadIdx.x * per + k;
+        loc[k] = i < n ? a[i] : 0;
+        s += loc[k];
+    }
+    const int32_t x = warp_incl_scan(s);
+    if (lane == 31) ws[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int32_t w = lane < (int)(blockDim.x >> 5) ? ws[lane] : 0;
+        w = warp_incl_scan(w);
+        ws[lane] = w;
+    }
+    __syncthreads();
+    int32_t run = partial[blockIdx.x] + (warp ? ws[warp - 1] : 0) + x - s;
+    for (int k = 0; k < per; ++k) {
+        const int64_t i = base + (int64_t)threadIdx.x * per + k;
+        run += loc[k];
+        if (i < n) out[i] = run;
+    }
+}
+
+// ---- which (peptide, level) lists the batch needs ----
+__global__ void k_mark_levels(const SpecMeta *__restrict__ meta, const uint32_t *__restrict__ wb,
+                              const uint32_t *__restrict__ we, int32_t nspec, int64_t npep1,
+                              int32_t *__restrict__ diff) {
+    const int32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nspec) return;
+    const SpecMeta m = meta[s];
+    const int z = m.charges_plain;
+    if (m.status != 0 || z < 1 || z > kLevels || we[s] <= wb[s]) return;
+    atomicAdd(&diff[(int64_t)(z - 1) * npep1 + wb[s]], 1);
+    atomicAdd(&diff[(int64_t)(z - 1) * npep1 + we[s]], -1);
+}
+
+// Warp-cooperative compaction of plane words [wr.lo, wr.hi) into the
+// ascending distinct-bin list `list` (entries (bin << 2) | level); clears the
+// words when `clear`.  Returns the number of distinct bins (may exceed cap;
+// entries beyond cap are dropped).
+__device__ __forceinline__ int compact_planes(const Planes &pl, WordRange wr, bool clear, uint16_t *list, int cap) {
+    const int lane = threadIdx.x & 31;
+    int n = 0;
+    for (int w0 = wr.lo; w0 < wr.hi; w0 += 32) {
+        const int w = w0 + lane;
+        uint32_t a = 0, h = 0, tt = 0;
+        if (w < wr.hi) {
+            h = pl.H[w];
+            tt = pl.T[w];
+            a = pl.A[w] | h;
+            if (clear) {
+                pl.A[w] = 0u;
+                pl.H[w] = 0u;
+                pl.T[w] = 0u;
+            }
+        }
+        const int pc = __popc(a);
+        const int incl = warp_incl_scan(pc);
+        int pos = n + incl - pc;
+        while (a) {
+            const int b = __ffs(a) - 1;
+            a &= a - 1u;
+            const uint32_t l3 = ((tt >> b) & 1u) ? 3u : (((h >> b) & 1u) ? 2u : 1u);
+            if (pos < cap) list[pos] = (uint16_t)((((uint32_t)w << 5 | (uint32_t)b) << 2) | l3);
+            ++pos;
+        }
+        n += __shfl_sync(kFullMask, incl, 31);
+    }
+    __syncwarp();
+    return n;
+}
+
+// Offset of the list of (level z, mass-order position p): every level has a
+// static region; position p's slot holds up to 10 * z * (tn - tc) entries.
+__device__ __forceinline__ uint64_t list_offset(const uint32_t *__restrict__ lstart, uint64_t total10, int z,
+                                                uint32_t p) {
+    return total10 * (uint64_t)(z * (z - 1) / 2) + (uint64_t)z * lstart[p];
+}
+
+// One warp per candidate peptide: for every charge level some spectrum of
+// the batch needs, the sorted distinct-bin list, built incrementally (the
+// level-z planes are the level-(z-1) planes plus the charge-z ions).
+template <bool FastDiv>
+__global__ void __launch_bounds__(256) k_gen_lists(DevDB db, const int32_t *__restrict__ cover, int64_t npep1,
+                                                   int32_t nbins, const uint32_t *__restrict__ lstart,
+                                                   uint64_t total10, uint16_t *__restrict__ lists,
+                                                   uint16_t *__restrict__ list_len,
+                                                   unsigned long long *__restrict__ stats,
+                                                   uint32_t *__restrict__ err) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int32_t words = (nbins + 31) / 32;
+    uint32_t *planes = reinterpret_cast<uint32_t *>(smem) + (size_t)warp * 3 * words;
+    uint16_t *list = reinterpret_cast<uint16_t *>(reinterpret_cast<uint32_t *>(smem) + (size_t)nw * 3 * words) +
+                     (size_t)warp * kMaxListLen;
+    __shared__ unsigned long long s_stats[2];
+    if (threadIdx.x < 2) s_stats[threadIdx.x] = 0ull;
+    for (int32_t i = lane; i < 3 * words; i += 32) planes[i] = 0u;
+    __syncthreads();
+    const Planes pl{planes, planes + words, planes + 2 * words};
+    const float mt_lane = db.mt[lane];
+    unsigned long long my_lists = 0, my_entries = 0;
+    for (int64_t t = (int64_t)blockIdx.x * nw + warp; t < (int64_t)db.num_pep; t += (int64_t)gridDim.x * nw) {
+        const uint32_t p = (uint32_t)t;
+        uint32_t need = 0;
+        if (lane < kLevels && cover[(int64_t)lane * npep1 + p] > 0) need = 1u;
+        need = __ballot_sync(kFullMask, need) & ((1u << kLevels) - 1u);
+        if (lane < kLevels && !((need >> lane) & 1u)) list_len[(size_t)lane * db.num_pep + p] = 0;
+        if (!need) continue;
+        const int zmax = 32 - __clz(need);
+        const uint32_t tc = db.tc_sorted[p], tn = db.tn_sorted[p];
+        const float r = db.r_sorted[p];
+        WordRange all{0x7FFFFFFF, 0};
+        for (int z = 1; z <= zmax; ++z) {
+            const WordRange wr = build_planes_range<FastDiv>(pl, db.ions, tc, tn, r, z, z, nbins, mt_lane, NoMods{});
+            if (wr.hi > wr.lo) {
+                all.lo = min(all.lo, wr.lo);
+                all.hi = max(all.hi, wr.hi);
+            }
+            if (!((need >> (z - 1)) & 1u)) continue;
+            const WordRange use = all.hi > all.lo ? all : WordRange{0, 0};
+            int n = compact_planes(pl, use, z == zmax, list, kMaxListLen);
+            if (n > kMaxListLen) {
+                if (lane == 0) atomicOr(err, kErrListOverflow);
+                n = kMaxListLen;
+            }
+            const uint64_t off = list_offset(lstart, total10, z, p);
+            for (int i = lane; i < n; i += 32) lists[off + i] = list[i];
+            if (lane == 0) list_len[(size_t)(z - 1) * db.num_pep + p] = (uint16_t)n;
+            my_lists += 1;
+            my_entries += (unsigned long long)n;
+            __syncwarp();
+        }
+    }
+    if (stats) {
+        if (lane == 0) {
+            atomicAdd(&s_stats[0], my_lists);
+            atomicAdd(&s_stats[1], my_entries);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            atomicAdd(&stats[0], s_stats[0]);
+            atomicAdd(&stats[1], s_stats[1]);
+        }
+    }
+}
+
+// Scorer over precomputed lists: a persistent grid pulls work items (group x
+// candidate chunk); the group's interleaved tile is staged by one bulk copy;
+// a warp streams each candidate's list (entry i by lane i % 32, four loads
+// in flight per lane) and gathers the tile; CTA-wide top-K per member.
+template <typename T, int G>
+__global__ void __launch_bounds__(1024, 1)
+k_score_lists(const uint16_t *__restrict__ lists, const uint32_t *__restrict__ lstart, uint64_t total10,
+              const uint16_t *__restrict__ list_len, uint32_t num_pep, const T *__restrict__ tiles, int64_t stride,
+              const uint32_t *__restrict__ wb, const uint32_t *__restrict__ we, const int32_t *__restrict__ perm,
+              const GroupInfo *__restrict__ groups, const uint32_t *__restrict__ item_off,
+              const uint32_t *__restrict__ ngroups_p, int32_t chunk, int32_t K, uint32_t *__restrict__ counter,
+              float *__restrict__ part_s, uint64_t *__restrict__ part_k, unsigned long long *__restrict__ stats,
+              uint32_t *__restrict__ err) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    const int lane = threadIdx.x & 31;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+    T *stile = reinterpret_cast<T *>(smem + 128);
+    const size_t tile_bytes = ((size_t)stride * G * sizeof(T) + 15) & ~(size_t)15;
+    float *tk_s = reinterpret_cast<float *>(smem + 128 + tile_bytes);
+    uint64_t *tk_k = reinterpret_cast<uint64_t *>(tk_s + ((G * K + 1) & ~1));
+    float *thr = reinterpret_cast<float *>(tk_k + G * K);
+    uint32_t *locks = reinterpret_cast<uint32_t *>(thr + G);
+    __shared__ int32_t s_item;
+    __shared__ uint32_t s_next;
+    __shared__ uint32_t s_wb[G], s_we[G];
+    __shared__ unsigned long long s_stats[3];
+
+    const int32_t ngroups = (int32_t)*ngroups_p;
+    const uint32_t total = item_off[ngroups];
+    if (threadIdx.x == 0) mbar_init(bar, 1);
+    if (threadIdx.x < 3) s_stats[threadIdx.x] = 0ull;
+    __syncthreads();
+    const int my_slot = reduce_slot_of_lane<G>(lane);
+    unsigned long long my_cand = 0, my_entries = 0, my_psm = 0;
+    uint32_t phase = 0;
+    while (true) {
+        if (threadIdx.x == 0) s_item = (int32_t)atomicAdd(counter, 1u);
+        __syncthreads();
+        const uint32_t item = (uint32_t)s_item;
+        if (item >= total) break;
+        const int32_t g = find_group(item_off, ngroups, item);
+        const GroupInfo gi = groups[g];
+        const uint32_t p0 = gi.lo + (item - item_off[g]) * (uint32_t)chunk;
+        const uint32_t p1 = min(gi.hi, p0 + (uint32_t)chunk);
+        const int cnt = (int)gi.count;
+        if (threadIdx.x < G) {
+            const int j = threadIdx.x;
+            uint32_t b = 0, e = 0;
+            if (j < cnt) {
+                const int32_t s = perm[gi.pos0 + j];
+                b = wb[s];
+                e = we[s];
+            }
+            s_wb[j] = b;
+            s_we[j] = e;
+        }
+        for (int i = threadIdx.x; i < G * K; i += blockDim.x) {
+            tk_s[i] = -INFINITY;
+            tk_k[i] = ~0ull;
+        }
+        if (threadIdx.x < G) {
+            thr[threadIdx.x] = -INFINITY;
+            locks[threadIdx.x] = 0u;
+        }
+        if (threadIdx.x == 0) s_next = p0;
+        const int32_t nb = tile_bins(gi.maxlen);
+        if (threadIdx.x == 0) {
+            fence_proxy_async();
+            const uint32_t bytes = (uint32_t)((size_t)nb * G * sizeof(T));
+            mbar_arrive_expect_tx(bar, bytes);
+            bulk_g2s(stile, tiles + (size_t)g * stride * G, bytes, bar);
+        }
+        __syncthreads();
+        if (!mbar_wait(bar, phase, kWaitLimit)) {
+            if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
+            return;
+        }
+        phase ^= 1u;
+        const uint32_t my_b = lane < G ? s_wb[lane] : 0u, my_e = lane < G ? s_we[lane] : 0u;
+        const int z = (int)gi.charges;
+        const uint16_t *llen = list_len + (size_t)(z >= 1 ? z - 1 : 0) * num_pep;
+        while (true) {
+            uint32_t p = 0;
+            if (lane == 0) p = atomicAdd(&s_next, 1u);
+            p = __shfl_sync(kFullMask, p, 0);
+            if (p >= p1) break;
+            const uint32_t act = __ballot_sync(kFullMask, lane < G && my_b <= p && p < my_e) & ((1u << G) - 1u);
+            if (!act) continue;
+            float acc[G];
+#pragma unroll
+            for (int j = 0; j < G; ++j) acc[j] = 0.0f;
+            if (z >= 1) {
+                const int n = llen[p];
+                const uint16_t *lp = lists + list_offset(lstart, total10, z, p);
+                my_cand += 1;
+                my_entries += (unsigned long long)n;
+                my_psm += (unsigned long long)__popc(act);
+                for (int i0 = 0; i0 < n; i0 += 128) {
+                    uint32_t e[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const int i = i0 + 32 * k + lane;
+                        e[k] = i < n ? (uint32_t)__ldg(lp + i) : 0xFFFFFFFFu;
+                    }
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const uint32_t bin = e[k] >> 2;
+                        if ((int32_t)bin < nb) {
+                            const float w = level_weight(e[k] & 3u);
+                            float x[G];
+                            TileLoad<T, G>::load(stile, bin, x);
+#pragma unroll
+                            for (int j = 0; j < G; ++j) acc[j] = __fmaf_rn(w, x[j], acc[j]);
+                        }
+                    }
+                }
+            }
+            const float sc = reduce_scatter<G>(acc);
+            const bool want = ((act >> my_slot) & 1u) && sc >= thr[my_slot];
+            uint32_t ins = __ballot_sync(kFullMask, want) & slot_owner_mask<G>();
+            while (ins) {
+                const int src = __ffs(ins) - 1;
+                ins &= ins - 1u;
+                const int j = reduce_slot_of_lane<G>(src);
+                const float s = __shfl_sync(kFullMask, sc, src);
+                uint32_t ok = 1u;
+                if (lane == 0) {
+                    uint32_t nn = 0;
+                    while (atomicCAS(&locks[j], 0u, 1u) != 0u) {
+                        if (++nn > kLockLimit) { ok = 0u; break; }
+                    }
+                }
+                ok = __shfl_sync(kFullMask, ok, 0);
+                if (!ok) {
+                    if (lane == 0) atomicOr(err, kErrTimeout);
+                    continue;
+                }
+                __threadfence_block();
+                const float t = smem_topk_insert(tk_s + j * K, tk_k + j * K, s, (uint64_t)p, K);
+                if (lane == 0) thr[j] = t;
+                __threadfence_block();
+                __syncwarp();
+                if (lane == 0) atomicExch(&locks[j], 0u);
+            }
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < cnt * K; i += blockDim.x) {
+            const size_t o = (size_t)item * G * K + i;
+            part_s[o] = tk_s[i];
+            part_k[o] = tk_k[i];
+        }
+        __syncthreads();
+    }
+    if (stats) {
+        if (lane == 0) {
+            atomicAdd(&s_stats[0], my_cand);
+            atomicAdd(&s_stats[1], my_entries);
+            atomicAdd(&s_stats[2], my_psm);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            atomicAdd(&stats[2], s_stats[0]);
+            atomicAdd(&stats[3], s_stats[1]);
+            atomicAdd(&stats[4], s_stats[2]);
+        }
+    }
+}
+
+}  // namespace hfx
+
+using namespace hfx;
+
+int hfx_scan_inclusive(const int32_t *in, int64_t n, int32_t *out, int32_t *partial, cudaStream_t st) {
+    if (n <= 0) return 0;
+    const int64_t nb = (n + kScanTile - 1) / kScanTile;
+    k_scan_reduce<<<(unsigned)nb, 512, 0, st>>>(in, n, partial);
+    k_scan_partials<<<1, 1024, 0, st>>>(partial, (int32_t)nb);
+    k_scan_apply<<<(unsigned)nb, 256, 0, st>>>(in, n, partial, out);
+    return (int)cudaGetLastError();
+}
+
+int64_t hfx_scan_partials_needed(int64_t n) { return (n + kScanTile - 1) / kScanTile + 1; }
+
+int hfx_lists_mark(const SpecMeta *meta, const uint32_t *wb, const uint32_t *we, int32_t nspec, int64_t npep1,
+                   int32_t *diff, cudaStream_t st) {
+    cudaMemsetAsync(diff, 0, sizeof(int32_t) * (size_t)kLevels * npep1, st);
+    if (nspec > 0) k_mark_levels<<<(nspec + 255) / 256, 256, 0, st>>>(meta, wb, we, nspec, npep1, diff);
+    return (int)cudaGetLastError();
+}
+
+int hfx_lists_generate(const DevDB &db, const int32_t *cover, int64_t npep1, int32_t nbins, const uint32_t *lstart,
+                       uint64_t total10, uint16_t *lists, uint16_t *list_len, int fastdiv, unsigned long long *stats,
+                       uint32_t *err, cudaStream_t st) {
+    const int nw = 8;
+    const int32_t words = (nbins + 31) / 32;
+    const size_t smem = (size_t)nw * 3 * words * 4 + (size_t)nw * kMaxListLen * 2;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    auto f = fastdiv ? k_gen_lists<true> : k_gen_lists<false>;
+    cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, nw * 32, smem);
+    f<<<sms * (per > 0 ? per : 1), nw * 32, smem, st>>>(db, cover, npep1, nbins, lstart, total10, lists, list_len,
+                                                        stats, err);
+    return (int)cudaGetLastError();
+}
+
+template <typename T, int G>
+static int launch_lists_t(const uint16_t *lists, const uint32_t *lstart, uint64_t total10, const uint16_t *list_len,
+                          uint32_t num_pep, const T *rows, int64_t stride, const SpecMeta *meta, const uint32_t *wb,
+                          const uint32_t *we, const BatchedWs &ws, void *tiles, uint32_t ngroups, int32_t chunk,
+                          int32_t K, int nw, float *part_s, uint64_t *part_k, unsigned long long *stats,
+                          uint32_t *err, cudaStream_t st) {
+    if (ngroups > 0) hfx_pack_tiles_launch<T, G>(rows, stride, meta, ws, (T *)tiles, ngroups, st);
+    int dev = 0, sms = 0, smem_max = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const size_t tile = ((size_t)stride * G * sizeof(T) + 15) & ~(size_t)15;
+    const size_t smem = 128 + tile + ((size_t)((G * K + 1) & ~1) * 4 + (size_t)G * K * 8 + (size_t)G * 8 + 15);
+    if (smem > (size_t)smem_max) return (int)cudaErrorInvalidValue;
+    auto fn = k_score_lists<T, G>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    if (nw <= 0) nw = 16;
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, nw * 32, smem);
+    const int grid = sms * (per > 0 ? per : 1);
+    cudaMemsetAsync(ws.counter, 0, 4, st);
+    fn<<<grid, nw * 32, smem, st>>>(lists, lstart, total10, list_len, num_pep, (const T *)tiles, stride, wb, we,
+                                    ws.perm, ws.groups, ws.item_off, ws.ngroups, chunk, K, ws.counter, part_s, part_k,
+                                    stats, err);
+    return (int)cudaGetLastError();
+}
+
+int hfx_lists_score(const uint16_t *lists, const uint32_t *lstart, uint64_t total10, const uint16_t *list_len,
+                    uint32_t num_pep, const void *rows, int elem_kind, int64_t stride, const SpecMeta *meta,
+                    const uint32_t *wb, const uint32_t *we, const BatchedWs &ws, void *tiles, uint32_t ngroups,
+                    int32_t G, int32_t chunk, int32_t K, int nw, float *part_s, uint64_t *part_k,
+                    unsigned long long *stats, uint32_t *err, cudaStream_t st) {
+#define HFX_L(T, GG)                                                                                              \
+    return launch_lists_t<T, GG>(lists, lstart, total10, list_len, num_pep, (const T *)rows, stride, meta, wb, we,\
+                                 ws, tiles, ngroups, chunk, K, nw, part_s, part_k, stats, err, st)
+    if (elem_kind == 0) {
+        if (G == 4) HFX_L(float, 4);
+        if (G == 8) HFX_L(float, 8);
+        if (G == 2) HFX_L(float, 2);
+        if (G == 1) HFX_L(float, 1);
+    } else if (elem_kind == 1) {
+        if (G == 8) HFX_L(__nv_bfloat16, 8);
+        if (G == 4) HFX_L(__nv_bfloat16, 4);
+        if (G == 2) HFX_L(__nv_bfloat16, 2);
+        if (G == 1) HFX_L(__nv_bfloat16, 1);
+    } else {
+        if (G == 8) HFX_L(__half, 8);
+        if (G == 4) HFX_L(__half, 4);
+        if (G == 2) HFX_L(__half, 2);
+        if (G == 1) HFX_L(__half, 1);
+    }
+#undef HFX_L
+    return (int)cudaErrorInvalidValue;
+}

@@ -1,0 +1,27 @@
+// Precomputed ion lists (lists.cu): declarations.
+#pragma once
+#include "hfx_internal.h"
+#include "batched.h"
+
+namespace hfx {
+constexpr int kLevels = 4;          // ion-charge levels 1..4 (Search.hs:182, ion_series.cu:301-309)
+constexpr int kMaxListLen = 4096;   // distinct bins kept per (peptide, level)
+}  // namespace hfx
+
+int hfx_scan_inclusive(const int32_t *in, int64_t n, int32_t *out, int32_t *partial, cudaStream_t st);
+int64_t hfx_scan_partials_needed(int64_t n);
+int hfx_lists_mark(const hfx::SpecMeta *meta, const uint32_t *wb, const uint32_t *we, int32_t nspec, int64_t npep1,
+                   int32_t *diff, cudaStream_t st);
+// lstart[p] = 10 * sum_{q<p} (tn_q - tc_q) in mass order; total10 = 10 * sum
+// over all peptides; the level-z list of p starts at
+// total10 * z(z-1)/2 + z * lstart[p].  stats (nullable, 8 counters): [0] lists
+// built, [1] list entries, [2] candidates scored, [3] entries streamed,
+// [4] peptide-spectrum pairs.
+int hfx_lists_generate(const hfx::DevDB &db, const int32_t *cover, int64_t npep1, int32_t nbins,
+                       const uint32_t *lstart, uint64_t total10, uint16_t *lists, uint16_t *list_len, int fastdiv,
+                       unsigned long long *stats, uint32_t *err, cudaStream_t st);
+int hfx_lists_score(const uint16_t *lists, const uint32_t *lstart, uint64_t total10, const uint16_t *list_len,
+                    uint32_t num_pep, const void *rows, int elem_kind, int64_t stride, const hfx::SpecMeta *meta,
+                    const uint32_t *wb, const uint32_t *we, const hfx::BatchedWs &ws, void *tiles, uint32_t ngroups,
+                    int32_t G, int32_t chunk, int32_t K, int nw, float *part_s, uint64_t *part_k,
+                    unsigned long long *stats, uint32_t *err, cudaStream_t st);

@@ -39,7 +39,8 @@ typedef struct hfx_search_params {
     int32_t top_n;                 /* matches kept per spectrum, 1..32                         */
     int32_t precision;             /* 0 FP32 rows; 1 BF16 rows + FP32 rescore; 2 FP16 + rescore */
     int32_t rescore_k;             /* candidates rescored in FP32 (>= top_n, <= 32)            */
-    int32_t batch_mode;            /* 0 one launch per spectrum; 1 persistent batched launch   */
+    int32_t batch_mode;            /* 0 one launch per spectrum; 1 batched over per-step ion
+                                      lists; 2 batched with ion lists rebuilt per work item    */
     int32_t fastdiv;               /* 1: __fdividef in ion m/z, as ion_series.cu:59-69         */
     int32_t search_plain;          /* score unmodified candidates                              */
     int32_t search_mods;           /* score variable-modification isoforms (needs hfx_set_mods) */
@@ -72,9 +73,14 @@ const char *hfx_last_error(const hfx_ctx *ctx);
 #define HFX_STAGE_TOPN 4        /* stage (e): top-N merge                   */
 #define HFX_STAGE_RESCORE 5     /* FP32 rescoring of the kept candidates    */
 #define HFX_STAGE_MODS 6        /* variable-modification isoforms           */
+#define HFX_STAGE_LISTS 7       /* per-peptide ion lists of the batch       */
 #define HFX_NSTAGES 8
 int32_t hfx_set_profiling(hfx_ctx *ctx, int32_t on);
 int32_t hfx_stage_stats(hfx_ctx *ctx, double *ms, int64_t *launches, int64_t *units, int32_t reset);
+/* Work counters of the batched list path, accumulated while profiling is on:
+ * [0] ion lists built, [1] list entries built, [2] candidates scored,
+ * [3] list entries streamed by the scorer, [4] peptide-spectrum pairs. */
+int32_t hfx_search_counters(hfx_ctx *ctx, uint64_t *out8, int32_t reset);
 
 /* Digest proteins into the search database and upload it.  Replaces
  * Fragment.hs:197-233 makeSeqDB + :239-258 withDeviceDB + sort.cu:28-35

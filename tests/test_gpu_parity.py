@@ -190,24 +190,26 @@ def test_search_edge_cases(tiny_engine, oracle):
     assert (res.score[2][res.key[2] != np.iinfo(np.uint64).max] == 0).all()
 
 
+@pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("G", [1, 2, 4, 8])
-def test_batched_fp32_bitexact(full_engine, oracle, G):
+def test_batched_fp32_bitexact(full_engine, oracle, G, mode):
     import hfx_gb300
     eng, prot, sp = full_engine
     ref = oracle.search(*_oracle_db(oracle, eng, prot), sp, topn=10)
-    res = eng.search(sp, hfx_gb300.default_params(top_n=10, batch_mode=1, group_size=G, chunk=512))
-    _compare(res, ref, f"batched G={G}")
+    res = eng.search(sp, hfx_gb300.default_params(top_n=10, batch_mode=mode, group_size=G, chunk=512))
+    _compare(res, ref, f"batched mode={mode} G={G}")
 
 
+@pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("precision", [1, 2])
-def test_batched_lowp_rescore_matches_fp32(full_engine, oracle, precision):
+def test_batched_lowp_rescore_matches_fp32(full_engine, oracle, precision, mode):
     """BF16 / FP16 rows pick the kept candidates, FP32 rescoring restores the
     exact FP32 scores: the top-10 equals the FP32 oracle's."""
     import hfx_gb300
     eng, prot, sp = full_engine
     ref = oracle.search(*_oracle_db(oracle, eng, prot), sp, topn=10)
-    res = eng.search(sp, hfx_gb300.default_params(top_n=10, batch_mode=1, precision=precision, rescore_k=32))
-    _compare(res, ref, f"precision {precision}")
+    res = eng.search(sp, hfx_gb300.default_params(top_n=10, batch_mode=mode, precision=precision, rescore_k=32))
+    _compare(res, ref, f"precision {precision} mode {mode}")
 
 
 def test_batched_tiny_and_edges(tiny_engine, oracle):
