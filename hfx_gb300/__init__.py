@@ -30,7 +30,7 @@ EXPORTED = [
     "hfx_default_params", "hfx_ctx_create", "hfx_ctx_destroy", "hfx_set_stream",
     "hfx_last_error", "hfx_build_db", "hfx_upload_db", "hfx_db_info", "hfx_db_export",
     "hfx_set_mods", "hfx_mod_table", "hfx_search_host", "hfx_search_device",
-    "hfx_preprocess", "hfx_find_windows", "hfx_ion_bins", "hfx_digest", "hfx_pack_ions",
+    "hfx_preprocess", "hfx_find_windows", "hfx_ion_bins", "hfx_mod_isoforms", "hfx_digest", "hfx_pack_ions",
     "hfx_set_profiling", "hfx_stage_stats", "hfx_search_counters",
 ]
 STAGES = ["layout", "preprocess", "windows", "score", "topn", "rescore", "mods", "lists"]
@@ -92,6 +92,7 @@ def load_library(path: str = LIB_PATH):
         "hfx_preprocess": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, i32, C.c_int64, P, P, P, P, P]),
         "hfx_find_windows": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, i32, P, P]),
         "hfx_ion_bins": (i32, [P, P, P, P, i32, i32, i32, P, P, P]),
+        "hfx_mod_isoforms": (i32, [P, P, P, P, i32, i32, P, P, P]),
         "hfx_digest": (C.c_int64, [P, P, i32, P, i32, i32, f32, f32, i32, i32, i32, P, P, P, C.c_int64]),
         "hfx_pack_ions": (i32, [P, u64, P, i32, P]),
         "hfx_set_profiling": (i32, [P, i32]),
@@ -297,3 +298,8 @@ class Engine:
     def ion_bins(self, pos, charges, lens, cap, bins, levels, count, fastdiv=False):
         self._check(self.lib.hfx_ion_bins(self.h, _ptr(pos), _ptr(charges), _ptr(lens), int(pos.numel()), cap,
                                           int(fastdiv), _ptr(bins), _ptr(levels), _ptr(count)))
+
+    def mod_isoforms(self, pos, mod, rank, cap, count, unrank, modded):
+        """Stage (e) alone (hfx_mod_isoforms); all arguments are device tensors."""
+        self._check(self.lib.hfx_mod_isoforms(self.h, _ptr(pos), _ptr(mod), _ptr(rank), int(pos.numel()), cap,
+                                              _ptr(count), _ptr(unrank), _ptr(modded)))

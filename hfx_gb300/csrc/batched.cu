@@ -21,11 +21,12 @@
 #include "device_common.cuh"
 #include "batched.h"
 #include "batched_common.cuh"
+#include "mods_device.cuh"
 
 namespace hfx {
 
 constexpr int kMassBuckets = 8192;   // 1 Da buckets of residual mass
-constexpr int kClasses = 10;         // (ion charges 0..4) x (narrow, wide)
+constexpr int kClasses = 12;         // (ion charge class 0..5) x (narrow, wide)
 constexpr float kWideEps = 1.0f;     // windows wider than this are "wide"
 
 // Shared memory of one scorer warp: bit planes + distinct-bin list.
@@ -39,7 +40,10 @@ __host__ __device__ __forceinline__ size_t batched_cta_bytes(int G, int K) {
 }
 
 __device__ __forceinline__ int spec_class(const SpecMeta &m) {
-    return m.charges_plain * 2 + (m.eps > kWideEps ? 1 : 0);
+    // charge class: plain charges 1..4 (modified ones equal them), 5 = no
+    // plain ions but modified ions (charge 6..11), 0 = none
+    const int cc = m.charges_plain > 0 ? m.charges_plain : (m.charges_mod > 0 ? 5 : 0);
+    return cc * 2 + (m.eps > kWideEps ? 1 : 0);
 }
 __device__ __forceinline__ int spec_bucket(const SpecMeta &m) {
     int mb = (int)fminf(fmaxf(m.mass, 0.0f), (float)(kMassBuckets - 1));
@@ -140,6 +144,7 @@ __global__ void k_groups(const uint32_t *__restrict__ bucket_off, const uint32_t
     gi.hi = 0u;
     gi.maxlen = 0;
     gi.charges = 0;
+    gi.charges_mod = 0;
     for (uint32_t j = 0; j < cnt; ++j) {
         const int32_t s = perm[pos0 + j];
         group_of[s] = g;
@@ -151,6 +156,7 @@ __global__ void k_groups(const uint32_t *__restrict__ bucket_off, const uint32_t
         }
         gi.maxlen = max(gi.maxlen, meta[s].len);
         gi.charges = meta[s].charges_plain;
+        gi.charges_mod = meta[s].charges_mod;
     }
     if (gi.hi <= gi.lo) {
         gi.lo = gi.hi = 0;
@@ -327,8 +333,9 @@ __global__ void k_merge_items(const float *__restrict__ part_s, const uint64_t *
 // per spectrum, each warp recomputes kept entries from the FP32 row, then
 // the CTA orders them and writes the top-N.
 template <bool FastDiv>
-__global__ void __launch_bounds__(256) k_rescore(DevDB db, const float *__restrict__ rows32, int64_t stride,
-                                                 const SpecMeta *__restrict__ meta, const float *__restrict__ kept_s,
+__global__ void __launch_bounds__(256) k_rescore(DevDB db, DevMods mods, const float *__restrict__ rows32,
+                                                 int64_t stride, const SpecMeta *__restrict__ meta,
+                                                 const float *__restrict__ kept_s,
                                                  const uint64_t *__restrict__ kept_k, int32_t K, int32_t topn,
                                                  float *__restrict__ out_s, uint64_t *__restrict__ out_k,
                                                  uint32_t *__restrict__ out_pep) {
@@ -354,10 +361,33 @@ __global__ void __launch_bounds__(256) k_rescore(DevDB db, const float *__restri
     for (int t = warp; t < K; t += nw) {
         const uint64_t kk = kept_k[(size_t)s * K + t];
         float sc = -INFINITY;
-        if (kk != ~0ull) {
+        if (kk != ~0ull && !(kk >> 63)) {
             const uint32_t p = (uint32_t)kk;
             const WordRange wr = build_planes<FastDiv>(pl, db.ions, db.tc_sorted[p], db.tn_sorted[p],
                                                        db.r_sorted[p], m.charges_plain, m.len, mt_lane, NoMods{});
+            float acc[1];
+            planes_dot<float, 1>(pl, list, wr, ss, acc);
+            sc = acc[0];
+        } else if (kk != ~0ull) {
+            // modified match: combination, mass-order position and isoform rank from the key
+            const int32_t mu = (int32_t)((kk >> 54) & 511u);
+            const uint32_t p = (uint32_t)((kk >> 27) & ((1u << 27) - 1u));
+            const uint32_t rank = (uint32_t)(kk & ((1u << 27) - 1u));
+            const uint32_t tc = db.tc_sorted[p], tn = db.tn_sorted[p];
+            const int32_t *dcount = mods.counts + (size_t)mu * mods.num_ma;
+            uint32_t D[kMaxMa], scan[kMaxMa];
+            modable_counts(db.ions, tc, tn, mods.num_ma, D);
+            isoform_count(D, dcount, mods.num_ma, scan);
+            ModIsoform iso;
+            iso.num_ma = mods.num_ma;
+            iso.per_type = mods.per_type;
+#pragma unroll
+            for (int i = 0; i < kMaxMa; ++i) iso.ma_mass[i] = mods.ma_mass[i];
+            isoform_masks(D, scan, dcount, mods.num_ma, rank, iso.mask);
+            iso.reset();
+            const float residual = __fadd_rn(db.r_sorted[p], mods.delta[mu]);
+            const WordRange wr = build_planes<FastDiv>(pl, db.ions, tc, tn, residual, m.charges_mod, m.len, mt_lane,
+                                                       iso);
             float acc[1];
             planes_dot<float, 1>(pl, list, wr, ss, acc);
             sc = acc[0];
@@ -376,7 +406,8 @@ __global__ void __launch_bounds__(256) k_rescore(DevDB db, const float *__restri
         if (lane < topn) {
             out_s[(size_t)s * topn + lane] = tk.s;
             out_k[(size_t)s * topn + lane] = tk.k;
-            out_pep[(size_t)s * topn + lane] = (tk.k != ~0ull) ? db.idx_sorted[(uint32_t)tk.k] : ~0u;
+            const uint64_t pos = (tk.k >> 63) ? ((tk.k >> 27) & ((1ull << 27) - 1)) : tk.k;
+            out_pep[(size_t)s * topn + lane] = (tk.k != ~0ull) ? db.idx_sorted[pos] : ~0u;
         }
     }
 }
@@ -384,7 +415,8 @@ __global__ void __launch_bounds__(256) k_rescore(DevDB db, const float *__restri
 __global__ void k_finish(const float *__restrict__ in_s, const uint64_t *__restrict__ in_k, int32_t nspec,
                          int32_t topn, const uint32_t *__restrict__ idx_sorted, const uint32_t *__restrict__ wb,
                          const uint32_t *__restrict__ we, const SpecMeta *__restrict__ meta, float *__restrict__ out_s,
-                         uint64_t *__restrict__ out_k, uint32_t *__restrict__ out_pep, int64_t *__restrict__ ncand) {
+                         uint64_t *__restrict__ out_k, uint32_t *__restrict__ out_pep, int32_t plain,
+                         const unsigned long long *__restrict__ ncand_mod, int64_t *__restrict__ ncand) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < (int64_t)nspec * topn) {
         const uint64_t k = in_k[i];
@@ -397,13 +429,18 @@ __global__ void k_finish(const float *__restrict__ in_s, const uint64_t *__restr
         }
         out_pep[i] = pep;
     }
-    if (ncand && i < nspec) ncand[i] = (meta[i].status == 0) ? (int64_t)(we[i] - wb[i]) : 0;
+    if (ncand && i < nspec)
+        ncand[i] = ((meta[i].status == 0 && plain) ? (int64_t)(we[i] - wb[i]) : 0) +
+                   (ncand_mod ? (int64_t)ncand_mod[i] : 0);
 }
 
 __global__ void k_ncand(const uint32_t *__restrict__ wb, const uint32_t *__restrict__ we,
-                        const SpecMeta *__restrict__ meta, int32_t nspec, int64_t *__restrict__ ncand) {
+                        const SpecMeta *__restrict__ meta, int32_t nspec, int32_t plain,
+                        const unsigned long long *__restrict__ ncand_mod, int64_t *__restrict__ ncand) {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < nspec) ncand[i] = (meta[i].status == 0) ? (int64_t)(we[i] - wb[i]) : 0;
+    if (i < nspec)
+        ncand[i] = ((meta[i].status == 0 && plain) ? (int64_t)(we[i] - wb[i]) : 0) +
+                   (ncand_mod ? (int64_t)ncand_mod[i] : 0);
 }
 
 }  // namespace hfx
@@ -512,7 +549,8 @@ int hfx_batched_merge(const float *part_s, const uint64_t *part_k, const Batched
     return (int)cudaGetLastError();
 }
 
-int hfx_rescore(const DevDB &db, const float *rows32, int64_t stride, const SpecMeta *meta, const float *kept_s,
+int hfx_rescore(const DevDB &db, const DevMods &mods, const float *rows32, int64_t stride, const SpecMeta *meta,
+                const float *kept_s,
                 const uint64_t *kept_k, int32_t nspec, int32_t K, int32_t topn, int fastdiv, float *out_s,
                 uint64_t *out_k, uint32_t *out_pep, cudaStream_t st) {
     const int nw = 8;
@@ -520,21 +558,42 @@ int hfx_rescore(const DevDB &db, const float *rows32, int64_t stride, const Spec
     const size_t smem = (size_t)nw * 3 * words * 4 + (size_t)nw * kListCap * 2 + 64 * 4 + 64 * 8;
     auto f = fastdiv ? k_rescore<true> : k_rescore<false>;
     cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    f<<<nspec, nw * 32, smem, st>>>(db, rows32, stride, meta, kept_s, kept_k, K, topn, out_s, out_k, out_pep);
+    f<<<nspec, nw * 32, smem, st>>>(db, mods, rows32, stride, meta, kept_s, kept_k, K, topn, out_s, out_k, out_pep);
     return (int)cudaGetLastError();
 }
 
 int hfx_finish(const float *in_s, const uint64_t *in_k, int32_t nspec, int32_t topn, const uint32_t *idx_sorted,
                const uint32_t *wb, const uint32_t *we, const SpecMeta *meta, float *out_s, uint64_t *out_k,
-               uint32_t *out_pep, int64_t *ncand, cudaStream_t st) {
+               uint32_t *out_pep, int32_t plain, const unsigned long long *ncand_mod, int64_t *ncand,
+               cudaStream_t st) {
     const int64_t n = std::max<int64_t>((int64_t)nspec * topn, nspec);
     k_finish<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in_s, in_k, nspec, topn, idx_sorted, wb, we, meta, out_s,
-                                                          out_k, out_pep, ncand);
+                                                          out_k, out_pep, plain, ncand_mod, ncand);
     return (int)cudaGetLastError();
 }
 
-int hfx_ncand(const uint32_t *wb, const uint32_t *we, const SpecMeta *meta, int32_t nspec, int64_t *ncand,
-              cudaStream_t st) {
-    k_ncand<<<(nspec + 255) / 256, 256, 0, st>>>(wb, we, meta, nspec, ncand);
+int hfx_ncand(const uint32_t *wb, const uint32_t *we, const SpecMeta *meta, int32_t nspec, int32_t plain,
+              const unsigned long long *ncand_mod, int64_t *ncand, cudaStream_t st) {
+    k_ncand<<<(nspec + 255) / 256, 256, 0, st>>>(wb, we, meta, nspec, plain, ncand_mod, ncand);
     return (int)cudaGetLastError();
+}
+
+template <typename T>
+static int pack_tiles_g(int32_t G, const void *rows, int64_t stride, const SpecMeta *meta, const BatchedWs &ws,
+                        void *tiles, uint32_t ngroups, cudaStream_t st) {
+    if (ngroups == 0) return 0;
+    const T *r = (const T *)rows;
+    if (G == 8) hfx_pack_tiles_launch<T, 8>(r, stride, meta, ws, (T *)tiles, ngroups, st);
+    else if (G == 4) hfx_pack_tiles_launch<T, 4>(r, stride, meta, ws, (T *)tiles, ngroups, st);
+    else if (G == 2) hfx_pack_tiles_launch<T, 2>(r, stride, meta, ws, (T *)tiles, ngroups, st);
+    else if (G == 1) hfx_pack_tiles_launch<T, 1>(r, stride, meta, ws, (T *)tiles, ngroups, st);
+    else return (int)cudaErrorInvalidValue;
+    return (int)cudaGetLastError();
+}
+
+int hfx_pack_tiles(const void *rows, int elem_kind, int64_t stride, const SpecMeta *meta, const BatchedWs &ws,
+                   void *tiles, uint32_t ngroups, int32_t G, cudaStream_t st) {
+    if (elem_kind == 0) return pack_tiles_g<float>(G, rows, stride, meta, ws, tiles, ngroups, st);
+    if (elem_kind == 1) return pack_tiles_g<__nv_bfloat16>(G, rows, stride, meta, ws, tiles, ngroups, st);
+    return pack_tiles_g<__half>(G, rows, stride, meta, ws, tiles, ngroups, st);
 }

@@ -7,7 +7,8 @@ struct GroupInfo {
     uint32_t pos0, count;  // members: perm[pos0 .. pos0+count)
     uint32_t lo, hi;       // union of the members' candidate windows
     int32_t maxlen;        // longest member row
-    int32_t charges;       // ion charges shared by the members
+    int32_t charges;       // ion charges shared by the members (unmodified)
+    int32_t charges_mod;   // ion charges of the members' modified candidates
 };
 
 struct BatchedWs {
@@ -24,7 +25,7 @@ struct BatchedWs {
     uint32_t *counter;      // [1] work-stealing cursor
 };
 
-constexpr int kBucketCount = 10 * 8192;
+constexpr int kBucketCount = 12 * 8192;
 }  // namespace hfx
 
 size_t hfx_batched_smem(int64_t stride, int elem_bytes, int G, int nw, int K);
@@ -40,11 +41,20 @@ int hfx_batched_score(const hfx::DevDB &db, const void *rows, int elem_kind, int
 int hfx_batched_merge(const float *part_s, const uint64_t *part_k, const hfx::BatchedWs &ws,
                       const hfx::SpecMeta *meta, int32_t nspec, int32_t G, int32_t K, int32_t kout, float *out_s,
                       uint64_t *out_k, cudaStream_t st);
-int hfx_rescore(const hfx::DevDB &db, const float *rows32, int64_t stride, const hfx::SpecMeta *meta,
-                const float *kept_s, const uint64_t *kept_k, int32_t nspec, int32_t K, int32_t topn, int fastdiv,
-                float *out_s, uint64_t *out_k, uint32_t *out_pep, cudaStream_t st);
+// FP32 rescoring of the kept low-precision matches (unmodified and modified
+// keys) and the final top-N.
+int hfx_rescore(const hfx::DevDB &db, const hfx::DevMods &mods, const float *rows32, int64_t stride,
+                const hfx::SpecMeta *meta, const float *kept_s, const uint64_t *kept_k, int32_t nspec, int32_t K,
+                int32_t topn, int fastdiv, float *out_s, uint64_t *out_k, uint32_t *out_pep, cudaStream_t st);
+// Peptide ids of the top-N and candidate counts: the unmodified window
+// (when plain) plus the modified isoforms counted by the scorer (ncand_mod,
+// may be null).
 int hfx_finish(const float *in_s, const uint64_t *in_k, int32_t nspec, int32_t topn, const uint32_t *idx_sorted,
                const uint32_t *wb, const uint32_t *we, const hfx::SpecMeta *meta, float *out_s, uint64_t *out_k,
-               uint32_t *out_pep, int64_t *ncand, cudaStream_t st);
-int hfx_ncand(const uint32_t *wb, const uint32_t *we, const hfx::SpecMeta *meta, int32_t nspec, int64_t *ncand,
-              cudaStream_t st);
+               uint32_t *out_pep, int32_t plain, const unsigned long long *ncand_mod, int64_t *ncand,
+               cudaStream_t st);
+int hfx_ncand(const uint32_t *wb, const uint32_t *we, const hfx::SpecMeta *meta, int32_t nspec, int32_t plain,
+              const unsigned long long *ncand_mod, int64_t *ncand, cudaStream_t st);
+// Interleaved group tiles only (the scorers pack their own otherwise).
+int hfx_pack_tiles(const void *rows, int elem_kind, int64_t stride, const hfx::SpecMeta *meta,
+                   const hfx::BatchedWs &ws, void *tiles, uint32_t ngroups, int32_t G, cudaStream_t st);

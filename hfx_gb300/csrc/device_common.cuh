@@ -143,10 +143,11 @@ __device__ __forceinline__ float residue_mass(float mt_lane, uint32_t byte) {
     return i < 26u ? m : 0.0f;
 }
 
-// Per-residue modification hook: returns the mass to add (0 = unmodified).
+// Per-residue modification hook, called by every lane once per 32-residue
+// chunk in peptide order: returns the mass to add to this lane's residue
+// (0 = unmodified).  `valid` is false for lanes past the peptide's end.
 struct NoMods {
-    __device__ __forceinline__ bool modded(uint32_t /*pos*/) const { return false; }
-    __device__ __forceinline__ float add(uint32_t /*byte*/) const { return 0.0f; }
+    __device__ __forceinline__ float chunk_add(uint32_t /*byte*/, bool /*valid*/) { return 0.0f; }
 };
 
 // Words [lo, hi) of the bit planes that hold set bits.
@@ -158,7 +159,7 @@ template <bool FastDiv, typename Mods>
 __device__ __forceinline__ WordRange build_planes_range(const Planes &pl, const uint8_t *__restrict__ ions,
                                                         uint32_t tc, uint32_t tn, float residual, int c_first,
                                                         int c_last, int32_t nbins, float mt_lane,
-                                                        const Mods &mods);
+                                                        Mods mods);
 
 // Build the ion bit planes of one candidate.  Residues [tc, tn) of `ions`,
 // `charges` ion charges (0 = none), bins >= nbins dropped.  Returns the
@@ -167,7 +168,7 @@ template <bool FastDiv, typename Mods>
 __device__ __forceinline__ WordRange build_planes(const Planes &pl, const uint8_t *__restrict__ ions,
                                                   uint32_t tc, uint32_t tn, float residual,
                                                   int charges, int32_t nbins, float mt_lane,
-                                                  const Mods &mods) {
+                                                  Mods mods) {
     return build_planes_range<FastDiv>(pl, ions, tc, tn, residual, 1, charges, nbins, mt_lane, mods);
 }
 
@@ -177,7 +178,7 @@ template <bool FastDiv, typename Mods>
 __device__ __forceinline__ WordRange build_planes_range(const Planes &pl, const uint8_t *__restrict__ ions,
                                                         uint32_t tc, uint32_t tn, float residual, int c_first,
                                                         int c_last, int32_t nbins, float mt_lane,
-                                                        const Mods &mods) {
+                                                        Mods mods) {
     const int lane = threadIdx.x & 31;
     BinRange br;
     const int charges = c_last - c_first + 1;
@@ -188,7 +189,10 @@ __device__ __forceinline__ WordRange build_planes_range(const Planes &pl, const 
         uint32_t byte = 0;
         if (lane < cnt) byte = __ldg(ions + base + lane);
         float v = residue_mass(mt_lane, byte);
-        if (lane < cnt && mods.modded(base + lane - tc)) v = __fadd_rn(v, mods.add(byte));
+        {
+            const float add = mods.chunk_add(byte, lane < cnt);
+            if (add != 0.0f) v = __fadd_rn(v, add);
+        }
         if (lane >= cnt) v = 0.0f;
         if (lane == 0) v = __fadd_rn(v, carry);
 #pragma unroll

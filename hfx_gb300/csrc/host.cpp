@@ -10,6 +10,7 @@
 #include "search_kernels.h"
 #include "batched.h"
 #include "lists.h"
+#include "mods.h"
 #include "../../include/hfx_gpu.h"
 
 #include <algorithm>
@@ -141,6 +142,16 @@ struct hfx_ctx {
         db.num_pep = (uint32_t)num_pep;
         for (int i = 0; i < 32; ++i) db.mt[i] = i < 26 ? mt[i] : 0.0f;
         return db;
+    }
+    DevMods devmods() const {
+        DevMods m;
+        m.num_ma = num_ma;
+        m.num_mod = num_mod;
+        for (int i = 0; i < 8; ++i) m.ma_mass[i] = i < num_ma ? ma_mass[i] : 0.0f;
+        m.counts = num_mod > 0 ? d_mod_counts.as<int32_t>() : nullptr;
+        m.delta = num_mod > 0 ? d_mod_delta.as<float>() : nullptr;
+        m.per_type = per_type;
+        return m;
     }
 };
 
@@ -427,7 +438,12 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     if (e) return cuda_fail(ctx, e, "alloc parts");
     const DevDB db = ctx->devdb();
     const void *src_rows = elem_kind == 0 ? (const void *)rows : rows_lo;
-    if (p->batch_mode == 2) {
+    const bool plain_on = p->search_plain != 0;
+    const bool mods_on = p->search_mods != 0 && ctx->num_mod > 0;
+    if (!plain_on) {
+        rc = hfx_pack_tiles(src_rows, elem_kind, stride, meta, ws, tiles, ngroups, G, ctx->stream);
+        if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_pack_tiles");
+    } else if (p->batch_mode != 1) {
         // fused: every work item rebuilds its candidates' ion lists
         ctx->stage_begin(HFX_STAGE_SCORE);
         rc = hfx_batched_score(db, src_rows, elem_kind, stride, meta, wb, we, ws, tiles, ngroups, G, chunk, K, 0, 0,
@@ -476,26 +492,76 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
             for (int i = 0; i < 8; ++i) ctx->counters[i] += h[i];
         }
     }
+    // modified isoforms: fused enumeration + scoring over the same group tiles
+    const DevMods dm = ctx->devmods();
+    float *ms = nullptr;
+    uint64_t *mk = nullptr;
+    uint32_t *mitem_off = nullptr;
+    unsigned long long *ncm = nullptr;
+    if (mods_on) {
+        const int32_t nm = ctx->num_mod;
+        const int32_t n_gm = (int32_t)ngroups * nm;
+        uint32_t *mb = ctx->buf<uint32_t>("m_wb", (size_t)ns * nm, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        uint32_t *me = ctx->buf<uint32_t>("m_we", (size_t)ns * nm, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        uint32_t *mlo = ctx->buf<uint32_t>("m_lo", (size_t)n_gm + 1, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        uint32_t *mhi = ctx->buf<uint32_t>("m_hi", (size_t)n_gm + 1, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        int32_t *nch = ctx->buf<int32_t>("m_nchunks", (size_t)n_gm + 1, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        mitem_off = ctx->buf<uint32_t>("m_itemoff", (size_t)n_gm + 2, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        int32_t *partial = ctx->buf<int32_t>("m_partial", hfx_scan_partials_needed(n_gm + 1) + 1, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        ncm = ctx->buf<unsigned long long>("m_ncand", (size_t)ns, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        HFX_CUDA(cudaMemsetAsync(ncm, 0, 8ull * ns, ctx->stream), "memset");
+        ctx->stage_begin(HFX_STAGE_MODS);
+        rc = hfx_mods_windows(ctx->d_r.as<float>(), (uint32_t)ctx->num_pep, meta, ns, dm, mb, me, ctx->stream);
+        if (!rc) rc = hfx_mods_plan(ws, ngroups, mb, me, nm, chunk, mlo, mhi, nch, mitem_off, partial, ctx->stream);
+        if (rc) return cuda_fail(ctx, (cudaError_t)rc, "modification plan");
+        uint32_t mtotal = 0;
+        if (n_gm > 0) {
+            HFX_CUDA(cudaMemcpyAsync(&mtotal, mitem_off + n_gm, 4, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+            HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+        }
+        ms = ctx->buf<float>("m_part_s", (size_t)mtotal * G * K + 1, e);
+        if (e) return cuda_fail(ctx, e, "alloc mod parts");
+        mk = ctx->buf<uint64_t>("m_part_k", (size_t)mtotal * G * K + 1, e);
+        if (e) return cuda_fail(ctx, e, "alloc mod parts");
+        if (mtotal > 0) {
+            rc = hfx_mods_score(db, dm, tiles, elem_kind, stride, mb, me, ws, mlo, mhi, mitem_off, n_gm, G, chunk, K,
+                                p->fastdiv, ms, mk, ncm, ctx->d_err.as<uint32_t>(), ctx->stream);
+            if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_mods");
+        }
+        ctx->stage_end(HFX_STAGE_MODS, 4, mtotal);
+    }
     float *ks = ctx->buf<float>("kept_s", (size_t)ns * K, e);
     if (e) return cuda_fail(ctx, e, "alloc");
     uint64_t *kk = ctx->buf<uint64_t>("kept_k", (size_t)ns * K, e);
     if (e) return cuda_fail(ctx, e, "alloc");
     ctx->stage_begin(HFX_STAGE_TOPN);
-    rc = hfx_batched_merge(ps, pk, ws, meta, ns, G, K, K, ks, kk, ctx->stream);
+    if (mods_on)
+        rc = hfx_merge_with_mods(ps, pk, ws.item_off, ms, mk, mitem_off, ctx->num_mod, ws, meta, ns, G, K, plain_on,
+                                 ks, kk, ctx->stream);
+    else
+        rc = hfx_batched_merge(ps, pk, ws, meta, ns, G, K, K, ks, kk, ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_merge_items");
     ctx->stage_end(HFX_STAGE_TOPN, 1, ns);
     if (elem_kind == 0) {
         rc = hfx_finish(ks, kk, ns, p->top_n, ctx->d_idx.as<uint32_t>(), wb, we, meta, out_s, out_k, out_pep,
-                        out_ncand, ctx->stream);
+                        plain_on, ncm, out_ncand, ctx->stream);
         if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_finish");
     } else {
         ctx->stage_begin(HFX_STAGE_RESCORE);
-        rc = hfx_rescore(db, rows, stride, meta, ks, kk, ns, K, p->top_n, p->fastdiv, out_s, out_k, out_pep,
+        rc = hfx_rescore(db, dm, rows, stride, meta, ks, kk, ns, K, p->top_n, p->fastdiv, out_s, out_k, out_pep,
                          ctx->stream);
         if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_rescore");
         ctx->stage_end(HFX_STAGE_RESCORE, 1, (int64_t)ns * K);
         if (out_ncand) {
-            rc = hfx_ncand(wb, we, meta, ns, out_ncand, ctx->stream);
+            rc = hfx_ncand(wb, we, meta, ns, plain_on, ncm, out_ncand, ctx->stream);
             if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_ncand");
         }
     }
@@ -517,8 +583,9 @@ int32_t search_device(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, 
     __half *rows_h = nullptr;
     rc = run_stage_a(ctx, p, b, stride, meta, rows, rows_bf, rows_h, p->precision == 1, p->precision == 2);
     if (rc) return rc;
-    if (p->search_mods && ctx->num_mod > 0) return fail(ctx, HFX_ERR_UNSUPPORTED, "modification search not built yet");
-    if (p->batch_mode)
+    // the modified isoforms are scored by the batched engine only: with
+    // modifications on, batch_mode 0 runs the fused batched path
+    if (p->batch_mode || (p->search_mods && ctx->num_mod > 0) || !p->search_plain)
         rc = search_batched(ctx, p, b, meta, rows, p->precision == 1 ? (const void *)rows_bf : (const void *)rows_h,
                             p->precision, stride, out_s, out_k, out_pep, out_ncand);
     else if (p->precision != 0)
@@ -902,6 +969,28 @@ int32_t hfx_ion_bins(hfx_ctx *ctx, const uint32_t *pos, const int32_t *charges, 
     int rc = hfx_launch_ion_bins(ctx->devdb(), pos, charges, lens, n, kMaxWords * 32, cap, fastdiv, bins, levels,
                                  count, ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_ion_bins");
+    HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    return HFX_OK;
+}
+
+int32_t hfx_mod_isoforms(hfx_ctx *ctx, const uint32_t *pos, const int32_t *mod, const uint32_t *rank, int32_t n,
+                         int32_t cap, uint32_t *count, uint32_t *unrank, uint8_t *modded) {
+    if (!ctx || n < 0 || cap < 0 || !pos || !mod || !rank || !count || !unrank || !modded)
+        return fail(ctx, HFX_ERR_ARG, "bad hfx_mod_isoforms arguments");
+    if (ctx->num_mod <= 0) return fail(ctx, HFX_ERR_ARG, "no modification table (hfx_set_mods)");
+    if (n == 0) return HFX_OK;
+    // queries are checked on the host: positions and combinations index device tables
+    std::vector<uint32_t> hp(n);
+    std::vector<int32_t> hm(n);
+    HFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    HFX_CUDA(cudaMemcpy(hp.data(), pos, 4ull * n, cudaMemcpyDeviceToHost), "D2H pos");
+    HFX_CUDA(cudaMemcpy(hm.data(), mod, 4ull * n, cudaMemcpyDeviceToHost), "D2H mod");
+    for (int32_t i = 0; i < n; ++i)
+        if (hp[i] >= ctx->num_pep || hm[i] < 0 || hm[i] >= ctx->num_mod)
+            return fail(ctx, HFX_ERR_ARG, "query out of range");
+    int rc = hfx_mods_isoforms(ctx->devdb(), ctx->devmods(), pos, mod, rank, n, cap, count, unrank, modded,
+                               ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_mod_isoforms");
     HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
     return HFX_OK;
 }

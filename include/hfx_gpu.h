@@ -160,6 +160,15 @@ int32_t hfx_find_windows(hfx_ctx *ctx, const hfx_search_params *p, const float *
 int32_t hfx_ion_bins(hfx_ctx *ctx, const uint32_t *pos, const int32_t *charges, const int32_t *lens,
                      int32_t n, int32_t cap, int32_t fastdiv, uint32_t *bins, uint8_t *levels,
                      int32_t *count);
+/* Stage (e) alone, device buffers: for queries (mass-order position pos[i],
+ * combination mod[i] of hfx_mod_table, isoform rank[i]) the isoform count
+ * of the candidate (0 when not modable; filter_by_mod.cu:216-261,
+ * calc_mod_cands.cu:49-66), and when rank[i] < count the unranked
+ * occurrence indices (unrank[i*8 ..], acids ascending, each acid's indices in
+ * the order of combinatorics.h:90-134; gen_mod_pep.cu:127-227) and the
+ * per-residue modified flags (modded[i*cap + residue], mion_series.cu:244-286). */
+int32_t hfx_mod_isoforms(hfx_ctx *ctx, const uint32_t *pos, const int32_t *mod, const uint32_t *rank,
+                         int32_t n, int32_t cap, uint32_t *count, uint32_t *unrank, uint8_t *modded);
 
 /* Allocation-free scoring of ONE spectrum.  It has no counterpart in the
  * reference.  It is for callers that cannot call cudaMalloc: code running

@@ -1,0 +1,180 @@
+"""GPU parity of stage (e), variable-modification search: the combination
+table, the isoform enumeration (counts, unranked positions, modified
+residues) and the full search with modified candidates, against the oracle
+on the same seeded inputs.  Everything is bit-exact: candidate counts, keys
+(combination, mass-order position, isoform rank), FP32 scores, peptides."""
+import numpy as np
+import pytest
+
+from hfx_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+MA = b"MSTY"
+MA_MASS = [15.995, 79.966, 79.966, 79.966]   # Met oxidation, Ser/Thr/Tyr phosphorylation
+
+
+def _engine(prot, max_ma=4, per_type=False):
+    import hfx_gb300
+    eng = hfx_gb300.Engine(0)
+    eng.build_db(prot.seq, prot.seg, static_add=synth.static_mods(), **synth.DIGEST)
+    eng.set_mods(MA.decode(), MA_MASS, max_ma, per_type)
+    return eng
+
+
+def _oracle_db(oracle, eng, prot):
+    r, tc, tn, idx, mt = eng.db_export()
+    return oracle.pack_ions(prot.seq, MA), mt, r, tc, tn, idx
+
+
+def _compare(res, ref, label):
+    sc, _, key, pep, nc = ref
+    assert np.array_equal(res.ncand, nc), label
+    assert np.array_equal(res.key, key), label
+    assert np.array_equal(res.score.view(np.uint32), sc.view(np.uint32)), label
+    assert np.array_equal(res.pep, pep), label
+
+
+@pytest.fixture(scope="module")
+def mods_full(gpulib):
+    prot = synth.proteins(20000, seed=1)
+    sp = synth.spectra(prot, 96, seed=101, charge_p={1: 0.05, 2: 0.5, 3: 0.35, 4: 0.10}, npeaks=(50, 400))
+    eng = _engine(prot)
+    yield eng, prot, sp
+    eng.close()
+
+
+@pytest.fixture(scope="module")
+def mods_tiny(gpulib, tiny):
+    prot, sp, cfg = tiny
+    eng = _engine(prot)
+    yield eng, prot, sp
+    eng.close()
+
+
+def test_mod_table_matches_oracle(mods_tiny, oracle):
+    eng, prot, sp = mods_tiny
+    n, counts, deltas = eng.mod_table()
+    oc, _, od = oracle.mod_combos(MA_MASS, 4)
+    assert n == len(oc) == 34
+    assert np.array_equal(counts[: n * 4].reshape(n, 4), oc)
+    assert np.array_equal(deltas[:n].view(np.uint32), od.view(np.uint32))
+
+
+@pytest.mark.parametrize("per_type", [False, True])
+def test_mod_isoforms_exact(gpulib, tiny, oracle, per_type):
+    """Per (peptide, combination, rank): the isoform count, the unranked
+    occurrence indices and the modified residues equal the oracle's."""
+    prot, sp, cfg = tiny
+    eng = _engine(prot, per_type=per_type)
+    try:
+        ions, mt, r, tc, tn, idx = _oracle_db(oracle, eng, prot)
+        n, counts, _ = eng.mod_table()
+        counts = counts[: n * 4].reshape(n, 4)
+        rng = np.random.default_rng(7)
+        pos_l, mu_l, rank_l, ref = [], [], [], []
+        # candidates rich in S/T/Y and M, every combination, first/last/random ranks
+        cand = rng.choice(len(r), 400, replace=False)
+        for q in cand:
+            pi = idx[q]
+            for mu in rng.choice(n, 6, replace=False):
+                niso, _, _ = oracle.mod_isoform(ions, int(tc[pi]), int(tn[pi]), MA, counts[mu], per_type=per_type)
+                ranks = {0, max(0, niso - 1), int(rng.integers(0, max(1, niso)))} if niso else {0}
+                for rk in sorted(ranks):
+                    pos_l.append(q)
+                    mu_l.append(mu)
+                    rank_l.append(rk)
+                    ref.append((niso,) + oracle.mod_isoform(ions, int(tc[pi]), int(tn[pi]), MA, counts[mu], rank=rk,
+                                                            per_type=per_type)[1:] if niso else (0, None, None))
+        d = torch.device("cuda:0")
+        cap = 64
+        m = len(pos_l)
+        pos = torch.tensor(np.array(pos_l, np.uint32).view(np.int32), device=d)
+        mu_t = torch.tensor(np.array(mu_l, np.int32), device=d)
+        rank = torch.tensor(np.array(rank_l, np.uint32).view(np.int32), device=d)
+        cnt = torch.zeros(m, dtype=torch.int32, device=d)
+        unr = torch.full((m, 8), -1, dtype=torch.int32, device=d)
+        modded = torch.zeros((m, cap), dtype=torch.uint8, device=d)
+        eng.mod_isoforms(pos, mu_t, rank, cap, cnt, unr, modded)
+        cnt = cnt.cpu().numpy().view(np.uint32)
+        unr = unr.cpu().numpy().view(np.uint32)
+        modded = modded.cpu().numpy()
+        nonzero = 0
+        for i, (niso, un, md) in enumerate(ref):
+            assert cnt[i] == niso, i
+            if niso == 0:
+                continue
+            nonzero += 1
+            k = int(counts[mu_l[i]].sum())
+            assert np.array_equal(unr[i, :k], un), (i, unr[i], un)
+            L = len(md)
+            assert np.array_equal(modded[i, :L], md), i
+        assert nonzero > 100
+    finally:
+        eng.close()
+
+
+def test_search_mods_tiny(mods_tiny, oracle):
+    import hfx_gb300
+    eng, prot, sp = mods_tiny
+    ref = oracle.search(*_oracle_db(oracle, eng, prot), sp, topn=10, ma=MA, ma_mass=MA_MASS, max_ma=4)
+    assert (ref[2] >> np.uint64(63)).any()           # modified matches reach the top-10
+    for mode in (0, 1, 2):
+        res = eng.search(sp, hfx_gb300.default_params(top_n=10, batch_mode=mode))
+        _compare(res, ref, f"tiny mods mode={mode}")
+
+
+@pytest.mark.parametrize("G", [1, 4, 8])
+@pytest.mark.parametrize("mode", [1, 2])
+def test_search_mods_full(mods_full, oracle, G, mode):
+    import hfx_gb300
+    eng, prot, sp = mods_full
+    ref = oracle.search(*_oracle_db(oracle, eng, prot), sp, topn=10, ma=MA, ma_mass=MA_MASS, max_ma=4)
+    res = eng.search(sp, hfx_gb300.default_params(top_n=10, batch_mode=mode, group_size=G, chunk=512))
+    _compare(res, ref, f"full mods G={G} mode={mode}")
+
+
+@pytest.mark.parametrize("precision", [1, 2])
+def test_search_mods_lowp_rescore(mods_full, oracle, precision):
+    """BF16 / FP16 rows choose the kept candidates (modified included), FP32
+    rescoring restores the oracle's FP32 top-10."""
+    import hfx_gb300
+    eng, prot, sp = mods_full
+    ref = oracle.search(*_oracle_db(oracle, eng, prot), sp, topn=10, ma=MA, ma_mass=MA_MASS, max_ma=4)
+    res = eng.search(sp, hfx_gb300.default_params(top_n=10, batch_mode=1, precision=precision, rescore_k=32))
+    _compare(res, ref, f"mods precision {precision}")
+
+
+def test_search_mods_only_and_per_type(gpulib, tiny, oracle):
+    """Modified candidates alone (no unmodified search) and the per-acid
+    i-th counter."""
+    import hfx_gb300
+    prot, sp, cfg = tiny
+    for per_type in (False, True):
+        eng = _engine(prot, max_ma=3, per_type=per_type)
+        try:
+            db = _oracle_db(oracle, eng, prot)
+            ref = oracle.search(*db, sp, topn=10, ma=MA, ma_mass=MA_MASS, max_ma=3, per_type=per_type, plain=False)
+            res = eng.search(sp, hfx_gb300.default_params(top_n=10, batch_mode=1, search_plain=0))
+            _compare(res, ref, f"mods only per_type={per_type}")
+            assert (res.key[res.key != np.iinfo(np.uint64).max] >> np.uint64(63) == 1).all()
+        finally:
+            eng.close()
+
+
+def test_search_mods_edge_charges(mods_tiny, oracle):
+    """Charge 7 (no unmodified ions, 4 modified charges) and charge 12 (no
+    ions either way: every candidate scores 0) next to ordinary spectra."""
+    import hfx_gb300
+    eng, prot, sp = mods_tiny
+    sub = sp.subset(np.arange(8))
+    sub.z[1] = 7.0
+    sub.z[2] = 12.0
+    sub.tol[3] = 1e-7
+    ref = oracle.search(*_oracle_db(oracle, eng, prot), sub, topn=10, ma=MA, ma_mass=MA_MASS, max_ma=4)
+    for mode in (1, 2):
+        res = eng.search(sub, hfx_gb300.default_params(top_n=10, batch_mode=mode))
+        _compare(res, ref, f"mods edges mode={mode}")
+    assert (res.score[2][res.key[2] != np.iinfo(np.uint64).max] == 0).all()
