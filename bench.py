@@ -1,12 +1,19 @@
 """Benchmark: peptide-spectrum XCorrs/s of the SEQUEST search hot path.
 
 One step = one full search (stages a-e) of one batch of synthetic spectra
-against the synthetic database: the 'full' configuration (20,000 random
-proteins, 10,000 spectra at charge 1-4, 50-400 peaks, +-3 Da, 1.0005 Da bins,
-top-10).  `value` times steps whose inputs are already resident in HBM
+against the synthetic database.  Default workload 'full': 20,000 random
+proteins, 10,000 spectra at charge 1-4, 50-400 peaks, +-3 Da, 1.0005 Da
+bins, top-10, searched by the batched engine over per-step ion lists with
+BF16-stored spectra and FP32 rescoring (the top-10 equals the FP32
+search's).  `value` times steps whose inputs are already resident in HBM
 (hfx_search_device); `e2e` times the same search through hfx_search_host
 with pinned host buffers, copies included.  Between timed steps the L2 is
 flushed by writing a 512 MB buffer (outside the timed events).
+
+Beside the headline the line carries the plain FP32 path (one launch per
+spectrum) timed on the same spectra, the top-10 agreement of the headline
+search with it and with the FP64 oracle on a sample, and the oracle timed
+on the host cores (cpu_baseline).
 
 --impl reference times the reference's search restated on the CPU (the
 oracle port: the reference's Haskell host and CUDA kernels cannot run on
@@ -34,6 +41,12 @@ sys.path.insert(0, ROOT)
 
 METRIC = "peptide-spectrum XCorrs/s"
 UNIT = "PSM/s"
+KERNELS = {0: "k_score_spectrum", 1: "k_score_lists", 2: "k_score_batched"}
+
+# DRAM bytes (read + write) per launch of the scorer, from one ncu capture
+# of the default workload (profiles/k_score_lists_full_bf16.txt), keyed by
+# (kernel, workload, precision, spectra).
+TRAFFIC = {}
 
 
 def _args():
@@ -44,11 +57,14 @@ def _args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="full")
     ap.add_argument("--spectra", type=int, default=0, help="override the number of spectra")
-    ap.add_argument("--precision", type=int, default=-1, help="0 fp32, 1 bf16+rescore, 2 fp16+rescore")
-    ap.add_argument("--batch-mode", type=int, default=-1, help="0 per-spectrum launches, 1 batched")
-    ap.add_argument("--cpu-sample", type=int, default=2000, help="spectra in the CPU baseline sample")
-    ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--precision", type=int, default=1, help="0 fp32, 1 bf16+rescore, 2 fp16+rescore")
+    ap.add_argument("--batch-mode", type=int, default=1,
+                    help="0 per-spectrum launches, 1 batched over ion lists, 2 batched fused")
+    ap.add_argument("--cpu-sample", type=int, default=10000, help="spectra in the CPU baseline sample")
+    ap.add_argument("--agree-sample", type=int, default=1000, help="spectra checked against the FP64 oracle")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and the FP64 agreement")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison")
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--out", default="")
     ap.add_argument("--group-size", type=int, default=0, help="spectra per batched work item (0 = default)")
     ap.add_argument("--chunk", type=int, default=0, help="candidates per batched work item (0 = default)")
@@ -128,6 +144,13 @@ def _peaks():
         return 6800.0, "fallback"
 
 
+def _charges(z):
+    zm = z - 1.0
+    mc = zm if zm >= 1.0 else 1.0
+    ch = int(np.rint(mc))
+    return ch if 1 <= ch <= 4 else 0
+
+
 def _bytes_per_psm(eng, rows_dtype_bytes, wb, we, lens, charges, idx_tc_tn, rng, n=4000):
     """Algorithmic bytes per pair: U*s + L + 16 (U = distinct in-range ion
     bins, s = stored element size, L = residue bytes, 16 = r, tc, tn, id),
@@ -150,29 +173,35 @@ def _bytes_per_psm(eng, rows_dtype_bytes, wb, we, lens, charges, idx_tc_tn, rng,
     return float(np.mean(U * rows_dtype_bytes + L + 16)), float(U.mean())
 
 
-def run_reference(a, rank, world):
-    """CPU arm: the oracle port of the reference search, all host threads."""
-    if rank != 0:
-        return
+def _oracle_inputs(prot, cfg):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     from hfx_gb300 import synth
     O.build()
-    prot, sp, cfg = _workload(a.workload, a.spectra, 0)
     mt = O.mass_table(True, synth.static_mods())
     d = {k: v for k, v in synth.DIGEST.items() if k != "mono"}
     r, tc, tn = O.digest(prot.seq, prot.seg, mt, **d)
     idx = O.sort_idx(r)
-    ions = O.pack_ions(prot.seq)
+    ma = cfg.get("ma", "").encode()
+    ions = O.pack_ions(prot.seq, ma)
+    mods = dict(ma=ma, ma_mass=cfg.get("ma_mass", ()), max_ma=cfg.get("max_ma", 0))
+    return O, (ions, mt, r, tc, tn, idx), mods
+
+
+def run_reference(a, rank, world):
+    """CPU arm: the oracle port of the reference search, all host threads."""
+    if rank != 0:
+        return
+    prot, sp, cfg = _workload(a.workload, a.spectra, 0)
+    O, db, mods = _oracle_inputs(prot, cfg)
     sample = sp.subset(np.arange(min(len(sp), max(50, a.cpu_sample // 4))))
     threads = os.cpu_count() or 1
     for _ in range(max(1, min(a.warmup, 1))):
-        O.search(ions, mt, r, tc, tn, idx, sample.subset(np.arange(min(20, len(sample)))), topn=cfg["top_n"],
-                 nthreads=threads)
+        O.search(*db, sample.subset(np.arange(min(20, len(sample)))), topn=cfg["top_n"], nthreads=threads, **mods)
     t0 = time.perf_counter()
     psm = 0
     for _ in range(a.steps):
-        res = O.search(ions, mt, r, tc, tn, idx, sample, topn=cfg["top_n"], nthreads=threads)
+        res = O.search(*db, sample, topn=cfg["top_n"], nthreads=threads, **mods)
         psm += int(res[4].sum())
     dt = time.perf_counter() - t0
     v = psm / dt
@@ -185,6 +214,49 @@ def run_reference(a, rank, world):
                              "sample": f"{len(sample)} spectra of the {a.workload} workload per step"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def _cpu_baseline(a, O, db, mods, sp, cfg):
+    sample = sp.subset(np.arange(min(len(sp), a.cpu_sample)))
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    res = O.search(*db, sample, topn=cfg["top_n"], nthreads=threads, **mods)
+    dt = time.perf_counter() - t0
+    return {"value": float(res[4].sum()) / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {len(sample)} of {len(sp)} spectra, {int(res[4].sum())} pairs, {dt:.1f} s"}
+
+
+def _agreement(a, O, db, mods, sp, cfg, key, score):
+    """Top-10 agreement of the GPU result with the FP64 oracle on a sample:
+    the fraction of spectra whose top-N candidates (keys, in order) match,
+    and the largest relative XCorr difference of the matched entries."""
+    n = min(len(sp), a.agree_sample)
+    sample = sp.subset(np.arange(n))
+    threads = os.cpu_count() or 1
+    _, s64, k64, _, _ = O.search(*db, sample, topn=cfg["top_n"], prec=3, nthreads=threads, **mods)
+    same_order = np.all(k64 == key[:n], axis=1)
+    same_set = np.array([set(k64[i]) == set(key[i]) for i in range(n)])
+    ok = (k64 != np.iinfo(np.uint64).max) & (k64 == key[:n])
+    denom = np.maximum(np.abs(s64[ok]), 1e-30)
+    rel = np.abs(score[:n][ok].astype(np.float64) - s64[ok]) / denom
+    return {"spectra": n, "top_order": float(same_order.mean()), "top_set": float(same_set.mean()),
+            "max_rel_err": float(rel.max()) if rel.size else 0.0,
+            "mean_rel_err": float(rel.mean()) if rel.size else 0.0}
+
+
+def _timed(eng, dev, p, out, steps, flush, stream):
+    """Device time of `steps` searches, L2 flushed before each (outside the events)."""
+    import torch
+    total_ms = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        eng.search_device(dev, p, out)
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+    return total_ms
 
 
 def main():
@@ -202,10 +274,12 @@ def main():
     from hfx_gb300 import synth
     eng = hfx_gb300.Engine(local)
     eng.build_db(prot.seq, prot.seg, static_add=synth.static_mods(), **synth.DIGEST)
+    has_mods = bool(cfg.get("ma"))
+    if has_mods:
+        eng.set_mods(cfg["ma"], cfg["ma_mass"], cfg["max_ma"])
     stream = torch.cuda.current_stream()
     eng.set_stream(stream.cuda_stream)
-    prec = a.precision if a.precision >= 0 else 0
-    mode = a.batch_mode if a.batch_mode >= 0 else 0
+    prec, mode = a.precision, a.batch_mode
     p = hfx_gb300.default_params(top_n=cfg["top_n"], bin_width=cfg["bin_width"], precision=prec, batch_mode=mode,
                                  rescore_k=32 if prec else 0, group_size=a.group_size, chunk=a.chunk)
     d = torch.device("cuda", local)
@@ -213,41 +287,41 @@ def main():
                off=torch.from_numpy(sp.off).to(d), pcr=torch.from_numpy(sp.pcr).to(d),
                z=torch.from_numpy(sp.z).to(d), tol=torch.from_numpy(sp.tol).to(d))
     ns, tn_ = len(sp), cfg["top_n"]
-    out = dict(score=torch.empty((ns, tn_), dtype=torch.float32, device=d),
-               key=torch.empty((ns, tn_), dtype=torch.int64, device=d),
-               pep=torch.empty((ns, tn_), dtype=torch.int32, device=d),
-               ncand=torch.empty(ns, dtype=torch.int64, device=d))
+
+    def outputs():
+        return dict(score=torch.empty((ns, tn_), dtype=torch.float32, device=d),
+                    key=torch.empty((ns, tn_), dtype=torch.int64, device=d),
+                    pep=torch.empty((ns, tn_), dtype=torch.int32, device=d),
+                    ncand=torch.empty(ns, dtype=torch.int64, device=d))
+    out = outputs()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=d)
     for _ in range(a.warmup):
         eng.search_device(dev, p, out)
     torch.cuda.synchronize()
     psm_step = int(out["ncand"].sum().item())
-    eng.set_profiling(True)
-    eng.stage_stats(reset=True)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     clk = Clocks(local)
-    total_ms = 0.0
-    for _ in range(a.steps):
-        flush.zero_()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        eng.search_device(dev, p, out)
-        e1.record(stream)
-        e1.synchronize()
-        total_ms += e0.elapsed_time(e1)
+    total_ms = _timed(eng, dev, p, out, a.steps, flush, stream)
     torch.cuda.synchronize()
     clocks = clk.stop()
-    stats = eng.stage_stats(reset=True)
-    work = {k: v // a.steps for k, v in eng.counters(reset=True).items()}
-    eng.set_profiling(False)
     if world > 1:
         t = torch.tensor([total_ms], device=d)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
     ms_step = total_ms / a.steps
     value = psm_step * world / (ms_step / 1000.0)
+    # per-stage device times and work counters: the same steps again, with stage events
+    eng.set_profiling(True)
+    eng.stage_stats(reset=True)
+    eng.counters(reset=True)
+    _timed(eng, dev, p, out, a.steps, flush, stream)
+    stats = eng.stage_stats(reset=True)
+    work = {k: v // a.steps for k, v in eng.counters(reset=True).items()}
+    eng.set_profiling(False)
+    key = out["key"].cpu().numpy().view(np.uint64)
+    score = out["score"].cpu().numpy()
     # e2e through the host-buffer C ABI (pinned buffers, copies in the timed region)
     pin = {k: torch.from_numpy(v).pin_memory() for k, v in
            dict(mz=sp.mz, it=sp.it, off=sp.off, pcr=sp.pcr, z=sp.z, tol=sp.tol).items()}
@@ -267,8 +341,27 @@ def main():
         eng.search(Pinned(), p)
         e2e_tot += time.perf_counter() - t1
     e2e_value = psm_step * world / (e2e_tot / a.e2e_steps)
-    # roofline of the dominant kernel (the scorer)
-    sc_ms, sc_launch, sc_units = stats["score"]
+    # the plain FP32 path (one launch per spectrum) on the same spectra
+    plain = None
+    if not a.no_plain and not has_mods:
+        p0 = hfx_gb300.default_params(top_n=tn_, bin_width=cfg["bin_width"], precision=0, batch_mode=0)
+        out0 = outputs()
+        eng.search_device(dev, p0, out0)
+        torch.cuda.synchronize()
+        n0 = max(1, min(3, a.steps))
+        ms0 = _timed(eng, dev, p0, out0, n0, flush, stream) / n0
+        k0 = out0["key"].cpu().numpy().view(np.uint64)
+        s0 = out0["score"].cpu().numpy()
+        plain = {"value": psm_step / (ms0 / 1000.0), "unit": UNIT, "ms_per_step": ms0,
+                 "speedup": (psm_step / (ms_step / 1000.0)) / (psm_step / (ms0 / 1000.0)),
+                 "top_agreement": float(np.mean(np.all(k0 == key, axis=1))),
+                 "scores_bitexact": bool(np.array_equal(s0.view(np.uint32), score.view(np.uint32)))}
+    # roofline of the dominant kernel
+    stage = "mods" if has_mods and stats["mods"][0] > stats["score"][0] else "score"
+    kern = "k_score_mods" if stage == "mods" else KERNELS[mode if mode in KERNELS else 1]
+    if has_mods and mode == 0:
+        kern = "k_score_mods" if stage == "mods" else "k_score_batched"
+    sc_ms, sc_launch, _ = stats[stage]
     rng = np.random.Generator(np.random.PCG64(7))
     r, tc, tn, idx, mt = eng.db_export()
     bsz = 2 if prec else 4
@@ -284,32 +377,45 @@ def main():
     del rows
     charges = np.array([_charges(z) for z in sp.z], np.int64)
     bpp, meanU = _bytes_per_psm(eng, bsz, wb, we, lens, charges, (tc[idx], tn[idx]), rng)
+    # pairs scored by the dominant kernel per launch (all of the step's pairs
+    # go through it, or its modified share when it is the modification scorer)
+    psm_kernel = psm_step
+    if stage == "mods":
+        psm_kernel = psm_step - int(np.sum(np.where(lens > 0, we - wb, 0)))
+    elif has_mods:
+        psm_kernel = int(np.sum(np.where(lens > 0, we - wb, 0)))
     per_launch_ms = sc_ms / max(1, sc_launch)
-    # every pair of the step is scored by exactly one launch of the scorer
-    per_launch_psm = psm_step * a.steps / max(1, sc_launch)
+    per_launch_psm = psm_kernel * a.steps / max(1, sc_launch)
     achieved = bpp * per_launch_psm / (per_launch_ms / 1000.0) / 1e9
     peak, peak_kind = _peaks()
+    traffic = TRAFFIC.get((kern, a.workload, prec, ns))
     launches_per_step = sum(v[1] for v in stats.values()) / a.steps
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": ["f32", "bf16-store/f32", "f16-store/f32"][prec], "data": "synthetic",
-        "config": {"workload": f"{a.workload}: 20000 proteins, {ns} spectra, +-3 Da, 1.0005 Da bins, top-{tn_}",
-                   "psm_per_step": psm_step, "precision": ["fp32", "bf16+fp32 rescore", "fp16+fp32 rescore"][prec],
-                   "batch_mode": ["per-spectrum launches", "persistent batched"][mode],
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{a.workload}: 20000 proteins, {ns} spectra, +-3 Da, 1.0005 Da bins, top-{tn_}"
+                               + (", variable M+15.995 S/T/Y+79.966 up to 3" if has_mods else ""),
+                   "psm_per_step": psm_step,
+                   "precision": ["fp32", "bf16 store + fp32 rescore", "fp16 store + fp32 rescore"][prec],
+                   "batch_mode": ["per-spectrum launches", "batched over ion lists", "batched fused"][mode],
                    "l2": "flushed between timed steps (512 MB write)",
                    "stage_ms_per_step": {k: v[0] / a.steps for k, v in stats.items() if v[1]},
                    "work_per_step": work},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": int(launches_per_step),
+        "gpu_launches": int(launches_per_step * a.steps),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "kernel": "k_score_spectrum" if mode == 0 else "k_score_batched",
-                     "bytes_per_psm": bpp, "mean_distinct_bins": meanU, "peak_kind": peak_kind},
+                     "frac": achieved / peak, "traffic": traffic, "kernel": kern,
+                     "bytes_per_psm": bpp, "mean_distinct_bins": meanU, "peak_kind": peak_kind,
+                     "step_achieved": bpp * psm_step / (ms_step / 1000.0) / 1e9},
         "clocks": clocks,
     }
+    if plain is not None:
+        line["plain_fp32"] = plain
     if rank == 0 and not a.no_cpu:
-        line["cpu_baseline"] = _cpu_baseline(a, prot, sp, cfg)
+        O, db, mods = _oracle_inputs(prot, cfg)
+        line["fp64_agreement"] = _agreement(a, O, db, mods, sp, cfg, key, score)
+        line["cpu_baseline"] = _cpu_baseline(a, O, db, mods, sp, cfg)
     if rank == 0:
         s = json.dumps(line)
         print(s, flush=True)
@@ -319,32 +425,6 @@ def main():
     eng.close()
     if world > 1:
         torch.distributed.destroy_process_group()
-
-
-def _charges(z):
-    zm = z - 1.0
-    mc = zm if zm >= 1.0 else 1.0
-    ch = int(np.rint(mc))
-    return ch if 1 <= ch <= 4 else 0
-
-
-def _cpu_baseline(a, prot, sp, cfg):
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    from hfx_gb300 import synth
-    O.build()
-    mt = O.mass_table(True, synth.static_mods())
-    d = {k: v for k, v in synth.DIGEST.items() if k != "mono"}
-    r, tc, tn = O.digest(prot.seq, prot.seg, mt, **d)
-    idx = O.sort_idx(r)
-    ions = O.pack_ions(prot.seq)
-    sample = sp.subset(np.arange(min(len(sp), a.cpu_sample)))
-    threads = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    res = O.search(ions, mt, r, tc, tn, idx, sample, topn=cfg["top_n"], nthreads=threads)
-    dt = time.perf_counter() - t0
-    return {"value": float(res[4].sum()) / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"first {len(sample)} of {len(sp)} spectra, {int(res[4].sum())} pairs, {dt:.1f} s"}
 
 
 if __name__ == "__main__":

@@ -33,7 +33,7 @@ EXPORTED = [
     "hfx_preprocess", "hfx_find_windows", "hfx_ion_bins", "hfx_mod_isoforms", "hfx_digest", "hfx_pack_ions",
     "hfx_set_profiling", "hfx_stage_stats", "hfx_search_counters",
 ]
-STAGES = ["layout", "preprocess", "windows", "score", "topn", "rescore", "mods", "lists"]
+STAGES = ["layout", "preprocess", "windows", "score", "topn", "rescore", "mods", "lists", "pack"]
 
 
 class HfxError(RuntimeError):
@@ -196,11 +196,12 @@ class Engine:
 
     def stage_stats(self, reset: bool = True):
         """{stage: (milliseconds, launches, units)} accumulated since the last reset."""
-        ms = np.zeros(8, np.float64)
-        nl = np.zeros(8, np.int64)
-        nu = np.zeros(8, np.int64)
+        n = len(STAGES)
+        ms = np.zeros(n, np.float64)
+        nl = np.zeros(n, np.int64)
+        nu = np.zeros(n, np.int64)
         self._check(self.lib.hfx_stage_stats(self.h, _ptr(ms), _ptr(nl), _ptr(nu), int(reset)))
-        return {STAGES[i]: (float(ms[i]), int(nl[i]), int(nu[i])) for i in range(8)}
+        return {STAGES[i]: (float(ms[i]), int(nl[i]), int(nu[i])) for i in range(n)}
 
     def counters(self, reset: bool = True):
         """Work counters of the batched list path (see hfx_search_counters)."""

@@ -475,7 +475,7 @@ static int launch_batched_t(const DevDB &db, const T *rows, int64_t stride, cons
                             const uint32_t *we, const BatchedWs &ws, void *tiles, uint32_t ngroups, int32_t chunk,
                             int32_t K, int nw, int grid, float *part_s, uint64_t *part_k, uint32_t *err,
                             cudaStream_t st) {
-    if (ngroups > 0) hfx_pack_tiles_launch<T, G>(rows, stride, meta, ws, (T *)tiles, ngroups, st);
+    (void)rows;
     int dev = 0, sms = 0, smem_max = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -31,8 +31,8 @@ constexpr int kBucketCount = 12 * 8192;
 size_t hfx_batched_smem(int64_t stride, int elem_bytes, int G, int nw, int K);
 int hfx_batched_plan(const hfx::SpecMeta *meta, int32_t nspec, const uint32_t *wb, const uint32_t *we, int32_t G,
                      int32_t chunk, const hfx::BatchedWs &ws, cudaStream_t st);
-// Packs the group tiles (tiles: ngroups * stride * G elements) and runs the
-// persistent scorer; nw = warps per CTA (0 = as many as shared memory holds,
+// Runs the persistent scorer over the group tiles packed by hfx_pack_tiles
+// (tiles: ngroups * stride * G elements); nw = warps per CTA (0 = as many as shared memory holds,
 // at most 16), grid = CTAs (0 = one wave).
 int hfx_batched_score(const hfx::DevDB &db, const void *rows, int elem_kind, int64_t stride,
                       const hfx::SpecMeta *meta, const uint32_t *wb, const uint32_t *we, const hfx::BatchedWs &ws,

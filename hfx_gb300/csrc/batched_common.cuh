@@ -84,6 +84,105 @@ __device__ __forceinline__ float smem_topk_insert(float *ks, uint64_t *kk, float
     return __shfl_sync(kFullMask, out, K - 1);
 }
 
+// Order-preserving map of a float score to uint32 (for atomicMax thresholds).
+__device__ __forceinline__ uint32_t score_order(float s) {
+    const uint32_t b = __float_as_uint(s);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+// Lane that holds member slot j's score after reduce_scatter<G>.
+template <int G> __host__ __device__ constexpr int slot_lane(int j) { return j * (32 / G); }
+
+// Per-warp top-K of every member slot, in registers (lane i holds entry i
+// of each slot, best first).  A shared per-slot admission threshold -- the
+// best K-th score any warp of the CTA has reached, a lower bound of the
+// CTA's K-th -- filters the offers, so warps share what they learn without
+// locks; the CTA's top-K is the top-K of the union of the warps' lists.
+template <int G>
+struct WarpSlots {
+    float s[G];
+    uint32_t k[G];
+
+    __device__ __forceinline__ void init() {
+#pragma unroll
+        for (int j = 0; j < G; ++j) {
+            s[j] = -INFINITY;
+            k[j] = 0xFFFFFFFFu;
+        }
+    }
+
+    // Offer candidate `key`: slot j's score sits in lane slot_lane<G>(j) of
+    // sc; ins has that lane's bit set when slot j takes the offer.
+    __device__ __forceinline__ void offer(float sc, uint32_t key, uint32_t ins, int K, uint32_t *thr_u) {
+        const int lane = threadIdx.x & 31;
+#pragma unroll
+        for (int j = 0; j < G; ++j) {
+            if (ins & (1u << slot_lane<G>(j))) {
+                const float ns = __shfl_sync(kFullMask, sc, slot_lane<G>(j));
+                const bool mb = lane < K && (s[j] > ns || (s[j] == ns && k[j] < key));
+                const int pos = __popc(__ballot_sync(kFullMask, mb));
+                const float us = __shfl_up_sync(kFullMask, s[j], 1);
+                const uint32_t uk = __shfl_up_sync(kFullMask, k[j], 1);
+                if (pos < K) {
+                    if (lane == pos) {
+                        s[j] = ns;
+                        k[j] = key;
+                    } else if (lane > pos && lane < K) {
+                        s[j] = us;
+                        k[j] = uk;
+                    }
+                    const float kth = __shfl_sync(kFullMask, s[j], K - 1);
+                    if (lane == 0 && kth != -INFINITY) {
+                        const uint32_t o = score_order(kth);
+                        if (o > *(volatile uint32_t *)(thr_u + j)) atomicMax(thr_u + j, o);
+                    }
+                }
+            }
+        }
+    }
+
+    // Item end, step 1: append the entries that can still be in the CTA's
+    // top-K (score order >= the final threshold) to the slot's buffer.
+    __device__ __forceinline__ void flush(const uint32_t *thr_u, uint32_t *cnt, float *buf_s, uint32_t *buf_k,
+                                          int cap, int K) {
+        const int lane = threadIdx.x & 31;
+#pragma unroll
+        for (int j = 0; j < G; ++j) {
+            const bool keep = lane < K && k[j] != 0xFFFFFFFFu && score_order(s[j]) >= thr_u[j];
+            const uint32_t bal = __ballot_sync(kFullMask, keep);
+            if (!bal) continue;
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(cnt + j, (uint32_t)__popc(bal));
+            base = __shfl_sync(kFullMask, base, 0);
+            const uint32_t at = base + __popc(bal & ((1u << lane) - 1u));
+            if (keep && at < (uint32_t)cap) {
+                buf_s[j * cap + at] = s[j];
+                buf_k[j * cap + at] = k[j];
+            }
+        }
+    }
+};
+
+// Item end, step 2 (one warp per slot): the slot's top-K from its buffer.
+__device__ __forceinline__ void slot_merge(const float *bs, const uint32_t *bk, uint32_t n, int K, float *out_s,
+                                           uint64_t *out_k) {
+    const int lane = threadIdx.x & 31;
+    WarpTopK tk;
+    tk.init();
+    for (uint32_t b0 = 0; b0 < n; b0 += 32) {
+        const uint32_t i = b0 + lane;
+        const float es = i < n ? bs[i] : -INFINITY;
+        const uint32_t ek = i < n ? bk[i] : 0xFFFFFFFFu;
+        const uint32_t m = min(32u, n - b0);
+        for (uint32_t t = 0; t < m; ++t)
+            tk.insert(__shfl_sync(kFullMask, es, t), (uint64_t)__shfl_sync(kFullMask, ek, t), K);
+    }
+    if (lane < K) {
+        out_s[lane] = tk.s;
+        out_k[lane] = tk.k;
+    }
+}
+
 template <int G>
 __device__ __forceinline__ uint32_t slot_owner_mask() {
     // one lane per slot among the lanes that hold the same reduced slot

@@ -423,7 +423,7 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_windows");
     rc = hfx_batched_plan(meta, ns, wb, we, G, chunk, ws, ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "plan");
-    ctx->stage_end(HFX_STAGE_WINDOWS, 7, ns);
+    ctx->stage_end(HFX_STAGE_WINDOWS, 6, ns);  // k_windows + 5 planning kernels
     uint32_t hs[4];
     HFX_CUDA(cudaMemcpyAsync(hs, scal, 16, cudaMemcpyDeviceToHost, ctx->stream), "D2H plan");
     HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
@@ -440,16 +440,18 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     const void *src_rows = elem_kind == 0 ? (const void *)rows : rows_lo;
     const bool plain_on = p->search_plain != 0;
     const bool mods_on = p->search_mods != 0 && ctx->num_mod > 0;
+    ctx->stage_begin(HFX_STAGE_PACK);
+    rc = hfx_pack_tiles(src_rows, elem_kind, stride, meta, ws, tiles, ngroups, G, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_pack_tiles");
+    ctx->stage_end(HFX_STAGE_PACK, ngroups > 0 ? 1 : 0, ngroups);
     if (!plain_on) {
-        rc = hfx_pack_tiles(src_rows, elem_kind, stride, meta, ws, tiles, ngroups, G, ctx->stream);
-        if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_pack_tiles");
     } else if (p->batch_mode != 1) {
         // fused: every work item rebuilds its candidates' ion lists
         ctx->stage_begin(HFX_STAGE_SCORE);
         rc = hfx_batched_score(db, src_rows, elem_kind, stride, meta, wb, we, ws, tiles, ngroups, G, chunk, K, 0, 0,
                                p->fastdiv, ps, pk, ctx->d_err.as<uint32_t>(), ctx->stream);
         if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_batched");
-        ctx->stage_end(HFX_STAGE_SCORE, 2, 0);
+        ctx->stage_end(HFX_STAGE_SCORE, 1, 0);
     } else {
         // lists: one ion list per needed (peptide, charge level), then scoring
         const int64_t npep1 = (int64_t)ctx->num_pep + 1;
@@ -484,7 +486,7 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
                              elem_kind, stride, meta, wb, we, ws, tiles, ngroups, G, chunk, K, 0, ps, pk, stats,
                              ctx->d_err.as<uint32_t>(), ctx->stream);
         if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_lists");
-        ctx->stage_end(HFX_STAGE_SCORE, 2, 0);
+        ctx->stage_end(HFX_STAGE_SCORE, 1, 0);
         if (stats) {
             unsigned long long h[8];
             HFX_CUDA(cudaMemcpyAsync(h, stats, 64, cudaMemcpyDeviceToHost, ctx->stream), "D2H stats");
@@ -536,7 +538,8 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
                                 p->fastdiv, ms, mk, ncm, ctx->d_err.as<uint32_t>(), ctx->stream);
             if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_mods");
         }
-        ctx->stage_end(HFX_STAGE_MODS, 4, mtotal);
+        // k_mod_windows, k_mod_groups, 3 scan kernels, k_score_mods
+        ctx->stage_end(HFX_STAGE_MODS, n_gm > 0 ? 5 + (mtotal > 0 ? 1 : 0) : 1, mtotal);
     }
     float *ks = ctx->buf<float>("kept_s", (size_t)ns * K, e);
     if (e) return cuda_fail(ctx, e, "alloc");
@@ -549,21 +552,22 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     else
         rc = hfx_batched_merge(ps, pk, ws, meta, ns, G, K, K, ks, kk, ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_merge_items");
-    ctx->stage_end(HFX_STAGE_TOPN, 1, ns);
     if (elem_kind == 0) {
         rc = hfx_finish(ks, kk, ns, p->top_n, ctx->d_idx.as<uint32_t>(), wb, we, meta, out_s, out_k, out_pep,
                         plain_on, ncm, out_ncand, ctx->stream);
         if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_finish");
+        ctx->stage_end(HFX_STAGE_TOPN, 2, ns);
     } else {
+        ctx->stage_end(HFX_STAGE_TOPN, 1, ns);
         ctx->stage_begin(HFX_STAGE_RESCORE);
         rc = hfx_rescore(db, dm, rows, stride, meta, ks, kk, ns, K, p->top_n, p->fastdiv, out_s, out_k, out_pep,
                          ctx->stream);
         if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_rescore");
-        ctx->stage_end(HFX_STAGE_RESCORE, 1, (int64_t)ns * K);
         if (out_ncand) {
             rc = hfx_ncand(wb, we, meta, ns, plain_on, ncm, out_ncand, ctx->stream);
             if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_ncand");
         }
+        ctx->stage_end(HFX_STAGE_RESCORE, out_ncand ? 2 : 1, (int64_t)ns * K);
     }
     return HFX_OK;
 }

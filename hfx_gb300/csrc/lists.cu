@@ -19,6 +19,7 @@
 #include "device_common.cuh"
 #include "batched.h"
 #include "lists.h"
+#include <algorithm>
 #include "batched_common.cuh"
 
 namespace hfx {
@@ -238,17 +239,17 @@ k_score_lists(const uint16_t *__restrict__ lists, const uint32_t *__restrict__ l
               float *__restrict__ part_s, uint64_t *__restrict__ part_k, unsigned long long *__restrict__ stats,
               uint32_t *__restrict__ err) {
     extern __shared__ __align__(128) uint8_t smem[];
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     T *stile = reinterpret_cast<T *>(smem + 128);
-    const size_t tile_bytes = ((size_t)stride * G * sizeof(T) + 15) & ~(size_t)15;
-    float *tk_s = reinterpret_cast<float *>(smem + 128 + tile_bytes);
-    uint64_t *tk_k = reinterpret_cast<uint64_t *>(tk_s + ((G * K + 1) & ~1));
-    float *thr = reinterpret_cast<float *>(tk_k + G * K);
-    uint32_t *locks = reinterpret_cast<uint32_t *>(thr + G);
+    // after an item's candidates the tile region holds the warps' surviving entries
+    const int cap = nw * K;
+    float *buf_s = reinterpret_cast<float *>(smem + 128);
+    uint32_t *buf_k = reinterpret_cast<uint32_t *>(buf_s + (size_t)G * cap);
     __shared__ int32_t s_item;
     __shared__ uint32_t s_next;
     __shared__ uint32_t s_wb[G], s_we[G];
+    __shared__ uint32_t thr_u[G], cnt[G];
     __shared__ unsigned long long s_stats[3];
 
     const int32_t ngroups = (int32_t)*ngroups_p;
@@ -259,6 +260,7 @@ k_score_lists(const uint16_t *__restrict__ lists, const uint32_t *__restrict__ l
     const int my_slot = reduce_slot_of_lane<G>(lane);
     unsigned long long my_cand = 0, my_entries = 0, my_psm = 0;
     uint32_t phase = 0;
+    WarpSlots<G> slots;
     while (true) {
         if (threadIdx.x == 0) s_item = (int32_t)atomicAdd(counter, 1u);
         __syncthreads();
@@ -268,25 +270,19 @@ k_score_lists(const uint16_t *__restrict__ lists, const uint32_t *__restrict__ l
         const GroupInfo gi = groups[g];
         const uint32_t p0 = gi.lo + (item - item_off[g]) * (uint32_t)chunk;
         const uint32_t p1 = min(gi.hi, p0 + (uint32_t)chunk);
-        const int cnt = (int)gi.count;
+        const int cnt_members = (int)gi.count;
         if (threadIdx.x < G) {
             const int j = threadIdx.x;
             uint32_t b = 0, e = 0;
-            if (j < cnt) {
+            if (j < cnt_members) {
                 const int32_t s = perm[gi.pos0 + j];
                 b = wb[s];
                 e = we[s];
             }
             s_wb[j] = b;
             s_we[j] = e;
-        }
-        for (int i = threadIdx.x; i < G * K; i += blockDim.x) {
-            tk_s[i] = -INFINITY;
-            tk_k[i] = ~0ull;
-        }
-        if (threadIdx.x < G) {
-            thr[threadIdx.x] = -INFINITY;
-            locks[threadIdx.x] = 0u;
+            thr_u[j] = 0u;
+            cnt[j] = 0u;
         }
         if (threadIdx.x == 0) s_next = p0;
         const int32_t nb = tile_bins(gi.maxlen);
@@ -296,6 +292,7 @@ k_score_lists(const uint16_t *__restrict__ lists, const uint32_t *__restrict__ l
             mbar_arrive_expect_tx(bar, bytes);
             bulk_g2s(stile, tiles + (size_t)g * stride * G, bytes, bar);
         }
+        slots.init();
         __syncthreads();
         if (!mbar_wait(bar, phase, kWaitLimit)) {
             if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
@@ -342,38 +339,17 @@ k_score_lists(const uint16_t *__restrict__ lists, const uint32_t *__restrict__ l
                 }
             }
             const float sc = reduce_scatter<G>(acc);
-            const bool want = ((act >> my_slot) & 1u) && sc >= thr[my_slot];
-            uint32_t ins = __ballot_sync(kFullMask, want) & slot_owner_mask<G>();
-            while (ins) {
-                const int src = __ffs(ins) - 1;
-                ins &= ins - 1u;
-                const int j = reduce_slot_of_lane<G>(src);
-                const float s = __shfl_sync(kFullMask, sc, src);
-                uint32_t ok = 1u;
-                if (lane == 0) {
-                    uint32_t nn = 0;
-                    while (atomicCAS(&locks[j], 0u, 1u) != 0u) {
-                        if (++nn > kLockLimit) { ok = 0u; break; }
-                    }
-                }
-                ok = __shfl_sync(kFullMask, ok, 0);
-                if (!ok) {
-                    if (lane == 0) atomicOr(err, kErrTimeout);
-                    continue;
-                }
-                __threadfence_block();
-                const float t = smem_topk_insert(tk_s + j * K, tk_k + j * K, s, (uint64_t)p, K);
-                if (lane == 0) thr[j] = t;
-                __threadfence_block();
-                __syncwarp();
-                if (lane == 0) atomicExch(&locks[j], 0u);
-            }
+            const bool want = ((act >> my_slot) & 1u) && score_order(sc) >= *(volatile uint32_t *)(thr_u + my_slot);
+            const uint32_t ins = __ballot_sync(kFullMask, want) & slot_owner_mask<G>();
+            if (ins) slots.offer(sc, p, ins, K, thr_u);
         }
+        __syncthreads();  // every warp is done with the tile: its region takes the survivors
+        slots.flush(thr_u, cnt, buf_s, buf_k, cap, K);
         __syncthreads();
-        for (int i = threadIdx.x; i < cnt * K; i += blockDim.x) {
-            const size_t o = (size_t)item * G * K + i;
-            part_s[o] = tk_s[i];
-            part_k[o] = tk_k[i];
+        for (int j = warp; j < cnt_members; j += nw) {
+            const size_t o = ((size_t)item * G + j) * K;
+            slot_merge(buf_s + (size_t)j * cap, buf_k + (size_t)j * cap, min(cnt[j], (uint32_t)cap), K, part_s + o,
+                       part_k + o);
         }
         __syncthreads();
     }
@@ -438,18 +414,20 @@ static int launch_lists_t(const uint16_t *lists, const uint32_t *lstart, uint64_
                           const uint32_t *we, const BatchedWs &ws, void *tiles, uint32_t ngroups, int32_t chunk,
                           int32_t K, int nw, float *part_s, uint64_t *part_k, unsigned long long *stats,
                           uint32_t *err, cudaStream_t st) {
-    if (ngroups > 0) hfx_pack_tiles_launch<T, G>(rows, stride, meta, ws, (T *)tiles, ngroups, st);
+    (void)rows;
     int dev = 0, sms = 0, smem_max = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (nw <= 0) nw = 16;
     const size_t tile = ((size_t)stride * G * sizeof(T) + 15) & ~(size_t)15;
-    const size_t smem = 128 + tile + ((size_t)((G * K + 1) & ~1) * 4 + (size_t)G * K * 8 + (size_t)G * 8 + 15);
+    // the tile region doubles as the item-end buffer of the warps' survivors
+    const size_t survivors = (size_t)G * nw * K * 8;
+    const size_t smem = 128 + std::max(tile, survivors);
     if (smem > (size_t)smem_max) return (int)cudaErrorInvalidValue;
     auto fn = k_score_lists<T, G>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
-    if (nw <= 0) nw = 16;
     int per = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, nw * 32, smem);
     const int grid = sms * (per > 0 ? per : 1);

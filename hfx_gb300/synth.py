@@ -194,6 +194,12 @@ DIGEST = dict(mono=True, rule=1, missed=1, min_mass=400.0, max_mass=7200.0, prol
               min_len=6, max_len=50)
 
 
+# Variable modifications of the modification workload: Met oxidation and
+# Ser/Thr/Tyr phosphorylation, up to 3 per peptide (max-modable-acids 4,
+# whose combination sums are strictly below it).
+MODS = dict(ma="MSTY", ma_mass=[15.995, 79.966, 79.966, 79.966], max_ma=4)
+
+
 def workload(name: str, n_spectra: int | None = None):
     """(proteins, spectra, search settings) of a named configuration."""
     if name == "tiny":
@@ -204,7 +210,10 @@ def workload(name: str, n_spectra: int | None = None):
         prot = proteins(20000, seed=1)
         sp = spectra(prot, n_spectra or 10000, seed=101, charge_p={1: 0.05, 2: 0.5, 3: 0.35, 4: 0.10},
                      npeaks=(50, 400))
-        return prot, sp, dict(bin_width=1.0005079, top_n=10)
+        cfg = dict(bin_width=1.0005079, top_n=10)
+        if name == "mods":
+            cfg.update(MODS)
+        return prot, sp, cfg
     if name in ("batch", "highres"):
         prot = proteins(20000, seed=1)
         sp = spectra(prot, n_spectra or 100000, seed=103, charge_p={1: 0.05, 2: 0.5, 3: 0.35, 4: 0.10},

@@ -74,7 +74,8 @@ const char *hfx_last_error(const hfx_ctx *ctx);
 #define HFX_STAGE_RESCORE 5     /* FP32 rescoring of the kept candidates    */
 #define HFX_STAGE_MODS 6        /* variable-modification isoforms           */
 #define HFX_STAGE_LISTS 7       /* per-peptide ion lists of the batch       */
-#define HFX_NSTAGES 8
+#define HFX_STAGE_PACK 8        /* interleaved spectrum tiles of the groups */
+#define HFX_NSTAGES 9
 int32_t hfx_set_profiling(hfx_ctx *ctx, int32_t on);
 int32_t hfx_stage_stats(hfx_ctx *ctx, double *ms, int64_t *launches, int64_t *units, int32_t reset);
 /* Work counters of the batched list path, accumulated while profiling is on:
