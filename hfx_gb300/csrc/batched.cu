@@ -29,16 +29,6 @@ constexpr int kMassBuckets = 8192;   // 1 Da buckets of residual mass
 constexpr int kClasses = 12;         // (ion charge class 0..5) x (narrow, wide)
 constexpr float kWideEps = 1.0f;     // windows wider than this are "wide"
 
-// Shared memory of one scorer warp: bit planes + distinct-bin list.
-__host__ __device__ __forceinline__ size_t batched_warp_bytes(int32_t words) {
-    return ((size_t)3 * words * 4 + (size_t)kListCap * 2 + 15) & ~(size_t)15;
-}
-// CTA-wide top-K lists: scores (padded to 8 bytes), keys, thresholds, locks.
-__host__ __device__ __forceinline__ size_t batched_cta_bytes(int G, int K) {
-    const size_t b = (size_t)((G * K + 1) & ~1) * 4 + (size_t)G * K * 8 + (size_t)G * 4 + (size_t)G * 4;
-    return (b + 15) & ~(size_t)15;
-}
-
 __device__ __forceinline__ int spec_class(const SpecMeta &m) {
     // charge class: plain charges 1..4 (modified ones equal them), 5 = no
     // plain ions but modified ions (charge 6..11), 0 = none
@@ -177,18 +167,18 @@ k_score_batched(DevDB db, const T *__restrict__ tiles, int64_t stride, const uin
     const int32_t words_cap = (int32_t)((stride + 31) / 32);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     T *stile = reinterpret_cast<T *>(smem + 128);
-    const size_t tile_bytes = ((size_t)stride * G * sizeof(T) + 15) & ~(size_t)15;
-    // CTA-wide top-K per member spectrum: scores, keys, admission thresholds, locks
-    float *tk_s = reinterpret_cast<float *>(smem + 128 + tile_bytes);
-    uint64_t *tk_k = reinterpret_cast<uint64_t *>(tk_s + ((G * K + 1) & ~1));
-    float *thr = reinterpret_cast<float *>(tk_k + G * K);
-    uint32_t *locks = reinterpret_cast<uint32_t *>(thr + G);
-    uint8_t *wbase = smem + 128 + tile_bytes + batched_cta_bytes(G, K) + (size_t)warp * batched_warp_bytes(words_cap);
+    // after an item's candidates the tile region holds the warps' survivors
+    const int cap = nw * K;
+    float *buf_s = reinterpret_cast<float *>(smem + 128);
+    uint32_t *buf_k = reinterpret_cast<uint32_t *>(buf_s + (size_t)G * cap);
+    uint8_t *wbase = smem + 128 + fused_region_bytes(stride, sizeof(T), G, nw, K, 4) +
+                     (size_t)warp * fused_warp_bytes(words_cap);
     uint32_t *planes = reinterpret_cast<uint32_t *>(wbase);
     uint16_t *list = reinterpret_cast<uint16_t *>(planes + 3 * words_cap);
     __shared__ int32_t s_item;
     __shared__ uint32_t s_next;
     __shared__ uint32_t s_wb[G], s_we[G];
+    __shared__ uint32_t thr_u[G], cnt[G];
 
     const int32_t ngroups = (int32_t)*ngroups_p;
     const uint32_t total = item_off[ngroups];
@@ -199,6 +189,7 @@ k_score_batched(DevDB db, const T *__restrict__ tiles, int64_t stride, const uin
     const float mt_lane = db.mt[lane];
     const int my_slot = reduce_slot_of_lane<G>(lane);
     uint32_t phase = 0;
+    WarpSlots<G> slots;
 
     while (true) {
         if (threadIdx.x == 0) s_item = (int32_t)atomicAdd(counter, 1u);
@@ -209,26 +200,21 @@ k_score_batched(DevDB db, const T *__restrict__ tiles, int64_t stride, const uin
         const GroupInfo gi = groups[g];
         const uint32_t p0 = gi.lo + (item - item_off[g]) * (uint32_t)chunk;
         const uint32_t p1 = min(gi.hi, p0 + (uint32_t)chunk);
-        const int cnt = (int)gi.count;
+        const int cnt_members = (int)gi.count;
         if (threadIdx.x < G) {
             const int j = threadIdx.x;
             uint32_t b = 0, e = 0;
-            if (j < cnt) {
+            if (j < cnt_members) {
                 const int32_t s = perm[gi.pos0 + j];
                 b = wb[s];
                 e = we[s];
             }
             s_wb[j] = b;
             s_we[j] = e;
+            thr_u[j] = 0u;
+            cnt[j] = 0u;
         }
-        for (int i = threadIdx.x; i < G * K; i += blockDim.x) {
-            tk_s[i] = -INFINITY;
-            tk_k[i] = ~0ull;
-        }
-        if (threadIdx.x < G) {
-            thr[threadIdx.x] = -INFINITY;
-            locks[threadIdx.x] = 0u;
-        }
+        slots.init();
         if (threadIdx.x == 0) s_next = p0;
         const int32_t nb = tile_bins(gi.maxlen);
         if (threadIdx.x == 0) {
@@ -259,40 +245,17 @@ k_score_batched(DevDB db, const T *__restrict__ tiles, int64_t stride, const uin
             float acc[G];
             planes_accumulate<G>(pl, list, wr, dot, acc);
             const float sc = reduce_scatter<G>(acc);
-            const bool want = ((act >> my_slot) & 1u) && sc >= thr[my_slot];
-            uint32_t ins = __ballot_sync(kFullMask, want) & slot_owner_mask<G>();
-            while (ins) {
-                const int src = __ffs(ins) - 1;
-                ins &= ins - 1u;
-                const int j = reduce_slot_of_lane<G>(src);
-                const float s = __shfl_sync(kFullMask, sc, src);
-                // the CTA's list of member j is updated under a short lock;
-                // the wait is bounded and reported, never endless
-                uint32_t ok = 1u;
-                if (lane == 0) {
-                    uint32_t n = 0;
-                    while (atomicCAS(&locks[j], 0u, 1u) != 0u) {
-                        if (++n > kLockLimit) { ok = 0u; break; }
-                    }
-                }
-                ok = __shfl_sync(kFullMask, ok, 0);
-                if (!ok) {
-                    if (lane == 0) atomicOr(err, kErrTimeout);
-                    continue;
-                }
-                __threadfence_block();
-                const float t = smem_topk_insert(tk_s + j * K, tk_k + j * K, s, (uint64_t)p, K);
-                if (lane == 0) thr[j] = t;
-                __threadfence_block();
-                __syncwarp();
-                if (lane == 0) atomicExch(&locks[j], 0u);
-            }
+            const bool want = ((act >> my_slot) & 1u) && score_order(sc) >= *(volatile uint32_t *)(thr_u + my_slot);
+            const uint32_t ins = __ballot_sync(kFullMask, want) & slot_owner_mask<G>();
+            if (ins) slots.offer(sc, p, ins, K, thr_u);
         }
+        __syncthreads();  // every warp is done with the tile: its region takes the survivors
+        slots.flush(thr_u, cnt, buf_s, buf_k, cap, K);
         __syncthreads();
-        for (int i = threadIdx.x; i < cnt * K; i += blockDim.x) {
-            const size_t o = (size_t)item * G * K + i;
-            part_s[o] = tk_s[i];
-            part_k[o] = tk_k[i];
+        for (int j = warp; j < cnt_members; j += nw) {
+            const size_t o = ((size_t)item * G + j) * K;
+            slot_merge(buf_s + (size_t)j * cap, buf_k + (size_t)j * cap, min(cnt[j], (uint32_t)cap), K, part_s + o,
+                       part_k + o);
         }
         __syncthreads();
     }
@@ -339,7 +302,7 @@ __global__ void __launch_bounds__(256) k_rescore(DevDB db, DevMods mods, const f
                                                  const uint64_t *__restrict__ kept_k, int32_t K, int32_t topn,
                                                  float *__restrict__ out_s, uint64_t *__restrict__ out_k,
                                                  uint32_t *__restrict__ out_pep) {
-    extern __shared__ __align__(16) uint8_t smem[];
+    extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int32_t s = blockIdx.x;
     const SpecMeta m = meta[s];
@@ -448,9 +411,7 @@ __global__ void k_ncand(const uint32_t *__restrict__ wb, const uint32_t *__restr
 using namespace hfx;
 
 size_t hfx_batched_smem(int64_t stride, int elem_bytes, int G, int nw, int K) {
-    const int32_t words = (int32_t)((stride + 31) / 32);
-    const size_t tile = ((size_t)stride * G * elem_bytes + 15) & ~(size_t)15;
-    return 128 + tile + batched_cta_bytes(G, K) + (size_t)nw * batched_warp_bytes(words);
+    return fused_smem_bytes(stride, elem_bytes, G, nw, K, 4);
 }
 
 int hfx_batched_plan(const SpecMeta *meta, int32_t nspec, const uint32_t *wb, const uint32_t *we, int32_t G,
@@ -480,13 +441,8 @@ static int launch_batched_t(const DevDB &db, const T *rows, int64_t stride, cons
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    const int32_t words = (int32_t)((stride + 31) / 32);
-    if (nw <= 0) {
-        const size_t fixed = hfx_batched_smem(stride, sizeof(T), G, 0, K);
-        const size_t per = batched_warp_bytes(words);
-        nw = (int)std::min<size_t>(24, fixed < (size_t)smem_max ? ((size_t)smem_max - fixed) / per : 0);
-        if (nw < 1) return (int)cudaErrorInvalidValue;
-    }
+    if (nw <= 0) nw = fused_warps(stride, sizeof(T), G, K, 4, (size_t)smem_max);
+    if (nw < 1) return (int)cudaErrorInvalidValue;
     const size_t smem = hfx_batched_smem(stride, sizeof(T), G, nw, K);
     auto fn = k_score_batched<F, T, G>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

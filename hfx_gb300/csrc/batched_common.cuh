@@ -84,6 +84,30 @@ __device__ __forceinline__ float smem_topk_insert(float *ks, uint64_t *kk, float
     return __shfl_sync(kFullMask, out, K - 1);
 }
 
+// Shared-memory layout of the fused scorers (unmodified and modified): an
+// mbarrier, the group tile -- which after an item holds the warps'
+// surviving top-K entries -- and per warp three bit planes and a list.
+__host__ __device__ __forceinline__ size_t fused_warp_bytes(int32_t words) {
+    return ((size_t)3 * words * 4 + (size_t)kListCap * 2 + 15) & ~(size_t)15;
+}
+__host__ __device__ __forceinline__ size_t fused_region_bytes(int64_t stride, int elem_bytes, int G, int nw, int K,
+                                                              int key_bytes) {
+    const size_t tile = ((size_t)stride * G * elem_bytes + 15) & ~(size_t)15;
+    const size_t surv = ((size_t)G * nw * K * (4 + key_bytes) + 15) & ~(size_t)15;
+    return tile > surv ? tile : surv;
+}
+__host__ __device__ __forceinline__ size_t fused_smem_bytes(int64_t stride, int elem_bytes, int G, int nw, int K,
+                                                            int key_bytes) {
+    return 128 + fused_region_bytes(stride, elem_bytes, G, nw, K, key_bytes) +
+           (size_t)nw * fused_warp_bytes((int32_t)((stride + 31) / 32));
+}
+// Largest warp count (<= 24) whose layout fits in smem_max bytes, 0 if none.
+inline int fused_warps(int64_t stride, int elem_bytes, int G, int K, int key_bytes, size_t smem_max) {
+    for (int nw = 24; nw >= 1; --nw)
+        if (fused_smem_bytes(stride, elem_bytes, G, nw, K, key_bytes) <= smem_max) return nw;
+    return 0;
+}
+
 // Order-preserving map of a float score to uint32 (for atomicMax thresholds).
 __device__ __forceinline__ uint32_t score_order(float s) {
     const uint32_t b = __float_as_uint(s);
@@ -98,22 +122,23 @@ template <int G> __host__ __device__ constexpr int slot_lane(int j) { return j *
 // best K-th score any warp of the CTA has reached, a lower bound of the
 // CTA's K-th -- filters the offers, so warps share what they learn without
 // locks; the CTA's top-K is the top-K of the union of the warps' lists.
-template <int G>
+template <int G, typename Key = uint32_t>
 struct WarpSlots {
+    static constexpr Key kNone = ~Key(0);
     float s[G];
-    uint32_t k[G];
+    Key k[G];
 
     __device__ __forceinline__ void init() {
 #pragma unroll
         for (int j = 0; j < G; ++j) {
             s[j] = -INFINITY;
-            k[j] = 0xFFFFFFFFu;
+            k[j] = kNone;
         }
     }
 
     // Offer candidate `key`: slot j's score sits in lane slot_lane<G>(j) of
     // sc; ins has that lane's bit set when slot j takes the offer.
-    __device__ __forceinline__ void offer(float sc, uint32_t key, uint32_t ins, int K, uint32_t *thr_u) {
+    __device__ __forceinline__ void offer(float sc, Key key, uint32_t ins, int K, uint32_t *thr_u) {
         const int lane = threadIdx.x & 31;
 #pragma unroll
         for (int j = 0; j < G; ++j) {
@@ -122,7 +147,7 @@ struct WarpSlots {
                 const bool mb = lane < K && (s[j] > ns || (s[j] == ns && k[j] < key));
                 const int pos = __popc(__ballot_sync(kFullMask, mb));
                 const float us = __shfl_up_sync(kFullMask, s[j], 1);
-                const uint32_t uk = __shfl_up_sync(kFullMask, k[j], 1);
+                const Key uk = __shfl_up_sync(kFullMask, k[j], 1);
                 if (pos < K) {
                     if (lane == pos) {
                         s[j] = ns;
@@ -143,12 +168,12 @@ struct WarpSlots {
 
     // Item end, step 1: append the entries that can still be in the CTA's
     // top-K (score order >= the final threshold) to the slot's buffer.
-    __device__ __forceinline__ void flush(const uint32_t *thr_u, uint32_t *cnt, float *buf_s, uint32_t *buf_k,
-                                          int cap, int K) {
+    __device__ __forceinline__ void flush(const uint32_t *thr_u, uint32_t *cnt, float *buf_s, Key *buf_k, int cap,
+                                          int K) {
         const int lane = threadIdx.x & 31;
 #pragma unroll
         for (int j = 0; j < G; ++j) {
-            const bool keep = lane < K && k[j] != 0xFFFFFFFFu && score_order(s[j]) >= thr_u[j];
+            const bool keep = lane < K && k[j] != kNone && score_order(s[j]) >= thr_u[j];
             const uint32_t bal = __ballot_sync(kFullMask, keep);
             if (!bal) continue;
             uint32_t base = 0;
@@ -164,7 +189,8 @@ struct WarpSlots {
 };
 
 // Item end, step 2 (one warp per slot): the slot's top-K from its buffer.
-__device__ __forceinline__ void slot_merge(const float *bs, const uint32_t *bk, uint32_t n, int K, float *out_s,
+template <typename Key>
+__device__ __forceinline__ void slot_merge(const float *bs, const Key *bk, uint32_t n, int K, float *out_s,
                                            uint64_t *out_k) {
     const int lane = threadIdx.x & 31;
     WarpTopK tk;
@@ -172,7 +198,7 @@ __device__ __forceinline__ void slot_merge(const float *bs, const uint32_t *bk, 
     for (uint32_t b0 = 0; b0 < n; b0 += 32) {
         const uint32_t i = b0 + lane;
         const float es = i < n ? bs[i] : -INFINITY;
-        const uint32_t ek = i < n ? bk[i] : 0xFFFFFFFFu;
+        const Key ek = i < n ? bk[i] : ~Key(0);
         const uint32_t m = min(32u, n - b0);
         for (uint32_t t = 0; t < m; ++t)
             tk.insert(__shfl_sync(kFullMask, es, t), (uint64_t)__shfl_sync(kFullMask, ek, t), K);

@@ -52,6 +52,7 @@ enum : uint32_t {
     kErrTimeout = 2u,
     kErrKeyOverflow = 4u,
     kErrTooLong = 8u,
+    kErrBounds = 16u,
 };
 
 }  // namespace hfx

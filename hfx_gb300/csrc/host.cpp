@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <numeric>
@@ -109,9 +110,19 @@ struct hfx_ctx {
         if (!ev[s][0]) { cudaEventCreate(&ev[s][0]); cudaEventCreate(&ev[s][1]); }
         cudaEventRecord(ev[s][0], stream);
     }
+    // HFX_DEBUG_SYNC=1: synchronize after every stage and remember the first
+    // stage whose kernels reported an error (for locating device faults)
+    bool debug_sync = false;
+    std::string fault_stage;
     void stage_end(int s, int64_t launches, int64_t units = 0) {
         stage_launches[s] += launches;
         stage_units[s] += units;
+        if (debug_sync && fault_stage.empty()) {
+            static const char *names[HFX_NSTAGES] = {"layout", "preprocess", "windows", "score", "topn",
+                                                     "rescore", "mods", "lists", "pack"};
+            const cudaError_t e = cudaStreamSynchronize(stream);
+            if (e != cudaSuccess) fault_stage = names[s];
+        }
         if (!profile) return;
         cudaEventRecord(ev[s][1], stream);
         ev_pending[s] = true;
@@ -164,7 +175,9 @@ int32_t fail(hfx_ctx *c, int32_t code, const std::string &msg) {
 int32_t cuda_fail(hfx_ctx *c, cudaError_t e, const char *where) {
     if (e == cudaErrorMemoryAllocation)
         return fail(c, HFX_ERR_OOM, std::string(where) + ": " + cudaGetErrorString(e));
-    return fail(c, HFX_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+    std::string msg = std::string(where) + ": " + cudaGetErrorString(e);
+    if (c && !c->fault_stage.empty()) msg += " (first failing stage: " + c->fault_stage + ")";
+    return fail(c, HFX_ERR_CUDA, msg);
 }
 #define HFX_CUDA(call, where)                         \
     do {                                              \
@@ -640,6 +653,8 @@ int32_t hfx_ctx_create(int32_t device, hfx_ctx **out) {
         return HFX_ERR_CUDA;
     }
     c->own_stream = true;
+    const char *dbg = std::getenv("HFX_DEBUG_SYNC");
+    c->debug_sync = dbg && dbg[0] == '1';
     *out = c;
     return HFX_OK;
 }

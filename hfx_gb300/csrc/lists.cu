@@ -232,7 +232,8 @@ __global__ void __launch_bounds__(256) k_gen_lists(DevDB db, const int32_t *__re
 template <typename T, int G>
 __global__ void __launch_bounds__(1024, 1)
 k_score_lists(const uint16_t *__restrict__ lists, const uint32_t *__restrict__ lstart, uint64_t total10,
-              const uint16_t *__restrict__ list_len, uint32_t num_pep, const T *__restrict__ tiles, int64_t stride,
+              uint64_t list_total, const uint16_t *__restrict__ list_len, uint32_t num_pep,
+              const T *__restrict__ tiles, int64_t stride,
               const uint32_t *__restrict__ wb, const uint32_t *__restrict__ we, const int32_t *__restrict__ perm,
               const GroupInfo *__restrict__ groups, const uint32_t *__restrict__ item_off,
               const uint32_t *__restrict__ ngroups_p, int32_t chunk, int32_t K, uint32_t *__restrict__ counter,
@@ -258,7 +259,7 @@ k_score_lists(const uint16_t *__restrict__ lists, const uint32_t *__restrict__ l
     if (threadIdx.x < 3) s_stats[threadIdx.x] = 0ull;
     __syncthreads();
     const int my_slot = reduce_slot_of_lane<G>(lane);
-    unsigned long long my_cand = 0, my_entries = 0, my_psm = 0;
+    uint32_t my_cand = 0, my_entries = 0, my_psm = 0;
     uint32_t phase = 0;
     WarpSlots<G> slots;
     while (true) {
@@ -302,46 +303,84 @@ k_score_lists(const uint16_t *__restrict__ lists, const uint32_t *__restrict__ l
         const uint32_t my_b = lane < G ? s_wb[lane] : 0u, my_e = lane < G ? s_we[lane] : 0u;
         const int z = (int)gi.charges;
         const uint16_t *llen = list_len + (size_t)(z >= 1 ? z - 1 : 0) * num_pep;
-        while (true) {
-            uint32_t p = 0;
-            if (lane == 0) p = atomicAdd(&s_next, 1u);
-            p = __shfl_sync(kFullMask, p, 0);
-            if (p >= p1) break;
-            const uint32_t act = __ballot_sync(kFullMask, lane < G && my_b <= p && p < my_e) & ((1u << G) - 1u);
-            if (!act) continue;
+        // Software pipeline over the warp's candidates: the next active
+        // candidate is claimed and its list length, offset and first 128
+        // entries are loaded before the current one is scored.
+        struct Cand {
+            uint32_t p, act;
+            int n;
+            const uint16_t *lp;
+            uint32_t e[4];
+        };
+        auto next_active = [&]() {
+            Cand c;
+            c.act = 0u;
+            c.n = 0;
+            c.lp = lists;
+            while (true) {
+                uint32_t q = 0;
+                if (lane == 0) q = atomicAdd(&s_next, 1u);
+                c.p = __shfl_sync(kFullMask, q, 0);
+                if (c.p >= p1) break;
+                c.act = __ballot_sync(kFullMask, lane < G && my_b <= c.p && c.p < my_e) & ((1u << G) - 1u);
+                if (c.act) break;
+            }
+            if (c.p < p1 && z >= 1) {
+                c.n = llen[c.p];
+                const uint64_t off = list_offset(lstart, total10, z, c.p);
+                if (c.p >= num_pep || off + (uint64_t)c.n > list_total) {
+                    if (lane == 0) atomicOr(err, kErrBounds);
+                    c.n = 0;
+                } else {
+                    c.lp = lists + off;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int i = 32 * k + lane;
+                c.e[k] = i < c.n ? (uint32_t)__ldg(c.lp + i) : 0xFFFFFFFFu;
+            }
+            return c;
+        };
+        Cand cur = next_active();
+        while (cur.p < p1) {
+            const Cand nxt = next_active();
             float acc[G];
 #pragma unroll
             for (int j = 0; j < G; ++j) acc[j] = 0.0f;
-            if (z >= 1) {
-                const int n = llen[p];
-                const uint16_t *lp = lists + list_offset(lstart, total10, z, p);
-                my_cand += 1;
-                my_entries += (unsigned long long)n;
-                my_psm += (unsigned long long)__popc(act);
-                for (int i0 = 0; i0 < n; i0 += 128) {
-                    uint32_t e[4];
+            const int n = cur.n;
+            my_cand += 1u;
+            my_entries += (uint32_t)n;
+            my_psm += (uint32_t)__popc(cur.act);
+            uint32_t e[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) e[k] = cur.e[k];
+            for (int i0 = 0; i0 < n; i0 += 128) {
+                if (i0 > 0) {
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
                         const int i = i0 + 32 * k + lane;
-                        e[k] = i < n ? (uint32_t)__ldg(lp + i) : 0xFFFFFFFFu;
+                        e[k] = i < n ? (uint32_t)__ldg(cur.lp + i) : 0xFFFFFFFFu;
                     }
+                }
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const uint32_t bin = e[k] >> 2;
-                        if ((int32_t)bin < nb) {
-                            const float w = level_weight(e[k] & 3u);
-                            float x[G];
-                            TileLoad<T, G>::load(stile, bin, x);
+                for (int k = 0; k < 4; ++k) {
+                    const uint32_t bin = e[k] >> 2;
+                    if ((int32_t)bin < nb) {
+                        const float w = level_weight(e[k] & 3u);
+                        float x[G];
+                        TileLoad<T, G>::load(stile, bin, x);
 #pragma unroll
-                            for (int j = 0; j < G; ++j) acc[j] = __fmaf_rn(w, x[j], acc[j]);
-                        }
+                        for (int j = 0; j < G; ++j) acc[j] = __fmaf_rn(w, x[j], acc[j]);
                     }
                 }
             }
             const float sc = reduce_scatter<G>(acc);
-            const bool want = ((act >> my_slot) & 1u) && score_order(sc) >= *(volatile uint32_t *)(thr_u + my_slot);
+            const bool want =
+                ((cur.act >> my_slot) & 1u) && score_order(sc) >= *(volatile uint32_t *)(thr_u + my_slot);
             const uint32_t ins = __ballot_sync(kFullMask, want) & slot_owner_mask<G>();
-            if (ins) slots.offer(sc, p, ins, K, thr_u);
+            if (ins) slots.offer(sc, cur.p, ins, K, thr_u);
+            cur = nxt;
         }
         __syncthreads();  // every warp is done with the tile: its region takes the survivors
         slots.flush(thr_u, cnt, buf_s, buf_k, cap, K);
@@ -355,9 +394,9 @@ k_score_lists(const uint16_t *__restrict__ lists, const uint32_t *__restrict__ l
     }
     if (stats) {
         if (lane == 0) {
-            atomicAdd(&s_stats[0], my_cand);
-            atomicAdd(&s_stats[1], my_entries);
-            atomicAdd(&s_stats[2], my_psm);
+            atomicAdd(&s_stats[0], (unsigned long long)my_cand);
+            atomicAdd(&s_stats[1], (unsigned long long)my_entries);
+            atomicAdd(&s_stats[2], (unsigned long long)my_psm);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -432,7 +471,8 @@ static int launch_lists_t(const uint16_t *lists, const uint32_t *lstart, uint64_
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, nw * 32, smem);
     const int grid = sms * (per > 0 ? per : 1);
     cudaMemsetAsync(ws.counter, 0, 4, st);
-    fn<<<grid, nw * 32, smem, st>>>(lists, lstart, total10, list_len, num_pep, (const T *)tiles, stride, wb, we,
+    fn<<<grid, nw * 32, smem, st>>>(lists, lstart, total10, total10 * 10, list_len, num_pep, (const T *)tiles,
+                                    stride, wb, we,
                                     ws.perm, ws.groups, ws.item_off, ws.ngroups, chunk, K, ws.counter, part_s, part_k,
                                     stats, err);
     return (int)cudaGetLastError();

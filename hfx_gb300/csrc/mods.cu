@@ -86,24 +86,23 @@ k_score_mods(DevDB db, DevMods mods, const T *__restrict__ tiles, int64_t stride
              uint32_t *__restrict__ counter, float *__restrict__ part_s, uint64_t *__restrict__ part_k,
              unsigned long long *__restrict__ ncand, uint32_t *__restrict__ err) {
     extern __shared__ __align__(128) uint8_t smem[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int32_t words_cap = (int32_t)((stride + 31) / 32);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     T *stile = reinterpret_cast<T *>(smem + 128);
-    const size_t tile_bytes = ((size_t)stride * G * sizeof(T) + 15) & ~(size_t)15;
-    float *tk_s = reinterpret_cast<float *>(smem + 128 + tile_bytes);
-    uint64_t *tk_k = reinterpret_cast<uint64_t *>(tk_s + ((G * K + 1) & ~1));
-    float *thr = reinterpret_cast<float *>(tk_k + G * K);
-    uint32_t *locks = reinterpret_cast<uint32_t *>(thr + G);
-    const size_t cta_bytes = (((size_t)((G * K + 1) & ~1) * 4 + (size_t)G * K * 8 + (size_t)G * 8) + 15) & ~(size_t)15;
-    const size_t warp_bytes = ((size_t)3 * words_cap * 4 + (size_t)kListCap * 2 + 15) & ~(size_t)15;
-    uint8_t *wbase = smem + 128 + tile_bytes + cta_bytes + (size_t)warp * warp_bytes;
+    // after an item's isoforms the tile region holds the warps' survivors
+    const int cap = nw * K;
+    uint64_t *buf_k = reinterpret_cast<uint64_t *>(smem + 128);
+    float *buf_s = reinterpret_cast<float *>(buf_k + (size_t)G * cap);
+    uint8_t *wbase = smem + 128 + fused_region_bytes(stride, sizeof(T), G, nw, K, 8) +
+                     (size_t)warp * fused_warp_bytes(words_cap);
     uint32_t *planes = reinterpret_cast<uint32_t *>(wbase);
     uint16_t *list = reinterpret_cast<uint16_t *>(planes + 3 * words_cap);
     __shared__ int32_t s_item;
     __shared__ uint32_t s_next;
     __shared__ uint32_t s_wb[G], s_we[G];
     __shared__ int32_t s_spec[G];
+    __shared__ uint32_t thr_u[G], cnt[G];
 
     const uint32_t total = item_off[n_gm];
     if (threadIdx.x == 0) mbar_init(bar, 1);
@@ -118,6 +117,7 @@ k_score_mods(DevDB db, DevMods mods, const T *__restrict__ tiles, int64_t stride
     iso.per_type = mods.per_type;
 #pragma unroll
     for (int i = 0; i < kMaxMa; ++i) iso.ma_mass[i] = mods.ma_mass[i];
+    WarpSlots<G, uint64_t> slots;
 
     while (true) {
         if (threadIdx.x == 0) s_item = (int32_t)atomicAdd(counter, 1u);
@@ -129,12 +129,12 @@ k_score_mods(DevDB db, DevMods mods, const T *__restrict__ tiles, int64_t stride
         const GroupInfo gi = groups[g];
         const uint32_t p0 = mlo[gm] + (item - item_off[gm]) * (uint32_t)chunk;
         const uint32_t p1 = min(mhi[gm], p0 + (uint32_t)chunk);
-        const int cnt = (int)gi.count;
+        const int cnt_members = (int)gi.count;
         if (threadIdx.x < G) {
             const int j = threadIdx.x;
             uint32_t b = 0, e = 0;
             int32_t s = -1;
-            if (j < cnt) {
+            if (j < cnt_members) {
                 s = perm[gi.pos0 + j];
                 b = mb[(size_t)s * mods.num_mod + mu];
                 e = me[(size_t)s * mods.num_mod + mu];
@@ -142,15 +142,10 @@ k_score_mods(DevDB db, DevMods mods, const T *__restrict__ tiles, int64_t stride
             s_wb[j] = b;
             s_we[j] = e;
             s_spec[j] = s;
+            thr_u[j] = 0u;
+            cnt[j] = 0u;
         }
-        for (int i = threadIdx.x; i < G * K; i += blockDim.x) {
-            tk_s[i] = -INFINITY;
-            tk_k[i] = ~0ull;
-        }
-        if (threadIdx.x < G) {
-            thr[threadIdx.x] = -INFINITY;
-            locks[threadIdx.x] = 0u;
-        }
+        slots.init();
         if (threadIdx.x == 0) s_next = p0;
         const int32_t nb = tile_bins(gi.maxlen);
         if (threadIdx.x == 0) {
@@ -203,40 +198,19 @@ k_score_mods(DevDB db, DevMods mods, const T *__restrict__ tiles, int64_t stride
                 float acc[G];
                 planes_accumulate<G>(pl, list, wr, dot, acc);
                 const float sc = reduce_scatter<G>(acc);
-                const bool want = ((act >> my_slot) & 1u) && sc >= thr[my_slot];
-                uint32_t ins = __ballot_sync(kFullMask, want) & slot_owner_mask<G>();
-                const uint64_t key = mod_key(mu, p, rank);
-                while (ins) {
-                    const int src = __ffs(ins) - 1;
-                    ins &= ins - 1u;
-                    const int j = reduce_slot_of_lane<G>(src);
-                    const float s = __shfl_sync(kFullMask, sc, src);
-                    uint32_t ok = 1u;
-                    if (lane == 0) {
-                        uint32_t nn = 0;
-                        while (atomicCAS(&locks[j], 0u, 1u) != 0u) {
-                            if (++nn > kLockLimit) { ok = 0u; break; }
-                        }
-                    }
-                    ok = __shfl_sync(kFullMask, ok, 0);
-                    if (!ok) {
-                        if (lane == 0) atomicOr(err, kErrTimeout);
-                        continue;
-                    }
-                    __threadfence_block();
-                    const float t = smem_topk_insert(tk_s + j * K, tk_k + j * K, s, key, K);
-                    if (lane == 0) thr[j] = t;
-                    __threadfence_block();
-                    __syncwarp();
-                    if (lane == 0) atomicExch(&locks[j], 0u);
-                }
+                const bool want =
+                    ((act >> my_slot) & 1u) && score_order(sc) >= *(volatile uint32_t *)(thr_u + my_slot);
+                const uint32_t ins = __ballot_sync(kFullMask, want) & slot_owner_mask<G>();
+                if (ins) slots.offer(sc, mod_key(mu, p, rank), ins, K, thr_u);
             }
         }
+        __syncthreads();  // every warp is done with the tile: its region takes the survivors
+        slots.flush(thr_u, cnt, buf_s, buf_k, cap, K);
         __syncthreads();
-        for (int i = threadIdx.x; i < cnt * K; i += blockDim.x) {
-            const size_t o = (size_t)item * G * K + i;
-            part_s[o] = tk_s[i];
-            part_k[o] = tk_k[i];
+        for (int j = warp; j < cnt_members; j += nw) {
+            const size_t o = ((size_t)item * G + j) * K;
+            slot_merge(buf_s + (size_t)j * cap, buf_k + (size_t)j * cap, min(cnt[j], (uint32_t)cap), K, part_s + o,
+                       part_k + o);
         }
         __syncthreads();
     }
@@ -387,14 +361,9 @@ static int launch_mods_t(const DevDB &db, const DevMods &m, const void *tiles, i
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    const int32_t words = (int32_t)((stride + 31) / 32);
-    const size_t tile = ((size_t)stride * G * sizeof(T) + 15) & ~(size_t)15;
-    const size_t cta = (((size_t)((G * K + 1) & ~1) * 4 + (size_t)G * K * 8 + (size_t)G * 8) + 15) & ~(size_t)15;
-    const size_t per = ((size_t)3 * words * 4 + (size_t)kListCap * 2 + 15) & ~(size_t)15;
-    const size_t fixed = 128 + tile + cta;
-    const int nw = (int)std::min<size_t>(24, fixed < (size_t)smem_max ? ((size_t)smem_max - fixed) / per : 0);
+    const int nw = fused_warps(stride, sizeof(T), G, K, 8, (size_t)smem_max);
     if (nw < 1) return (int)cudaErrorInvalidValue;
-    const size_t smem = fixed + (size_t)nw * per;
+    const size_t smem = fused_smem_bytes(stride, sizeof(T), G, nw, K, 8);
     auto fn = k_score_mods<F, T, G>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
