@@ -60,8 +60,12 @@ def _args():
     ap.add_argument("--precision", type=int, default=1, help="0 fp32, 1 bf16+rescore, 2 fp16+rescore")
     ap.add_argument("--batch-mode", type=int, default=1,
                     help="0 per-spectrum launches, 1 batched over ion lists, 2 batched fused")
-    ap.add_argument("--cpu-sample", type=int, default=10000, help="spectra in the CPU baseline sample")
-    ap.add_argument("--agree-sample", type=int, default=1000, help="spectra checked against the FP64 oracle")
+    ap.add_argument("--cpu-sample", type=int, default=-1,
+                    help="spectra in the CPU baseline sample (-1: whole 'full' workload, 300 otherwise)")
+    ap.add_argument("--agree-sample", type=int, default=-1,
+                    help="spectra checked against the FP64 oracle (-1: 1000 for 'full', 200 otherwise)")
+    ap.add_argument("--plain-sample", type=int, default=-1,
+                    help="spectra timed on the plain FP32 path (-1: all for 'full', 2000 otherwise)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and the FP64 agreement")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison")
     ap.add_argument("--e2e-steps", type=int, default=3)
@@ -76,6 +80,24 @@ def _dist():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+DESCRIBE = {
+    "tiny": "2000 proteins, {n} spectra, +-3 Da, 1.0005 Da bins, top-10",
+    "full": "20000 proteins, {n} spectra, +-3 Da, 1.0005 Da bins, top-10",
+    "mods": "20000 proteins, {n} spectra, +-3 Da, 1.0005 Da bins, top-10, variable M+15.995 S/T/Y+79.966 up to 3",
+    "batch": "20000 proteins, {n} spectra, 80% +-10 ppm / 20% +-500 Da, 1.0005 Da bins, top-10",
+    "highres": "20000 proteins, {n} spectra, 80% +-10 ppm / 20% +-500 Da, 0.02 Da bins, top-10",
+}
+
+
+def _samples(a):
+    """Workload-dependent default sample sizes of the CPU-side arms."""
+    full = a.workload in ("full", "tiny")
+    cpu = a.cpu_sample if a.cpu_sample >= 0 else (10000 if full else 300)
+    agree = a.agree_sample if a.agree_sample >= 0 else (1000 if full else 200)
+    plain = a.plain_sample if a.plain_sample >= 0 else (1 << 30 if full else 2000)
+    return cpu, agree, plain
 
 
 def _workload(name, n, rank):
@@ -173,6 +195,11 @@ def _bytes_per_psm(eng, rows_dtype_bytes, wb, we, lens, charges, idx_tc_tn, rng,
     return float(np.mean(U * rows_dtype_bytes + L + 16)), float(U.mean())
 
 
+def _okw(cfg):
+    """Oracle search settings of a workload."""
+    return dict(bw=cfg["bin_width"], custom_bw=bool(cfg.get("custom_bin_width", 0)), ppm=cfg.get("tol_ppm", 0))
+
+
 def _oracle_inputs(prot, cfg):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
@@ -194,14 +221,15 @@ def run_reference(a, rank, world):
         return
     prot, sp, cfg = _workload(a.workload, a.spectra, 0)
     O, db, mods = _oracle_inputs(prot, cfg)
-    sample = sp.subset(np.arange(min(len(sp), max(50, a.cpu_sample // 4))))
+    cpu_n, _, _ = _samples(a)
+    sample = sp.subset(np.arange(min(len(sp), max(50, cpu_n // 4))))
     threads = os.cpu_count() or 1
     for _ in range(max(1, min(a.warmup, 1))):
-        O.search(*db, sample.subset(np.arange(min(20, len(sample)))), topn=cfg["top_n"], nthreads=threads, **mods)
+        O.search(*db, sample.subset(np.arange(min(20, len(sample)))), topn=cfg["top_n"], nthreads=threads, **_okw(cfg), **mods)
     t0 = time.perf_counter()
     psm = 0
     for _ in range(a.steps):
-        res = O.search(*db, sample, topn=cfg["top_n"], nthreads=threads, **mods)
+        res = O.search(*db, sample, topn=cfg["top_n"], nthreads=threads, **_okw(cfg), **mods)
         psm += int(res[4].sum())
     dt = time.perf_counter() - t0
     v = psm / dt
@@ -220,7 +248,7 @@ def _cpu_baseline(a, O, db, mods, sp, cfg):
     sample = sp.subset(np.arange(min(len(sp), a.cpu_sample)))
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
-    res = O.search(*db, sample, topn=cfg["top_n"], nthreads=threads, **mods)
+    res = O.search(*db, sample, topn=cfg["top_n"], nthreads=threads, **_okw(cfg), **mods)
     dt = time.perf_counter() - t0
     return {"value": float(res[4].sum()) / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"first {len(sample)} of {len(sp)} spectra, {int(res[4].sum())} pairs, {dt:.1f} s"}
@@ -233,7 +261,7 @@ def _agreement(a, O, db, mods, sp, cfg, key, score):
     n = min(len(sp), a.agree_sample)
     sample = sp.subset(np.arange(n))
     threads = os.cpu_count() or 1
-    _, s64, k64, _, _ = O.search(*db, sample, topn=cfg["top_n"], prec=3, nthreads=threads, **mods)
+    _, s64, k64, _, _ = O.search(*db, sample, topn=cfg["top_n"], prec=3, nthreads=threads, **_okw(cfg), **mods)
     same_order = np.all(k64 == key[:n], axis=1)
     same_set = np.array([set(k64[i]) == set(key[i]) for i in range(n)])
     ok = (k64 != np.iinfo(np.uint64).max) & (k64 == key[:n])
@@ -280,8 +308,11 @@ def main():
     stream = torch.cuda.current_stream()
     eng.set_stream(stream.cuda_stream)
     prec, mode = a.precision, a.batch_mode
+    cpu_n, agree_n, plain_n = _samples(a)
+    a.cpu_sample, a.agree_sample = cpu_n, agree_n
     p = hfx_gb300.default_params(top_n=cfg["top_n"], bin_width=cfg["bin_width"], precision=prec, batch_mode=mode,
-                                 rescore_k=32 if prec else 0, group_size=a.group_size, chunk=a.chunk)
+                                 rescore_k=32 if prec else 0, group_size=a.group_size, chunk=a.chunk,
+                                 tol_ppm=cfg.get("tol_ppm", 0), custom_bin_width=cfg.get("custom_bin_width", 0))
     d = torch.device("cuda", local)
     dev = dict(mz=torch.from_numpy(sp.mz).to(d), it=torch.from_numpy(sp.it).to(d),
                off=torch.from_numpy(sp.off).to(d), pcr=torch.from_numpy(sp.pcr).to(d),
@@ -344,18 +375,29 @@ def main():
     # the plain FP32 path (one launch per spectrum) on the same spectra
     plain = None
     if not a.no_plain and not has_mods:
-        p0 = hfx_gb300.default_params(top_n=tn_, bin_width=cfg["bin_width"], precision=0, batch_mode=0)
-        out0 = outputs()
-        eng.search_device(dev, p0, out0)
+        p0 = hfx_gb300.default_params(top_n=tn_, bin_width=cfg["bin_width"], precision=0, batch_mode=0,
+                                      tol_ppm=cfg.get("tol_ppm", 0), custom_bin_width=cfg.get("custom_bin_width", 0))
+        n_pl = min(ns, plain_n)
+        sub = sp if n_pl == ns else sp.subset(np.arange(n_pl))
+        dev0 = dev if n_pl == ns else dict(mz=torch.from_numpy(sub.mz).to(d), it=torch.from_numpy(sub.it).to(d),
+                                           off=torch.from_numpy(sub.off).to(d), pcr=torch.from_numpy(sub.pcr).to(d),
+                                           z=torch.from_numpy(sub.z).to(d), tol=torch.from_numpy(sub.tol).to(d))
+        out0 = dict(score=torch.empty((n_pl, tn_), dtype=torch.float32, device=d),
+                    key=torch.empty((n_pl, tn_), dtype=torch.int64, device=d),
+                    pep=torch.empty((n_pl, tn_), dtype=torch.int32, device=d),
+                    ncand=torch.empty(n_pl, dtype=torch.int64, device=d))
+        eng.search_device(dev0, p0, out0)
         torch.cuda.synchronize()
+        psm0 = int(out0["ncand"].sum().item())
         n0 = max(1, min(3, a.steps))
-        ms0 = _timed(eng, dev, p0, out0, n0, flush, stream) / n0
+        ms0 = _timed(eng, dev0, p0, out0, n0, flush, stream) / n0
         k0 = out0["key"].cpu().numpy().view(np.uint64)
         s0 = out0["score"].cpu().numpy()
-        plain = {"value": psm_step / (ms0 / 1000.0), "unit": UNIT, "ms_per_step": ms0,
-                 "speedup": (psm_step / (ms_step / 1000.0)) / (psm_step / (ms0 / 1000.0)),
-                 "top_agreement": float(np.mean(np.all(k0 == key, axis=1))),
-                 "scores_bitexact": bool(np.array_equal(s0.view(np.uint32), score.view(np.uint32)))}
+        v0 = psm0 / (ms0 / 1000.0)
+        plain = {"value": v0, "unit": UNIT, "ms_per_step": ms0, "spectra": n_pl, "pairs": psm0,
+                 "speedup": (psm_step / (ms_step / 1000.0)) / v0,
+                 "top_agreement": float(np.mean(np.all(k0 == key[:n_pl], axis=1))),
+                 "scores_bitexact": bool(np.array_equal(s0.view(np.uint32), score[:n_pl].view(np.uint32)))}
     # roofline of the dominant kernel
     stage = "mods" if has_mods and stats["mods"][0] > stats["score"][0] else "score"
     kern = "k_score_mods" if stage == "mods" else KERNELS[mode if mode in KERNELS else 1]
@@ -394,8 +436,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"{a.workload}: 20000 proteins, {ns} spectra, +-3 Da, 1.0005 Da bins, top-{tn_}"
-                               + (", variable M+15.995 S/T/Y+79.966 up to 3" if has_mods else ""),
+        "config": {"workload": f"{a.workload}: " + DESCRIBE.get(a.workload, "{n} spectra").format(n=ns),
                    "psm_per_step": psm_step,
                    "precision": ["fp32", "bf16 store + fp32 rescore", "fp16 store + fp32 rescore"][prec],
                    "batch_mode": ["per-spectrum launches", "batched over ion lists", "batched fused"][mode],

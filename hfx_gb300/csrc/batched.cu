@@ -151,8 +151,10 @@ __global__ void k_groups(const uint32_t *__restrict__ bucket_off, const uint32_t
     if (gi.hi <= gi.lo) {
         gi.lo = gi.hi = 0;
     }
+    // wide windows (open search) are cut into at most ~16 items per group
+    gi.chunk = group_chunk(gi.hi - gi.lo, chunk);
     groups[g] = gi;
-    nchunks[g] = (gi.hi - gi.lo + (uint32_t)chunk - 1) / (uint32_t)chunk;
+    nchunks[g] = (gi.hi - gi.lo + gi.chunk - 1) / gi.chunk;
 }
 
 template <bool FastDiv, typename T, int G>
@@ -198,8 +200,8 @@ k_score_batched(DevDB db, const T *__restrict__ tiles, int64_t stride, const uin
         if (item >= total) break;
         const int32_t g = find_group(item_off, ngroups, item);
         const GroupInfo gi = groups[g];
-        const uint32_t p0 = gi.lo + (item - item_off[g]) * (uint32_t)chunk;
-        const uint32_t p1 = min(gi.hi, p0 + (uint32_t)chunk);
+        const uint32_t p0 = gi.lo + (item - item_off[g]) * gi.chunk;
+        const uint32_t p1 = min(gi.hi, p0 + gi.chunk);
         const int cnt_members = (int)gi.count;
         if (threadIdx.x < G) {
             const int j = threadIdx.x;

@@ -9,6 +9,7 @@ struct GroupInfo {
     int32_t maxlen;        // longest member row
     int32_t charges;       // ion charges shared by the members (unmodified)
     int32_t charges_mod;   // ion charges of the members' modified candidates
+    uint32_t chunk;        // candidates per work item of this group
 };
 
 struct BatchedWs {

@@ -10,6 +10,15 @@ namespace hfx {
 constexpr uint32_t kWaitLimit = 1u << 24;  // mbarrier polls before reporting a timeout
 constexpr uint32_t kLockLimit = 1u << 20;  // lock attempts before reporting a timeout
 
+// Candidates per work item for a union window of `width` candidates: the
+// requested chunk, or width/16 when that is larger (open-search windows of
+// 10^5-10^6 candidates would otherwise need 10^5+ items per group).
+__host__ __device__ __forceinline__ uint32_t group_chunk(uint32_t width, int32_t chunk) {
+    const uint32_t c = (uint32_t)(chunk > 0 ? chunk : 1);
+    const uint32_t w = (width + 15u) / 16u;
+    return w > c ? w : c;
+}
+
 // Bins of a group tile that the scorer copies (a multiple of 8 keeps every
 // bulk copy a multiple of 16 bytes).
 __host__ __device__ __forceinline__ int32_t tile_bins(int32_t maxlen) { return (maxlen + 7) & ~7; }

@@ -15,7 +15,7 @@ struct LayoutParams {
     float bw;           // spectrum bin width (Correlation.hs:29-30)
     int32_t custom_bw;  // 1: custom width, the length formula divides the cutoff
     int32_t remove_pcr; // remove-precursor-peak (Correlation.hs:69-71)
-    int32_t ppm;        // tolerances in ppm (new; the reference has Da only)
+    int32_t ppm;        // 0 Da, 1 ppm, 2 per spectrum: negative = ppm (new; the reference has Da only)
     int32_t max_len;    // longest row accepted
 };
 

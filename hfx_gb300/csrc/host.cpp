@@ -524,6 +524,8 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
         if (e) return cuda_fail(ctx, e, "alloc");
         uint32_t *mhi = ctx->buf<uint32_t>("m_hi", (size_t)n_gm + 1, e);
         if (e) return cuda_fail(ctx, e, "alloc");
+        uint32_t *mch = ctx->buf<uint32_t>("m_chunk", (size_t)n_gm + 1, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
         int32_t *nch = ctx->buf<int32_t>("m_nchunks", (size_t)n_gm + 1, e);
         if (e) return cuda_fail(ctx, e, "alloc");
         mitem_off = ctx->buf<uint32_t>("m_itemoff", (size_t)n_gm + 2, e);
@@ -535,7 +537,8 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
         HFX_CUDA(cudaMemsetAsync(ncm, 0, 8ull * ns, ctx->stream), "memset");
         ctx->stage_begin(HFX_STAGE_MODS);
         rc = hfx_mods_windows(ctx->d_r.as<float>(), (uint32_t)ctx->num_pep, meta, ns, dm, mb, me, ctx->stream);
-        if (!rc) rc = hfx_mods_plan(ws, ngroups, mb, me, nm, chunk, mlo, mhi, nch, mitem_off, partial, ctx->stream);
+        if (!rc) rc = hfx_mods_plan(ws, ngroups, mb, me, nm, chunk, mlo, mhi, mch, nch, mitem_off, partial,
+                                    ctx->stream);
         if (rc) return cuda_fail(ctx, (cudaError_t)rc, "modification plan");
         uint32_t mtotal = 0;
         if (n_gm > 0) {
@@ -547,7 +550,7 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
         mk = ctx->buf<uint64_t>("m_part_k", (size_t)mtotal * G * K + 1, e);
         if (e) return cuda_fail(ctx, e, "alloc mod parts");
         if (mtotal > 0) {
-            rc = hfx_mods_score(db, dm, tiles, elem_kind, stride, mb, me, ws, mlo, mhi, mitem_off, n_gm, G, chunk, K,
+            rc = hfx_mods_score(db, dm, tiles, elem_kind, stride, mb, me, ws, mlo, mhi, mch, mitem_off, n_gm, G, K,
                                 p->fastdiv, ms, mk, ncm, ctx->d_err.as<uint32_t>(), ctx->stream);
             if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_mods");
         }

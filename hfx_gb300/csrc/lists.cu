@@ -269,8 +269,8 @@ k_score_lists(const uint16_t *__restrict__ lists, const uint32_t *__restrict__ l
         if (item >= total) break;
         const int32_t g = find_group(item_off, ngroups, item);
         const GroupInfo gi = groups[g];
-        const uint32_t p0 = gi.lo + (item - item_off[g]) * (uint32_t)chunk;
-        const uint32_t p1 = min(gi.hi, p0 + (uint32_t)chunk);
+        const uint32_t p0 = gi.lo + (item - item_off[g]) * gi.chunk;
+        const uint32_t p1 = min(gi.hi, p0 + gi.chunk);
         const int cnt_members = (int)gi.count;
         if (threadIdx.x < G) {
             const int j = threadIdx.x;

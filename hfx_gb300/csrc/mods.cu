@@ -54,7 +54,8 @@ __global__ void k_mod_windows(const float *__restrict__ r_sorted, uint32_t n, co
 __global__ void k_mod_groups(const GroupInfo *__restrict__ groups, const uint32_t *__restrict__ ngroups_p,
                              const int32_t *__restrict__ perm, const uint32_t *__restrict__ mb,
                              const uint32_t *__restrict__ me, int32_t num_mod, int32_t chunk, int32_t max_gm,
-                             uint32_t *__restrict__ mlo, uint32_t *__restrict__ mhi, int32_t *__restrict__ nchunks) {
+                             uint32_t *__restrict__ mlo, uint32_t *__restrict__ mhi, uint32_t *__restrict__ mchunk,
+                             int32_t *__restrict__ nchunks) {
     const int32_t gm = blockIdx.x * blockDim.x + threadIdx.x;
     if (gm >= max_gm) return;
     const uint32_t ng = *ngroups_p;
@@ -72,9 +73,11 @@ __global__ void k_mod_groups(const GroupInfo *__restrict__ groups, const uint32_
         }
     }
     if (hi <= lo) lo = hi = 0u;
+    const uint32_t c = group_chunk(hi - lo, chunk);
     mlo[gm] = lo;
     mhi[gm] = hi;
-    nchunks[gm] = (int32_t)((hi - lo + (uint32_t)chunk - 1) / (uint32_t)chunk);
+    mchunk[gm] = c;
+    nchunks[gm] = (int32_t)((hi - lo + c - 1) / c);
 }
 
 template <bool FastDiv, typename T, int G>
@@ -82,7 +85,7 @@ __global__ void __launch_bounds__(768, 1)
 k_score_mods(DevDB db, DevMods mods, const T *__restrict__ tiles, int64_t stride, const uint32_t *__restrict__ mb,
              const uint32_t *__restrict__ me, const int32_t *__restrict__ perm,
              const GroupInfo *__restrict__ groups, const uint32_t *__restrict__ mlo, const uint32_t *__restrict__ mhi,
-             const uint32_t *__restrict__ item_off, int32_t n_gm, int32_t chunk, int32_t K,
+             const uint32_t *__restrict__ mchunk, const uint32_t *__restrict__ item_off, int32_t n_gm, int32_t K,
              uint32_t *__restrict__ counter, float *__restrict__ part_s, uint64_t *__restrict__ part_k,
              unsigned long long *__restrict__ ncand, uint32_t *__restrict__ err) {
     extern __shared__ __align__(128) uint8_t smem[];
@@ -127,8 +130,8 @@ k_score_mods(DevDB db, DevMods mods, const T *__restrict__ tiles, int64_t stride
         const int32_t gm = find_group(item_off, n_gm, item);
         const int32_t g = gm / mods.num_mod, mu = gm % mods.num_mod;
         const GroupInfo gi = groups[g];
-        const uint32_t p0 = mlo[gm] + (item - item_off[gm]) * (uint32_t)chunk;
-        const uint32_t p1 = min(mhi[gm], p0 + (uint32_t)chunk);
+        const uint32_t p0 = mlo[gm] + (item - item_off[gm]) * mchunk[gm];
+        const uint32_t p1 = min(mhi[gm], p0 + mchunk[gm]);
         const int cnt_members = (int)gi.count;
         if (threadIdx.x < G) {
             const int j = threadIdx.x;
@@ -342,12 +345,12 @@ int hfx_mods_windows(const float *r_sorted, uint32_t num_pep, const SpecMeta *me
 }
 
 int hfx_mods_plan(const BatchedWs &ws, uint32_t ngroups, const uint32_t *mb, const uint32_t *me, int32_t num_mod,
-                  int32_t chunk, uint32_t *mlo, uint32_t *mhi, int32_t *nchunks, uint32_t *item_off,
-                  int32_t *partial, cudaStream_t st) {
+                  int32_t chunk, uint32_t *mlo, uint32_t *mhi, uint32_t *mchunk, int32_t *nchunks,
+                  uint32_t *item_off, int32_t *partial, cudaStream_t st) {
     const int32_t n_gm = (int32_t)ngroups * num_mod;
     if (n_gm <= 0) return 0;
     k_mod_groups<<<(n_gm + 255) / 256, 256, 0, st>>>(ws.groups, ws.ngroups, ws.perm, mb, me, num_mod, chunk, n_gm,
-                                                     mlo, mhi, nchunks);
+                                                     mlo, mhi, mchunk, nchunks);
     cudaMemsetAsync(item_off, 0, sizeof(uint32_t), st);
     return hfx_scan_inclusive(nchunks, n_gm, (int32_t *)(item_off + 1), partial, st);
 }
@@ -355,7 +358,8 @@ int hfx_mods_plan(const BatchedWs &ws, uint32_t ngroups, const uint32_t *mb, con
 template <bool F, typename T, int G>
 static int launch_mods_t(const DevDB &db, const DevMods &m, const void *tiles, int64_t stride, const uint32_t *mb,
                          const uint32_t *me, const BatchedWs &ws, const uint32_t *mlo, const uint32_t *mhi,
-                         const uint32_t *item_off, int32_t n_gm, int32_t chunk, int32_t K, float *ps, uint64_t *pk,
+                         const uint32_t *mchunk, const uint32_t *item_off, int32_t n_gm, int32_t K, float *ps,
+                         uint64_t *pk,
                          unsigned long long *ncand, uint32_t *err, cudaStream_t st) {
     int dev = 0, sms = 0, smem_max = 0;
     cudaGetDevice(&dev);
@@ -371,18 +375,19 @@ static int launch_mods_t(const DevDB &db, const DevMods &m, const void *tiles, i
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, nw * 32, smem);
     cudaMemsetAsync(ws.counter, 0, 4, st);
     fn<<<sms * (occ > 0 ? occ : 1), nw * 32, smem, st>>>(db, m, (const T *)tiles, stride, mb, me, ws.perm, ws.groups,
-                                                         mlo, mhi, item_off, n_gm, chunk, K, ws.counter, ps, pk,
+                                                         mlo, mhi, mchunk, item_off, n_gm, K, ws.counter, ps, pk,
                                                          ncand, err);
     return (int)cudaGetLastError();
 }
 
 int hfx_mods_score(const DevDB &db, const DevMods &m, const void *tiles, int elem_kind, int64_t stride,
                    const uint32_t *mb, const uint32_t *me, const BatchedWs &ws, const uint32_t *mlo,
-                   const uint32_t *mhi, const uint32_t *item_off, int32_t n_gm, int32_t G, int32_t chunk, int32_t K,
-                   int fastdiv, float *ps, uint64_t *pk, unsigned long long *ncand, uint32_t *err, cudaStream_t st) {
+                   const uint32_t *mhi, const uint32_t *mchunk, const uint32_t *item_off, int32_t n_gm, int32_t G,
+                   int32_t K, int fastdiv, float *ps, uint64_t *pk, unsigned long long *ncand, uint32_t *err,
+                   cudaStream_t st) {
     if (n_gm <= 0) return 0;
-#define HFX_M(F, T, GG)                                                                                              \
-    return launch_mods_t<F, T, GG>(db, m, tiles, stride, mb, me, ws, mlo, mhi, item_off, n_gm, chunk, K, ps, pk, \
+#define HFX_M(F, T, GG)                                                                                            \
+    return launch_mods_t<F, T, GG>(db, m, tiles, stride, mb, me, ws, mlo, mhi, mchunk, item_off, n_gm, K, ps, pk, \
                                    ncand, err, st)
 #define HFX_MG(F, T)              \
     do {                          \

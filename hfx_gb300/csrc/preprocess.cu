@@ -56,7 +56,10 @@ __global__ void k_layout(const float *__restrict__ mz, const int64_t *__restrict
     // Spectrum/Data.hs:58-59 ms2Mass with host constants
     m.mass = __fsub_rn(__fsub_rn(__fmul_rn(ps, zs), __fmul_rn(__fsub_rn(zs, 1.0f), kHostH)),
                        __fadd_rn(kHostH, kHostH2O));
-    const float eps = lp.ppm ? __fmul_rn(m.mass, __fmul_rn(tol[s], 1e-6f)) : tol[s];
+    // tolerance unit: Da (filter.cu:105), ppm, or per spectrum (negative = ppm)
+    const float ts = tol[s];
+    const bool in_ppm = lp.ppm == 1 || (lp.ppm == 2 && ts < 0.0f);
+    const float eps = in_ppm ? __fmul_rn(m.mass, __fmul_rn(lp.ppm == 2 ? -ts : ts, 1e-6f)) : ts;
     m.eps = eps;
     m.lo = __fsub_rn(m.mass, eps);  // filter.cu:103-115 (m - eps), (m + eps)
     m.hi = __fadd_rn(m.mass, eps);

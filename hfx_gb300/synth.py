@@ -127,7 +127,8 @@ def spectra(prot: Proteins, n: int, seed: int, charge_p: dict, npeaks=(None, Non
 
     npeaks=(lo, hi): total peaks per spectrum drawn U[lo, hi] (noise fills the
     rest); (None, None) uses n_noise noise peaks.  ppm_frac of the spectra
-    get a +-ppm_tol ppm window, the rest a Da window (open_tol if ppm_frac>0,
+    get a +-ppm_tol ppm window, stored as -ppm_tol (the per-spectrum unit
+    convention, tol_ppm = 2), the rest a Da window (open_tol if ppm_frac>0,
     else tol_da).
     """
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -175,7 +176,7 @@ def spectra(prot: Proteins, n: int, seed: int, charge_p: dict, npeaks=(None, Non
         its.append(allit[o].astype(np.float32))
         off.append(off[-1] + len(o))
         if ppm_frac > 0.0:
-            tol[i] = ppm_tol if rng.random() < ppm_frac else open_tol
+            tol[i] = -ppm_tol if rng.random() < ppm_frac else open_tol
         else:
             tol[i] = tol_da
         src.append(seqb.decode())
@@ -219,5 +220,5 @@ def workload(name: str, n_spectra: int | None = None):
         sp = spectra(prot, n_spectra or 100000, seed=103, charge_p={1: 0.05, 2: 0.5, 3: 0.35, 4: 0.10},
                      npeaks=(50, 400), ppm_frac=0.8)
         bw = 0.02 if name == "highres" else 1.0005079
-        return prot, sp, dict(bin_width=bw, top_n=10)
+        return prot, sp, dict(bin_width=bw, top_n=10, tol_ppm=2, custom_bin_width=int(name == "highres"))
     raise KeyError(name)

@@ -35,7 +35,8 @@ typedef struct hfx_search_params {
     float bin_width;               /* Correlation.hs:29-30: 1.0005079 mono, 1.0011413 average */
     int32_t custom_bin_width;      /* 1: bin_width is a custom width (e.g. 0.02 Da)           */
     int32_t remove_precursor_peak; /* remove-precursor-peak (Config.hs:312-317)               */
-    int32_t tol_ppm;               /* 0: mass-tolerance in Da (Config.hs:308); 1: ppm          */
+    int32_t tol_ppm;               /* 0: mass-tolerance in Da (Config.hs:308); 1: ppm; 2: per
+                                      spectrum, tol < 0 is |tol| ppm, tol >= 0 is Da           */
     int32_t top_n;                 /* matches kept per spectrum, 1..32                         */
     int32_t precision;             /* 0 FP32 rows; 1 BF16 rows + FP32 rescore; 2 FP16 + rescore */
     int32_t rescore_k;             /* candidates rescored in FP32 (>= top_n, <= 32)            */

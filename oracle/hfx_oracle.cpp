@@ -641,7 +641,9 @@ int32_t hfxo_search(const uint8_t *ions, const float *mt, const float *r,
                 for (int32_t i = 0; i < len; ++i)
                     xs[i] = p->prec == 1 ? to_bf16(x32[i]) : p->prec == 2 ? to_fp16(x32[i]) : x32[i];
                 const float mass = hfxo_ms2_mass(pcr[s], z[s]);
-                const float eps = p->ppm ? mass * (tol[s] * ppm_scale) : tol[s];
+                const float ts = tol[s];
+                const bool in_ppm = p->ppm == 1 || (p->ppm == 2 && ts < 0.0f);
+                const float eps = in_ppm ? mass * ((p->ppm == 2 ? -ts : ts) * ppm_scale) : ts;
                 const float lo = mass - eps, hi = mass + eps;
                 auto score_list = [&](int32_t n, Entry &e) {
                     e.s = hfxo_score32(bins.data(), lv.data(), n, xs.data());

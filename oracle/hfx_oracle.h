@@ -122,7 +122,7 @@ typedef struct {
     float bw;            /* spectrum bin width (Correlation.hs:29-30)          */
     int32_t custom_bw;   /* 1: bw is a custom width (len formula divides)      */
     int32_t remove_pcr;  /* remove-precursor-peak (Config.hs:63)               */
-    int32_t ppm;         /* tolerances are ppm (new; reference is Da only)     */
+    int32_t ppm;         /* 0 Da, 1 ppm, 2 per spectrum: negative = ppm (new) */
     int32_t topn;        /* entries kept per spectrum                          */
     int32_t prec;        /* see above                                          */
     int32_t num_ma;      /* variable modifications: 0 = none                   */

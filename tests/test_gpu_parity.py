@@ -219,3 +219,22 @@ def test_batched_tiny_and_edges(tiny_engine, oracle):
     for prec in (0, 1):
         res = eng.search(sp, hfx_gb300.default_params(top_n=10, batch_mode=1, precision=prec))
         _compare(res, ref, f"tiny batched prec={prec}")
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_mixed_tolerance_open_search(tiny_engine, oracle, mode):
+    """Per-spectrum tolerance units (tol_ppm = 2: negative = ppm): narrow
+    +-10 ppm windows next to open +-500 Da windows (10^4-10^5 candidates,
+    cut into wide work items), bit-exact against the oracle."""
+    import hfx_gb300
+    eng, prot, sp = tiny_engine
+    sub = sp.subset(np.arange(40))
+    sub.tol[:] = -10.0
+    sub.tol[::5] = 500.0
+    ref = oracle.search(*_oracle_db(oracle, eng, prot), sub, topn=10, ppm=2)
+    assert ref[4][::5].min() > 10000 and ref[4][1::5].max() < 1000
+    res = eng.search(sub, hfx_gb300.default_params(top_n=10, batch_mode=mode, tol_ppm=2))
+    _compare(res, ref, f"mixed tolerance mode={mode}")
+    if mode:
+        res = eng.search(sub, hfx_gb300.default_params(top_n=10, batch_mode=mode, tol_ppm=2, precision=1))
+        _compare(res, ref, f"mixed tolerance bf16 mode={mode}")
