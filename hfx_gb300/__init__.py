@@ -59,6 +59,7 @@ class SearchParams(C.Structure):
         ("group_size", C.c_int32),
         ("chunk", C.c_int32),
         ("max_len", C.c_int32),
+        ("ion_bins_custom", C.c_int32),
     ]
 
 

@@ -62,5 +62,5 @@ int hfx_launch_layout(const float *mz, const int64_t *off, const float *pcr, con
                       hfx::SpecMeta *meta, uint32_t *max_len, cudaStream_t st);
 int hfx_launch_preprocess(const float *mz, const float *it, const int64_t *off, const float *pcr,
                           const hfx::LayoutParams &lp, const hfx::SpecMeta *meta, int32_t nspec,
-                          int64_t stride, float *out32, __nv_bfloat16 *outbf, __half *outh,
+                          int64_t stride, float *out32, __nv_bfloat16 *outbf, __half *outh, uint32_t *err,
                           cudaStream_t st);

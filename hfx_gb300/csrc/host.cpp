@@ -262,6 +262,9 @@ void make_mod_table(hfx_ctx *ctx) {
     }
 }
 
+// Longest spectrum row accepted by default (0.02 Da bins over 0-5000 m/z).
+constexpr int32_t kDefaultMaxLen = 262144;
+
 struct Batch {
     const float *mz, *it, *pcr, *z, *tol;
     const int64_t *off;
@@ -283,7 +286,7 @@ LayoutParams layout_params(const hfx_search_params *p) {
     lp.custom_bw = p->custom_bin_width;
     lp.remove_pcr = p->remove_precursor_peak;
     lp.ppm = p->tol_ppm;
-    lp.max_len = p->max_len > 0 ? p->max_len : 8192;
+    lp.max_len = p->max_len > 0 ? p->max_len : kDefaultMaxLen;
     return lp;
 }
 
@@ -321,7 +324,7 @@ int32_t run_stage_a(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, in
     }
     ctx->stage_begin(HFX_STAGE_PREPROCESS);
     rc = hfx_launch_preprocess(b.mz, b.it, b.off, b.pcr, lp, meta, b.nspec, stride, rows, rows_bf, rows_h,
-                               ctx->stream);
+                               ctx->d_err.as<uint32_t>(), ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_preprocess");
     ctx->stage_end(HFX_STAGE_PREPROCESS, 1, b.nspec);
     return HFX_OK;
@@ -405,7 +408,14 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     if (G != 1 && G != 2 && G != 4 && G != 8) return fail(ctx, HFX_ERR_ARG, "group_size must be 1, 2, 4 or 8");
     const int32_t K = elem_kind == 0 ? p->top_n : std::max(p->top_n, std::min(p->rescore_k > 0 ? p->rescore_k : 32,
                                                                                kMaxTopK));
-    if (stride > (int64_t)kMaxWords * 32) return fail(ctx, HFX_ERR_UNSUPPORTED, "spectrum rows longer than 8192 bins");
+    // rows longer than the shared-memory bit planes: 32-bit sorted lists,
+    // tiles read from global memory, list-based rescoring; no fused or
+    // modification scoring
+    const bool long_rows = stride > (int64_t)kMaxWords * 32;
+    if (long_rows && p->search_mods && ctx->num_mod > 0)
+        return fail(ctx, HFX_ERR_UNSUPPORTED, "modification search on rows longer than 8192 bins");
+    if (p->ion_bins_custom && !long_rows)
+        return fail(ctx, HFX_ERR_UNSUPPORTED, "custom ion bin width needs rows longer than 8192 bins");
     uint32_t *wb = ctx->buf<uint32_t>("wb", ns, e);
     if (e) return cuda_fail(ctx, e, "alloc");
     uint32_t *we = ctx->buf<uint32_t>("we", ns, e);
@@ -452,13 +462,16 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     const DevDB db = ctx->devdb();
     const void *src_rows = elem_kind == 0 ? (const void *)rows : rows_lo;
     const bool plain_on = p->search_plain != 0;
+    const uint32_t *lists32 = nullptr;  // long rows: the lists the rescoring reads
+    const uint16_t *llen_out = nullptr;
+    uint64_t total10_out = 0;
     const bool mods_on = p->search_mods != 0 && ctx->num_mod > 0;
     ctx->stage_begin(HFX_STAGE_PACK);
     rc = hfx_pack_tiles(src_rows, elem_kind, stride, meta, ws, tiles, ngroups, G, ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_pack_tiles");
     ctx->stage_end(HFX_STAGE_PACK, ngroups > 0 ? 1 : 0, ngroups);
     if (!plain_on) {
-    } else if (p->batch_mode != 1) {
+    } else if (p->batch_mode != 1 && !long_rows) {
         // fused: every work item rebuilds its candidates' ion lists
         ctx->stage_begin(HFX_STAGE_SCORE);
         rc = hfx_batched_score(db, src_rows, elem_kind, stride, meta, wb, we, ws, tiles, ngroups, G, chunk, K, 0, 0,
@@ -478,8 +491,12 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
         if (e) return cuda_fail(ctx, e, "alloc");
         // static slots: 10 ions per prefix and charge, levels 1..4 (1+2+3+4)
         const uint64_t total10 = 10ull * ctx->ladder_residues;
-        uint16_t *lists = ctx->buf<uint16_t>("l_lists", total10 * 10 + 64, e);
+        void *lists = long_rows ? (void *)ctx->buf<uint32_t>("l_lists32", total10 * 10 + 64, e)
+                                : (void *)ctx->buf<uint16_t>("l_lists", total10 * 10 + 64, e);
         if (e) return cuda_fail(ctx, e, "alloc lists");
+        lists32 = long_rows ? (const uint32_t *)lists : nullptr;
+        llen_out = llen;
+        total10_out = total10;
         unsigned long long *stats = nullptr;
         if (ctx->profile) {
             stats = ctx->buf<unsigned long long>("l_stats", 8, e);
@@ -489,14 +506,20 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
         ctx->stage_begin(HFX_STAGE_LISTS);
         rc = hfx_lists_mark(meta, wb, we, ns, npep1, diff, ctx->stream);
         if (!rc) rc = hfx_scan_inclusive(diff, kLevels * npep1, cover, partial, ctx->stream);
-        if (!rc)
-            rc = hfx_lists_generate(db, cover, npep1, kMaxWords * 32, ctx->d_lstart.as<uint32_t>(), total10, lists,
-                                    llen, p->fastdiv, stats, ctx->d_err.as<uint32_t>(), ctx->stream);
+        if (!rc && long_rows)
+            rc = hfx_lists_generate_long(db, cover, npep1, (int32_t)stride, ctx->d_lstart.as<uint32_t>(), total10,
+                                         (uint32_t *)lists, llen, p->fastdiv,
+                                         p->ion_bins_custom ? p->bin_width : 0.0f, stats,
+                                         ctx->d_err.as<uint32_t>(), ctx->stream);
+        else if (!rc)
+            rc = hfx_lists_generate(db, cover, npep1, kMaxWords * 32, ctx->d_lstart.as<uint32_t>(), total10,
+                                    (uint16_t *)lists, llen, p->fastdiv, stats, ctx->d_err.as<uint32_t>(),
+                                    ctx->stream);
         if (rc) return cuda_fail(ctx, (cudaError_t)rc, "ion lists");
         ctx->stage_end(HFX_STAGE_LISTS, 5, 0);
         ctx->stage_begin(HFX_STAGE_SCORE);
-        rc = hfx_lists_score(lists, ctx->d_lstart.as<uint32_t>(), total10, llen, (uint32_t)ctx->num_pep, src_rows,
-                             elem_kind, stride, meta, wb, we, ws, tiles, ngroups, G, chunk, K, 0, ps, pk, stats,
+        rc = hfx_lists_score(lists, long_rows, ctx->d_lstart.as<uint32_t>(), total10, llen, (uint32_t)ctx->num_pep,
+                             elem_kind, stride, wb, we, ws, tiles, G, K, 0, ps, pk, stats,
                              ctx->d_err.as<uint32_t>(), ctx->stream);
         if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_lists");
         ctx->stage_end(HFX_STAGE_SCORE, 1, 0);
@@ -576,8 +599,13 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     } else {
         ctx->stage_end(HFX_STAGE_TOPN, 1, ns);
         ctx->stage_begin(HFX_STAGE_RESCORE);
-        rc = hfx_rescore(db, dm, rows, stride, meta, ks, kk, ns, K, p->top_n, p->fastdiv, out_s, out_k, out_pep,
-                         ctx->stream);
+        if (long_rows)
+            rc = hfx_rescore_lists(lists32, ctx->d_lstart.as<uint32_t>(), total10_out, llen_out,
+                                   (uint32_t)ctx->num_pep, ctx->d_idx.as<uint32_t>(), rows, stride, meta, kk, ns, K,
+                                   p->top_n, out_s, out_k, out_pep, ctx->d_err.as<uint32_t>(), ctx->stream);
+        else
+            rc = hfx_rescore(db, dm, rows, stride, meta, ks, kk, ns, K, p->top_n, p->fastdiv, out_s, out_k,
+                             out_pep, ctx->stream);
         if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_rescore");
         if (out_ncand) {
             rc = hfx_ncand(wb, we, meta, ns, plain_on, ncm, out_ncand, ctx->stream);
@@ -605,7 +633,8 @@ int32_t search_device(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, 
     if (rc) return rc;
     // the modified isoforms are scored by the batched engine only: with
     // modifications on, batch_mode 0 runs the fused batched path
-    if (p->batch_mode || (p->search_mods && ctx->num_mod > 0) || !p->search_plain)
+    if (p->batch_mode || (p->search_mods && ctx->num_mod > 0) || !p->search_plain ||
+        stride > (int64_t)kMaxWords * 32)
         rc = search_batched(ctx, p, b, meta, rows, p->precision == 1 ? (const void *)rows_bf : (const void *)rows_h,
                             p->precision, stride, out_s, out_k, out_pep, out_ncand);
     else if (p->precision != 0)
@@ -642,6 +671,7 @@ void hfx_default_params(hfx_search_params *p) {
     p->group_size = 0;
     p->chunk = 0;
     p->max_len = 0;
+    p->ion_bins_custom = 0;
 }
 
 int32_t hfx_ctx_create(int32_t device, hfx_ctx **out) {
@@ -945,8 +975,10 @@ int32_t hfx_preprocess(hfx_ctx *ctx, const hfx_search_params *p, const float *mz
     HFX_CUDA(cudaMemsetAsync(tol, 0, 4ull * nspec, ctx->stream), "memset");
     int rc = hfx_launch_layout(mz, off, pcr, z, tol, nspec, lp, meta, d_max, ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_layout");
+    HFX_CUDA(ctx->d_err.ensure(16), "alloc err");
+    HFX_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, 4, ctx->stream), "memset err");
     rc = hfx_launch_preprocess(mz, it, off, pcr, lp, meta, nspec, stride, rows, (__nv_bfloat16 *)rows_bf16,
-                               (__half *)rows_fp16, ctx->stream);
+                               (__half *)rows_fp16, ctx->d_err.as<uint32_t>(), ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_preprocess");
     std::vector<SpecMeta> hm(nspec);
     HFX_CUDA(cudaMemcpyAsync(hm.data(), meta, sizeof(SpecMeta) * nspec, cudaMemcpyDeviceToHost, ctx->stream), "D2H");

@@ -225,18 +225,242 @@ __global__ void __launch_bounds__(256) k_gen_lists(DevDB db, const int32_t *__re
     }
 }
 
+// ---- long rows: 32-bit list entries built by sorting ----
+//
+// With ~10^5 bins per row the three bit planes no longer fit in shared
+// memory.  Instead, for every needed (peptide, level z) the warp writes the
+// ten keys (bin << 2 | level) of every (prefix, charge 1..z) into a per-warp
+// buffer (ion_series.cu:78-123, the same arithmetic as emit_ions), sorts the
+// buffer, and keeps the last key of each bin, i.e. its highest level -- the
+// reference's atomicMax into the dense row (ion_series.cu:71-75).
+constexpr int kLongKeys = 4096;  // keys per warp: 32-prefix chunks x charges x 10
+
+// rint(mz / width): the mono width as in bin_of, or a custom ion width
+// (ibw > 0, the 0.02 Da switch) by IEEE division (__fdividef with FastDiv).
+template <bool FastDiv>
+__device__ __forceinline__ int32_t bin_w(float mz, float ibw) {
+    if (ibw > 0.0f) return sat_bin(rintf(FastDiv ? __fdividef(mz, ibw) : __fdiv_rn(mz, ibw)));
+    return bin_of<FastDiv>(mz);
+}
+
+template <bool FastDiv>
+__device__ __forceinline__ void emit_keys(float b, float y, const ChargeConst &k, int32_t nbins, float ibw,
+                                          uint32_t *out) {
+    auto key = [&](int32_t x, uint32_t lvl) -> uint32_t {
+        return (x >= 0 && x < nbins) ? (((uint32_t)x << 2) | lvl) : 0xFFFFFFFFu;
+    };
+    // A ion
+    out[0] = key(bin_w<FastDiv>(div_charge<FastDiv>(__fadd_rn(__fsub_rn(b, kCO), k.hc), k.c), ibw), 1u);
+    // B ions: x-1, x, x+1 at 25/50/25, and the water and ammonia losses at 10
+    float m = div_charge<FastDiv>(__fadd_rn(b, k.hc), k.c);
+    int32_t x = bin_w<FastDiv>(m, ibw);
+    out[1] = key(x - 1, 2u);
+    out[2] = key(x, 3u);
+    out[3] = key(x + 1, 2u);
+    out[4] = key(bin_w<FastDiv>(__fsub_rn(m, k.dh2o), ibw), 1u);
+    out[5] = key(bin_w<FastDiv>(__fsub_rn(m, k.dnh3), ibw), 1u);
+    // Y ions
+    m = div_charge<FastDiv>(__fadd_rn(__fadd_rn(y, kH2O), k.hc), k.c);
+    x = bin_w<FastDiv>(m, ibw);
+    out[6] = key(x - 1, 2u);
+    out[7] = key(x, 3u);
+    out[8] = key(x + 1, 2u);
+    out[9] = key(bin_w<FastDiv>(__fsub_rn(m, k.dnh3), ibw), 1u);
+}
+
+// Warp-wide ascending bitonic sort of n2 (a power of two) keys in shared memory.
+__device__ __forceinline__ void warp_bitonic_sort(uint32_t *kb, int32_t n2) {
+    const int lane = threadIdx.x & 31;
+    for (int32_t kk = 2; kk <= n2; kk <<= 1) {
+        for (int32_t j = kk >> 1; j > 0; j >>= 1) {
+            for (int32_t i = lane; i < n2; i += 32) {
+                const int32_t l = i ^ j;
+                if (l > i) {
+                    const uint32_t a = kb[i], b = kb[l];
+                    if ((a > b) == ((i & kk) == 0)) {
+                        kb[i] = b;
+                        kb[l] = a;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+template <bool FastDiv>
+__global__ void __launch_bounds__(256) k_gen_lists_long(DevDB db, const int32_t *__restrict__ cover, int64_t npep1,
+                                                        int32_t nbins, const uint32_t *__restrict__ lstart,
+                                                        uint64_t total10, uint32_t *__restrict__ lists,
+                                                        uint16_t *__restrict__ list_len, float ibw,
+                                                        unsigned long long *__restrict__ stats,
+                                                        uint32_t *__restrict__ err) {
+    extern __shared__ __align__(16) uint32_t keybuf[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t *kb = keybuf + (size_t)warp * kLongKeys;
+    __shared__ unsigned long long s_stats[2];
+    if (threadIdx.x < 2) s_stats[threadIdx.x] = 0ull;
+    __syncthreads();
+    const float mt_lane = db.mt[lane];
+    uint32_t my_lists = 0, my_entries = 0;
+    for (int64_t t = (int64_t)blockIdx.x * nw + warp; t < (int64_t)db.num_pep; t += (int64_t)gridDim.x * nw) {
+        const uint32_t p = (uint32_t)t;
+        uint32_t need = 0;
+        if (lane < kLevels && cover[(int64_t)lane * npep1 + p] > 0) need = 1u;
+        need = __ballot_sync(kFullMask, need) & ((1u << kLevels) - 1u);
+        if (lane < kLevels && !((need >> lane) & 1u)) list_len[(size_t)lane * db.num_pep + p] = 0;
+        if (!need) continue;
+        const int zmax = 32 - __clz(need);
+        const uint32_t tc = db.tc_sorted[p], tn = db.tn_sorted[p];
+        const float r = db.r_sorted[p];
+        const uint32_t nchunk = (tn - tc + 31u) / 32u;
+        if (tn < tc || nchunk * 32u * (uint32_t)zmax * 10u > (uint32_t)kLongKeys) {
+            if (lane == 0) atomicOr(err, kErrTooLong);
+            if (lane < kLevels && ((need >> lane) & 1u)) list_len[(size_t)lane * db.num_pep + p] = 0;
+            continue;
+        }
+        for (int z = 1; z <= zmax; ++z) {
+            if (!((need >> (z - 1)) & 1u)) continue;
+            const int32_t nslot = (int32_t)nchunk * 32 * z * 10;
+            int32_t n2 = 32;
+            while (n2 < nslot) n2 <<= 1;
+            for (int32_t i = lane; i < n2; i += 32) kb[i] = 0xFFFFFFFFu;
+            __syncwarp();
+            // the b-ladder: the reference warp scan per 32-residue chunk
+            float carry = 0.0f;
+            for (uint32_t ci = 0; ci < nchunk; ++ci) {
+                const uint32_t base = tc + 32u * ci;
+                const int cnt = (int)min(32u, tn - base);
+                uint32_t byte = 0;
+                if (lane < cnt) byte = __ldg(db.ions + base + lane);
+                float v = residue_mass(mt_lane, byte);
+                if (lane >= cnt) v = 0.0f;
+                if (lane == 0) v = __fadd_rn(v, carry);
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const float u = __shfl_up_sync(kFullMask, v, d);
+                    if (lane >= d) v = __fadd_rn(v, u);
+                }
+                carry = __shfl_sync(kFullMask, v, cnt - 1);
+                if (lane < cnt) {
+                    const float y = __fsub_rn(r, v);
+                    for (int c = 1; c <= z; ++c)
+                        emit_keys<FastDiv>(v, y, charge_const<FastDiv>(c), nbins, ibw,
+                                           kb + ((size_t)(ci * z + (c - 1)) * 32 + lane) * 10);
+                }
+            }
+            __syncwarp();
+            warp_bitonic_sort(kb, n2);
+            // keep the last key of each bin (its highest level), in order
+            const uint64_t off = list_offset(lstart, total10, z, p);
+            const int32_t slot = 10 * z * (int32_t)(tn - tc);
+            int32_t n = 0;
+            for (int32_t i0 = 0; i0 < n2; i0 += 32) {
+                const int32_t i = i0 + lane;
+                const uint32_t k = kb[i];
+                const bool keep = k != 0xFFFFFFFFu && (i + 1 == n2 || (kb[i + 1] >> 2) != (k >> 2));
+                const uint32_t bal = __ballot_sync(kFullMask, keep);
+                const int32_t at = n + __popc(bal & ((1u << lane) - 1u));
+                if (keep && at < slot) lists[off + at] = k;
+                n += __popc(bal);
+            }
+            if (n > slot) {
+                if (lane == 0) atomicOr(err, kErrListOverflow);
+                n = slot;
+            }
+            if (lane == 0) list_len[(size_t)(z - 1) * db.num_pep + p] = (uint16_t)min(n, 65535);
+            my_lists += 1u;
+            my_entries += (uint32_t)n;
+            __syncwarp();
+        }
+    }
+    if (stats) {
+        if (lane == 0) {
+            atomicAdd(&s_stats[0], (unsigned long long)my_lists);
+            atomicAdd(&s_stats[1], (unsigned long long)my_entries);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            atomicAdd(&stats[0], s_stats[0]);
+            atomicAdd(&stats[1], s_stats[1]);
+        }
+    }
+}
+
+// FP32 rescoring of kept unmodified candidates from their lists and the
+// FP32 row in global memory (long rows), canonical order: entry i by lane
+// i % 32, XOR butterfly.  One CTA per spectrum.
+__global__ void __launch_bounds__(256) k_rescore_lists(const uint32_t *__restrict__ lists,
+                                                       const uint32_t *__restrict__ lstart, uint64_t total10,
+                                                       const uint16_t *__restrict__ list_len, uint32_t num_pep,
+                                                       const uint32_t *__restrict__ idx_sorted,
+                                                       const float *__restrict__ rows32, int64_t stride,
+                                                       const SpecMeta *__restrict__ meta,
+                                                       const uint64_t *__restrict__ kept_k, int32_t K, int32_t topn,
+                                                       float *__restrict__ out_s, uint64_t *__restrict__ out_k,
+                                                       uint32_t *__restrict__ out_pep, uint32_t *__restrict__ err) {
+    __shared__ float res_s[kMaxTopK];
+    __shared__ uint64_t res_k[kMaxTopK];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int32_t s = blockIdx.x;
+    const SpecMeta m = meta[s];
+    const float *row = rows32 + (size_t)s * stride;
+    const int z = m.charges_plain;
+    for (int t = warp; t < K; t += nw) {
+        const uint64_t kk = kept_k[(size_t)s * K + t];
+        float sc = -INFINITY;
+        if (kk != ~0ull) {
+            float acc = 0.0f;
+            if (!(kk >> 63) && z >= 1 && kk < num_pep) {
+                const uint32_t p = (uint32_t)kk;
+                const int n = list_len[(size_t)(z - 1) * num_pep + p];
+                const uint32_t *lp = lists + list_offset(lstart, total10, z, p);
+                for (int i = lane; i < n; i += 32) {
+                    const uint32_t e = __ldg(lp + i);
+                    const uint32_t bin = e >> 2;
+                    if ((int32_t)bin < m.len) acc = __fmaf_rn(level_weight(e & 3u), __ldg(row + bin), acc);
+                }
+            } else if (kk >> 63) {
+                if (lane == 0) atomicOr(err, kErrBounds);
+            }
+#pragma unroll
+            for (int o = 16; o >= 1; o >>= 1) acc = __fadd_rn(acc, __shfl_xor_sync(kFullMask, acc, o));
+            sc = acc;
+        }
+        if (lane == 0) {
+            res_s[t] = sc;
+            res_k[t] = kk;
+        }
+    }
+    __syncthreads();
+    if (warp == 0) {
+        WarpTopK tk;
+        tk.init();
+        for (int t = 0; t < K; ++t)
+            if (res_k[t] != ~0ull) tk.insert(res_s[t], res_k[t], topn);
+        if (lane < topn) {
+            out_s[(size_t)s * topn + lane] = tk.s;
+            out_k[(size_t)s * topn + lane] = tk.k;
+            out_pep[(size_t)s * topn + lane] = (tk.k != ~0ull && tk.k < num_pep) ? idx_sorted[tk.k] : ~0u;
+        }
+    }
+}
+
 // Scorer over precomputed lists: a persistent grid pulls work items (group x
 // candidate chunk); the group's interleaved tile is staged by one bulk copy;
 // a warp streams each candidate's list (entry i by lane i % 32, four loads
 // in flight per lane) and gathers the tile; CTA-wide top-K per member.
-template <typename T, int G>
+// E = list entry type (uint16_t up to 16,383 bins, uint32_t for long rows);
+// kGlobal: the group tile is read from global memory (L2) instead of being
+// staged in shared memory (rows too long for shared memory).
+template <typename T, int G, typename E, bool kGlobal>
 __global__ void __launch_bounds__(1024, 1)
-k_score_lists(const uint16_t *__restrict__ lists, const uint32_t *__restrict__ lstart, uint64_t total10,
+k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, uint64_t total10,
               uint64_t list_total, const uint16_t *__restrict__ list_len, uint32_t num_pep,
               const T *__restrict__ tiles, int64_t stride,
               const uint32_t *__restrict__ wb, const uint32_t *__restrict__ we, const int32_t *__restrict__ perm,
               const GroupInfo *__restrict__ groups, const uint32_t *__restrict__ item_off,
-              const uint32_t *__restrict__ ngroups_p, int32_t chunk, int32_t K, uint32_t *__restrict__ counter,
+              const uint32_t *__restrict__ ngroups_p, int32_t K, uint32_t *__restrict__ counter,
               float *__restrict__ part_s, uint64_t *__restrict__ part_k, unsigned long long *__restrict__ stats,
               uint32_t *__restrict__ err) {
     extern __shared__ __align__(128) uint8_t smem[];
@@ -247,6 +471,7 @@ k_score_lists(const uint16_t *__restrict__ lists, const uint32_t *__restrict__ l
     const int cap = nw * K;
     float *buf_s = reinterpret_cast<float *>(smem + 128);
     uint32_t *buf_k = reinterpret_cast<uint32_t *>(buf_s + (size_t)G * cap);
+    const T *tile = stile;
     __shared__ int32_t s_item;
     __shared__ uint32_t s_next;
     __shared__ uint32_t s_wb[G], s_we[G];
@@ -287,19 +512,25 @@ k_score_lists(const uint16_t *__restrict__ lists, const uint32_t *__restrict__ l
         }
         if (threadIdx.x == 0) s_next = p0;
         const int32_t nb = tile_bins(gi.maxlen);
-        if (threadIdx.x == 0) {
-            fence_proxy_async();
-            const uint32_t bytes = (uint32_t)((size_t)nb * G * sizeof(T));
-            mbar_arrive_expect_tx(bar, bytes);
-            bulk_g2s(stile, tiles + (size_t)g * stride * G, bytes, bar);
+        if constexpr (kGlobal) {
+            tile = tiles + (size_t)g * stride * G;
+            slots.init();
+            __syncthreads();
+        } else {
+            if (threadIdx.x == 0) {
+                fence_proxy_async();
+                const uint32_t bytes = (uint32_t)((size_t)nb * G * sizeof(T));
+                mbar_arrive_expect_tx(bar, bytes);
+                bulk_g2s(stile, tiles + (size_t)g * stride * G, bytes, bar);
+            }
+            slots.init();
+            __syncthreads();
+            if (!mbar_wait(bar, phase, kWaitLimit)) {
+                if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
+                return;
+            }
+            phase ^= 1u;
         }
-        slots.init();
-        __syncthreads();
-        if (!mbar_wait(bar, phase, kWaitLimit)) {
-            if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
-            return;
-        }
-        phase ^= 1u;
         const uint32_t my_b = lane < G ? s_wb[lane] : 0u, my_e = lane < G ? s_we[lane] : 0u;
         const int z = (int)gi.charges;
         const uint16_t *llen = list_len + (size_t)(z >= 1 ? z - 1 : 0) * num_pep;
@@ -309,7 +540,7 @@ k_score_lists(const uint16_t *__restrict__ lists, const uint32_t *__restrict__ l
         struct Cand {
             uint32_t p, act;
             int n;
-            const uint16_t *lp;
+            const E *lp;
             uint32_t e[4];
         };
         auto next_active = [&]() {
@@ -369,7 +600,7 @@ k_score_lists(const uint16_t *__restrict__ lists, const uint32_t *__restrict__ l
                     if ((int32_t)bin < nb) {
                         const float w = level_weight(e[k] & 3u);
                         float x[G];
-                        TileLoad<T, G>::load(stile, bin, x);
+                        TileLoad<T, G>::load(tile, bin, x);
 #pragma unroll
                         for (int j = 0; j < G; ++j) acc[j] = __fmaf_rn(w, x[j], acc[j]);
                     }
@@ -447,24 +678,23 @@ int hfx_lists_generate(const DevDB &db, const int32_t *cover, int64_t npep1, int
     return (int)cudaGetLastError();
 }
 
-template <typename T, int G>
-static int launch_lists_t(const uint16_t *lists, const uint32_t *lstart, uint64_t total10, const uint16_t *list_len,
-                          uint32_t num_pep, const T *rows, int64_t stride, const SpecMeta *meta, const uint32_t *wb,
-                          const uint32_t *we, const BatchedWs &ws, void *tiles, uint32_t ngroups, int32_t chunk,
-                          int32_t K, int nw, float *part_s, uint64_t *part_k, unsigned long long *stats,
-                          uint32_t *err, cudaStream_t st) {
-    (void)rows;
+template <typename T, int G, typename E, bool kGlobal>
+static int launch_lists_t(const E *lists, const uint32_t *lstart, uint64_t total10, const uint16_t *list_len,
+                          uint32_t num_pep, int64_t stride, const uint32_t *wb, const uint32_t *we,
+                          const BatchedWs &ws, void *tiles, int32_t K, int nw,
+                          float *part_s, uint64_t *part_k, unsigned long long *stats, uint32_t *err,
+                          cudaStream_t st) {
     int dev = 0, sms = 0, smem_max = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (nw <= 0) nw = 16;
-    const size_t tile = ((size_t)stride * G * sizeof(T) + 15) & ~(size_t)15;
+    const size_t tile = kGlobal ? 0 : (((size_t)stride * G * sizeof(T) + 15) & ~(size_t)15);
     // the tile region doubles as the item-end buffer of the warps' survivors
     const size_t survivors = (size_t)G * nw * K * 8;
     const size_t smem = 128 + std::max(tile, survivors);
     if (smem > (size_t)smem_max) return (int)cudaErrorInvalidValue;
-    auto fn = k_score_lists<T, G>;
+    auto fn = k_score_lists<T, G, E, kGlobal>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
     int per = 0;
@@ -472,20 +702,25 @@ static int launch_lists_t(const uint16_t *lists, const uint32_t *lstart, uint64_
     const int grid = sms * (per > 0 ? per : 1);
     cudaMemsetAsync(ws.counter, 0, 4, st);
     fn<<<grid, nw * 32, smem, st>>>(lists, lstart, total10, total10 * 10, list_len, num_pep, (const T *)tiles,
-                                    stride, wb, we,
-                                    ws.perm, ws.groups, ws.item_off, ws.ngroups, chunk, K, ws.counter, part_s, part_k,
-                                    stats, err);
+                                    stride, wb, we, ws.perm, ws.groups, ws.item_off, ws.ngroups, K,
+                                    ws.counter, part_s, part_k, stats, err);
     return (int)cudaGetLastError();
 }
 
-int hfx_lists_score(const uint16_t *lists, const uint32_t *lstart, uint64_t total10, const uint16_t *list_len,
-                    uint32_t num_pep, const void *rows, int elem_kind, int64_t stride, const SpecMeta *meta,
-                    const uint32_t *wb, const uint32_t *we, const BatchedWs &ws, void *tiles, uint32_t ngroups,
-                    int32_t G, int32_t chunk, int32_t K, int nw, float *part_s, uint64_t *part_k,
-                    unsigned long long *stats, uint32_t *err, cudaStream_t st) {
-#define HFX_L(T, GG)                                                                                              \
-    return launch_lists_t<T, GG>(lists, lstart, total10, list_len, num_pep, (const T *)rows, stride, meta, wb, we,\
-                                 ws, tiles, ngroups, chunk, K, nw, part_s, part_k, stats, err, st)
+int hfx_lists_score(const void *lists, int long_rows, const uint32_t *lstart, uint64_t total10,
+                    const uint16_t *list_len, uint32_t num_pep, int elem_kind, int64_t stride, const uint32_t *wb,
+                    const uint32_t *we, const BatchedWs &ws, void *tiles, int32_t G, int32_t K, int nw,
+                    float *part_s, uint64_t *part_k, unsigned long long *stats, uint32_t *err, cudaStream_t st) {
+#define HFX_L(T, GG)                                                                                           \
+    do {                                                                                                       \
+        if (long_rows)                                                                                         \
+            return launch_lists_t<T, GG, uint32_t, true>((const uint32_t *)lists, lstart, total10, list_len,   \
+                                                         num_pep, stride, wb, we, ws, tiles, K, nw, part_s,    \
+                                                         part_k, stats, err, st);                              \
+        return launch_lists_t<T, GG, uint16_t, false>((const uint16_t *)lists, lstart, total10, list_len,      \
+                                                      num_pep, stride, wb, we, ws, tiles, K, nw, part_s,       \
+                                                      part_k, stats, err, st);                                 \
+    } while (0)
     if (elem_kind == 0) {
         if (G == 4) HFX_L(float, 4);
         if (G == 8) HFX_L(float, 8);
@@ -504,4 +739,32 @@ int hfx_lists_score(const uint16_t *lists, const uint32_t *lstart, uint64_t tota
     }
 #undef HFX_L
     return (int)cudaErrorInvalidValue;
+}
+
+int hfx_lists_generate_long(const DevDB &db, const int32_t *cover, int64_t npep1, int32_t nbins,
+                            const uint32_t *lstart, uint64_t total10, uint32_t *lists, uint16_t *list_len,
+                            int fastdiv, float ion_bw, unsigned long long *stats, uint32_t *err,
+                            cudaStream_t st) {
+    const int nw = 8;
+    const size_t smem = (size_t)nw * kLongKeys * 4;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    auto f = fastdiv ? k_gen_lists_long<true> : k_gen_lists_long<false>;
+    cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, nw * 32, smem);
+    f<<<sms * (per > 0 ? per : 1), nw * 32, smem, st>>>(db, cover, npep1, nbins, lstart, total10, lists, list_len,
+                                                        ion_bw, stats, err);
+    return (int)cudaGetLastError();
+}
+
+int hfx_rescore_lists(const uint32_t *lists, const uint32_t *lstart, uint64_t total10, const uint16_t *list_len,
+                      uint32_t num_pep, const uint32_t *idx_sorted, const float *rows32, int64_t stride,
+                      const SpecMeta *meta, const uint64_t *kept_k, int32_t nspec, int32_t K, int32_t topn,
+                      float *out_s, uint64_t *out_k, uint32_t *out_pep, uint32_t *err, cudaStream_t st) {
+    if (nspec <= 0) return 0;
+    k_rescore_lists<<<nspec, 256, 0, st>>>(lists, lstart, total10, list_len, num_pep, idx_sorted, rows32, stride,
+                                           meta, kept_k, K, topn, out_s, out_k, out_pep, err);
+    return (int)cudaGetLastError();
 }

@@ -20,8 +20,20 @@ int hfx_lists_mark(const hfx::SpecMeta *meta, const uint32_t *wb, const uint32_t
 int hfx_lists_generate(const hfx::DevDB &db, const int32_t *cover, int64_t npep1, int32_t nbins,
                        const uint32_t *lstart, uint64_t total10, uint16_t *lists, uint16_t *list_len, int fastdiv,
                        unsigned long long *stats, uint32_t *err, cudaStream_t st);
-int hfx_lists_score(const uint16_t *lists, const uint32_t *lstart, uint64_t total10, const uint16_t *list_len,
-                    uint32_t num_pep, const void *rows, int elem_kind, int64_t stride, const hfx::SpecMeta *meta,
-                    const uint32_t *wb, const uint32_t *we, const hfx::BatchedWs &ws, void *tiles, uint32_t ngroups,
-                    int32_t G, int32_t chunk, int32_t K, int nw, float *part_s, uint64_t *part_k,
-                    unsigned long long *stats, uint32_t *err, cudaStream_t st);
+// Scorer over the lists; long_rows: 32-bit entries and group tiles read
+// from global memory (rows too long for shared memory), else 16-bit entries
+// and tiles staged in shared memory.
+int hfx_lists_score(const void *lists, int long_rows, const uint32_t *lstart, uint64_t total10,
+                    const uint16_t *list_len, uint32_t num_pep, int elem_kind, int64_t stride, const uint32_t *wb,
+                    const uint32_t *we, const hfx::BatchedWs &ws, void *tiles, int32_t G, int32_t K, int nw,
+                    float *part_s, uint64_t *part_k, unsigned long long *stats, uint32_t *err, cudaStream_t st);
+// Long rows: 32-bit lists built by sorting each (peptide, level)'s ion keys,
+// and FP32 rescoring of kept unmodified candidates from those lists.
+int hfx_lists_generate_long(const hfx::DevDB &db, const int32_t *cover, int64_t npep1, int32_t nbins,
+                            const uint32_t *lstart, uint64_t total10, uint32_t *lists, uint16_t *list_len,
+                            int fastdiv, float ion_bw, unsigned long long *stats, uint32_t *err,
+                            cudaStream_t st);
+int hfx_rescore_lists(const uint32_t *lists, const uint32_t *lstart, uint64_t total10, const uint16_t *list_len,
+                      uint32_t num_pep, const uint32_t *idx_sorted, const float *rows32, int64_t stride,
+                      const hfx::SpecMeta *meta, const uint64_t *kept_k, int32_t nspec, int32_t K, int32_t topn,
+                      float *out_s, uint64_t *out_k, uint32_t *out_pep, uint32_t *err, cudaStream_t st);

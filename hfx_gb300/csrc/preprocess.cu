@@ -146,6 +146,203 @@ __global__ void __launch_bounds__(256) k_preprocess(const float *__restrict__ mz
     }
 }
 
+// ---- long rows (e.g. 0.02 Da bins, ~10^5 bins): the same row, computed sparsely ----
+//
+// A row that does not fit in shared memory is built from its nonzero bins
+// only.  The binned values are the kept peaks' sqrt intensities, max per bin
+// (sort the (bin, value) keys, keep the last of each bin); normalisation
+// touches only those bins; and x[i] is nonzero only where the 151-bin window
+// of i holds a nonzero bin or e[i] != 0.  Every e is >= 0, so the reference's
+// left fold over the window equals the left fold over the window's nonzero
+// bins (adding +0 is exact and the sum never is -0): the row is bit-identical
+// to the dense computation.
+constexpr int kSparsePeaks = 4096;
+constexpr size_t kDenseRowBytes = 200 * 1024;  // rows up to 51,200 bins are built densely in shared memory
+
+// Block-wide exclusive scan of one value per thread (blockDim.x <= 1024).
+__device__ __forceinline__ int32_t block_excl_scan(int32_t v, int32_t *warp_tot, int32_t &total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int32_t x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int32_t t = __shfl_up_sync(0xFFFFFFFFu, x, d);
+        if (lane >= d) x += t;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int32_t w = lane < nw ? warp_tot[lane] : 0;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int32_t t = __shfl_up_sync(0xFFFFFFFFu, w, d);
+            if (lane >= d) w += t;
+        }
+        warp_tot[lane] = w;
+    }
+    __syncthreads();
+    total = warp_tot[nw - 1];
+    const int32_t before = (warp ? warp_tot[warp - 1] : 0) + x - v;
+    __syncthreads();
+    return before;
+}
+
+__global__ void __launch_bounds__(256) k_preprocess_sparse(const float *__restrict__ mz, const float *__restrict__ it,
+                                                           const int64_t *__restrict__ off,
+                                                           const float *__restrict__ pcr, LayoutParams lp,
+                                                           const SpecMeta *__restrict__ meta, int64_t stride,
+                                                           float *__restrict__ out32,
+                                                           __nv_bfloat16 *__restrict__ outbf,
+                                                           __half *__restrict__ outh, uint32_t *__restrict__ err) {
+    extern __shared__ __align__(16) uint8_t sm_sparse[];
+    unsigned long long *keys = reinterpret_cast<unsigned long long *>(sm_sparse);  // [kSparsePeaks]
+    int32_t *nzk = reinterpret_cast<int32_t *>(keys + kSparsePeaks);               // [kSparsePeaks]
+    float *nze = reinterpret_cast<float *>(nzk + kSparsePeaks);                    // [kSparsePeaks]
+    int32_t *ivs = reinterpret_cast<int32_t *>(nze + kSparsePeaks);                // [kSparsePeaks + 1]
+    __shared__ int32_t warp_tot[32];
+    __shared__ float rmax[11];
+    const int32_t s = blockIdx.x;
+    const SpecMeta m = meta[s];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    float *o32 = out32 + (int64_t)s * stride;
+    __nv_bfloat16 *obf = outbf ? outbf + (int64_t)s * stride : nullptr;
+    __half *oh = outh ? outh + (int64_t)s * stride : nullptr;
+    // zero rows (stride is a multiple of 16 elements, rows 16-byte aligned)
+    for (int64_t i = (int64_t)tid * 4; i < stride; i += (int64_t)nt * 4)
+        *reinterpret_cast<float4 *>(o32 + i) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int64_t i = (int64_t)tid * 8; i < stride; i += (int64_t)nt * 8) {
+        if (obf) *reinterpret_cast<uint4 *>(obf + i) = make_uint4(0u, 0u, 0u, 0u);
+        if (oh) *reinterpret_cast<uint4 *>(oh + i) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    if (m.status != 0) return;
+    if (m.npk > kSparsePeaks) {
+        if (tid == 0) atomicOr(err, kErrTooLong);
+        return;
+    }
+    const int32_t len = m.len;
+    // observedIntensity, Correlation.hs:58-71: (bin, sqrt intensity) keys
+    const float ps = pcr[s];
+    const float plo = __fsub_rn(ps, 15.0f), phi = __fadd_rn(ps, 15.0f);
+    const int64_t o0 = off[s];
+    int32_t n2 = 1;
+    while (n2 < m.npk) n2 <<= 1;
+    for (int32_t i = tid; i < n2; i += nt) {
+        unsigned long long k = ~0ull;
+        if (i < m.npk) {
+            const float x = mz[o0 + i];
+            const bool keep = lp.remove_pcr ? (x <= m.cutoff && (x <= plo || phi <= x)) : (x <= m.cutoff);
+            if (keep) {
+                const float q = rintf(__fdiv_rn(x, lp.bw));
+                const float v = __fsqrt_rn(it[o0 + i]);
+                if (q >= 0.0f && q < (float)len && v >= 0.0f)
+                    k = ((unsigned long long)(uint32_t)(int32_t)q << 32) | __float_as_uint(v);
+            }
+        }
+        keys[i] = k;
+    }
+    if (tid < 11) rmax[tid] = 0.0f;
+    __syncthreads();
+    // bitonic sort, ascending (bin, then value: non-negative floats order as their bits)
+    for (int32_t kk = 2; kk <= n2; kk <<= 1) {
+        for (int32_t j = kk >> 1; j > 0; j >>= 1) {
+            for (int32_t i = tid; i < n2; i += nt) {
+                const int32_t l = i ^ j;
+                if (l > i) {
+                    const unsigned long long a = keys[i], b = keys[l];
+                    const bool up = (i & kk) == 0;
+                    if ((a > b) == up) {
+                        keys[i] = b;
+                        keys[l] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // the last key of each bin carries the bin's max; compact them in order
+    int32_t nnz = 0;
+    for (int32_t base = 0; base < n2; base += nt) {
+        const int32_t i = base + tid;
+        const unsigned long long k = i < n2 ? keys[i] : ~0ull;
+        const bool last = k != ~0ull && (i + 1 >= n2 || (keys[i + 1] >> 32) != (k >> 32));
+        int32_t tot = 0;
+        const int32_t at = nnz + block_excl_scan(last ? 1 : 0, warp_tot, tot);
+        if (last) {
+            nzk[at] = (int32_t)(k >> 32);
+            nze[at] = __uint_as_float((uint32_t)k);
+        }
+        nnz += tot;
+    }
+    __syncthreads();
+    // normaliseByRegion, Correlation.hs:84-96
+    const int32_t sel = (len - 75) / 10;
+    for (int32_t j = tid; j < nnz; j += nt) {
+        const float v = nze[j];
+        if (v > 0.0f) atomicMax((int *)&rmax[min(10, nzk[j] / sel)], __float_as_int(v));
+    }
+    __syncthreads();
+    for (int32_t j = tid; j < nnz; j += nt) {
+        const int32_t k = nzk[j];
+        const float mx = rmax[min(10, k / sel)];
+        nze[j] = (mx > 1e-6f && k < sel * 10) ? __fmul_rn(50.0f, __fdiv_rn(nze[j], mx)) : 0.0f;
+    }
+    // positions whose window holds a nonzero bin: [0, 75), and per nonzero
+    // bin k the positions i >= 75 with |i - k| <= 75, minus the previous
+    // bin's (bins ascending, so the pieces are disjoint)
+    const int32_t head = min(75, len);
+    int32_t tot = 0;
+    for (int32_t base = 0; base < nnz; base += nt) {
+        const int32_t j = base + tid;
+        int32_t c = 0;
+        if (j < nnz) {
+            const int32_t k = nzk[j];
+            int32_t a = max(head, k - 75);
+            if (j > 0) a = max(a, nzk[j - 1] + 76);
+            const int32_t b = min(len, k + 76);
+            c = max(0, b - a);
+        }
+        int32_t t = 0;
+        const int32_t at = tot + block_excl_scan(c, warp_tot, t);
+        if (j < nnz) ivs[j] = at;
+        tot += t;
+    }
+    if (tid == 0) ivs[nnz] = tot;
+    __syncthreads();
+    // crossCorrolation, Correlation.hs:105-109, at those positions only
+    for (int32_t u = tid; u < head + tot; u += nt) {
+        int32_t i;
+        if (u < head) {
+            i = u;
+        } else {
+            const int32_t v = u - head;
+            int32_t lo = 0, hi = nnz;  // last j with ivs[j] <= v
+            while (hi - lo > 1) {
+                const int32_t mid = (lo + hi) >> 1;
+                if (ivs[mid] <= v) lo = mid; else hi = mid;
+            }
+            const int32_t k = nzk[lo];
+            int32_t a = max(head, k - 75);
+            if (lo > 0) a = max(a, nzk[lo - 1] + 76);
+            i = a + (v - ivs[lo]);
+        }
+        const int32_t wlo = max(0, i - 75);
+        const int32_t whi = min(len, wlo + 151);
+        int32_t a = 0, b = nnz;  // first nonzero bin >= wlo
+        while (a < b) {
+            const int32_t mid = (a + b) >> 1;
+            if (nzk[mid] < wlo) a = mid + 1; else b = mid;
+        }
+        float acc = 0.0f, ei = 0.0f;
+        for (int32_t j = a; j < nnz && nzk[j] < whi; ++j) {
+            acc = __fadd_rn(acc, nze[j]);
+            if (nzk[j] == i) ei = nze[j];
+        }
+        const float x = __fsub_rn(ei, __fdiv_rn(acc, 150.0f));
+        o32[i] = x;
+        if (obf) obf[i] = __float2bfloat16_rn(x);
+        if (oh) oh[i] = __float2half_rn(x);
+    }
+}
+
 }  // namespace hfx
 
 using namespace hfx;
@@ -160,15 +357,22 @@ int hfx_launch_layout(const float *mz, const int64_t *off, const float *pcr, con
 
 int hfx_launch_preprocess(const float *mz, const float *it, const int64_t *off, const float *pcr,
                           const LayoutParams &lp, const SpecMeta *meta, int32_t nspec, int64_t stride,
-                          float *out32, __nv_bfloat16 *outbf, __half *outh, cudaStream_t st) {
+                          float *out32, __nv_bfloat16 *outbf, __half *outh, uint32_t *err, cudaStream_t st) {
     if (nspec <= 0) return 0;
     const size_t smem = (size_t)stride * sizeof(float);
+    if (smem > kDenseRowBytes) {
+        // long rows: the sparse form (needs the error word for its peak limit)
+        if (!err) return (int)cudaErrorInvalidValue;
+        const size_t sm = (size_t)kSparsePeaks * (8 + 4 + 4 + 4) + 16;
+        cudaFuncSetAttribute(k_preprocess_sparse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_preprocess_sparse<<<nspec, 256, sm, st>>>(mz, it, off, pcr, lp, meta, stride, out32, outbf, outh, err);
+        return (int)cudaGetLastError();
+    }
     static bool attr_set = false;
     if (!attr_set) {
-        cudaFuncSetAttribute(k_preprocess, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_preprocess, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDenseRowBytes);
         attr_set = true;
     }
-    if (smem > 200 * 1024) return (int)cudaErrorInvalidValue;
     k_preprocess<<<nspec, 256, smem, st>>>(mz, it, off, pcr, lp, meta, stride, out32, outbf, outh);
     return (int)cudaGetLastError();
 }

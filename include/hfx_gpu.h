@@ -47,7 +47,10 @@ typedef struct hfx_search_params {
     int32_t search_mods;           /* score variable-modification isoforms (needs hfx_set_mods) */
     int32_t group_size;            /* spectra per batched work item (1..8), 0 = default       */
     int32_t chunk;                 /* candidates per batched work item, 0 = default            */
-    int32_t max_len;               /* longest spectrum row accepted, 0 = default               */
+    int32_t max_len;               /* longest spectrum row accepted, 0 = default (262,144)     */
+    int32_t ion_bins_custom;       /* 1: ion bins use bin_width too (new; the reference bins
+                                      ions with the mono width, ion_series.cu:68); rows longer
+                                      than 8,192 bins only                                     */
 } hfx_search_params;
 
 /* Fill p with the engine defaults (reference behaviour where it has one). */

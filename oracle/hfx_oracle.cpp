@@ -78,7 +78,9 @@ inline int32_t sat_bin(float r) {
 
 /* ion_series.cu:59-69 with IEEE division in place of __fdividef. */
 inline float ion_mz(float m, float c, float hc) { return (m + hc) / c; }
-inline int32_t bin_mz(float mz) { return sat_bin(std::rint(mz / kBinMono)); }
+/* ion_series.cu:65-69 bins every ion with the mono width (H3); ibw > 0 is
+ * the new switch that bins ions with a custom width instead (0.02 Da rows). */
+inline int32_t bin_mz(float mz, float ibw) { return sat_bin(std::rint(mz / (ibw > 0.0f ? ibw : kBinMono))); }
 
 struct Hist {
     /* dense max-level row over [0,len) + touched list: the reference's
@@ -99,28 +101,28 @@ struct Hist {
 };
 
 /* ion_series.cu:78-123: the 10 ions of one (b, y, charge). */
-inline void add_ions(Hist &h, float b, float y, int c, int32_t len) {
+inline void add_ions(Hist &h, float b, float y, int c, int32_t len, float ibw) {
     const float cf = (float)c;
     const float hc = kDevH * cf;           /* MASS_H * charge (compile-time) */
     const float dh2o = kDevH2O / cf;
     const float dnh3 = kDevNH3 / cf;
     /* A ion */
-    h.add(bin_mz(ion_mz(b - kDevCO, cf, hc)), 1, len);
+    h.add(bin_mz(ion_mz(b - kDevCO, cf, hc), ibw), 1, len);
     /* B ions */
     float m = ion_mz(b, cf, hc);
-    int32_t x = bin_mz(m);
+    int32_t x = bin_mz(m, ibw);
     h.add(x, 3, len);
     h.add(x + 1, 2, len);
     h.add(x - 1, 2, len);
-    h.add(bin_mz(m - dh2o), 1, len);
-    h.add(bin_mz(m - dnh3), 1, len);
+    h.add(bin_mz(m - dh2o, ibw), 1, len);
+    h.add(bin_mz(m - dnh3, ibw), 1, len);
     /* Y ions */
     m = ion_mz(y + kDevH2O, cf, hc);
-    x = bin_mz(m);
+    x = bin_mz(m, ibw);
     h.add(x, 3, len);
     h.add(x + 1, 2, len);
     h.add(x - 1, 2, len);
-    h.add(bin_mz(m - dnh3), 1, len);
+    h.add(bin_mz(m - dnh3, ibw), 1, len);
 }
 
 /* ion_series.cu:176-213: per 32-residue chunk, lane 0 adds the previous
@@ -128,7 +130,7 @@ inline void add_ions(Hist &h, float b, float y, int c, int32_t len) {
  * 1,2,4,8,16) in FP32; y = residual - b. */
 void gen_ions(Hist &h, const uint8_t *ions, const float *mt, uint32_t tc,
               uint32_t tn, float residual, int charges, int32_t len,
-              const float *res_add, const uint8_t *modded) {
+              const float *res_add, const uint8_t *modded, float ibw = 0.0f) {
     h.reset(len);
     if (charges <= 0) return;
     float carry = 0.0f;
@@ -151,7 +153,7 @@ void gen_ions(Hist &h, const uint8_t *ions, const float *mt, uint32_t tc,
         for (int l = 0; l < cnt; ++l) {
             const float b = v[l];
             const float y = residual - b;
-            for (int c = 1; c <= charges; ++c) add_ions(h, b, y, c, len);
+            for (int c = 1; c <= charges; ++c) add_ions(h, b, y, c, len, ibw);
         }
     }
 }
@@ -666,7 +668,7 @@ int32_t hfxo_search(const uint8_t *ions, const float *mt, const float *r,
                     uint32_t e = (uint32_t)(std::upper_bound(rs.begin(), rs.end(), hi) - rs.begin());
                     for (uint32_t q = b; q < e; ++q) {
                         const uint32_t pi = idx[q];
-                        gen_ions(h, ions, mt, tc[pi], tn[pi], r[pi], ch, len, nullptr, nullptr);
+                        gen_ions(h, ions, mt, tc[pi], tn[pi], r[pi], ch, len, nullptr, nullptr, p->ion_bw);
                         int32_t n = collect(h, bins.data(), lv.data(), (int32_t)bins.size());
                         Entry en;
                         if (n < 0) { status = -2; n = 0; }
@@ -700,7 +702,8 @@ int32_t hfxo_search(const uint8_t *ions, const float *mt, const float *r,
                                     uint32_t mod = (ions[tc[pi] + a] >> 5) & 7u;
                                     radd[a] = mod ? p->ma_mass[mod - 1] : 0.0f;
                                 }
-                                gen_ions(h, ions, mt, tc[pi], tn[pi], resid, ch, len, radd.data(), modded.data());
+                                gen_ions(h, ions, mt, tc[pi], tn[pi], resid, ch, len, radd.data(), modded.data(),
+                                         p->ion_bw);
                                 int32_t n = collect(h, bins.data(), lv.data(), (int32_t)bins.size());
                                 Entry en;
                                 if (n < 0) { status = -2; n = 0; }

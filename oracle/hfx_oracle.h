@@ -131,6 +131,8 @@ typedef struct {
     int32_t plain;       /* 1: score unmodified candidates                     */
     uint8_t ma[16];
     float ma_mass[16];
+    float ion_bw;        /* 0: ion bins use the mono width (ion_series.cu:68); */
+                         /* > 0: ion bins use this width (new, 0.02 Da rows)   */
 } hfxo_params;
 
 int32_t hfxo_search(const uint8_t *ions, const float *mt26, const float *r,

@@ -22,6 +22,7 @@ class Params(C.Structure):
         ("bw", C.c_float), ("custom_bw", C.c_int32), ("remove_pcr", C.c_int32), ("ppm", C.c_int32),
         ("topn", C.c_int32), ("prec", C.c_int32), ("num_ma", C.c_int32), ("max_ma", C.c_int32),
         ("per_type", C.c_int32), ("plain", C.c_int32), ("ma", C.c_uint8 * 16), ("ma_mass", C.c_float * 16),
+        ("ion_bw", C.c_float),
     ]
 
 
@@ -193,12 +194,13 @@ def mod_isoform(ions_packed, tc, tn, ma, mod_counts, rank=None, per_type=False):
 
 
 def search(ions_packed, mt, r, tc, tn, idx, spectra, bw=1.0005079, custom_bw=False, remove_pcr=True, ppm=False,
-           topn=10, prec=0, ma=b"", ma_mass=(), max_ma=0, per_type=False, plain=True, nthreads=0):
+           topn=10, prec=0, ma=b"", ma_mass=(), max_ma=0, per_type=False, plain=True, nthreads=0, ion_bw=0.0):
     """Full search (Search.hs:98-124); returns (score, score64, key, pep, ncand)."""
     mz, it, off, pcr, z, tol = spectra.arrays()
     p = Params()
     p.bw, p.custom_bw, p.remove_pcr, p.ppm = bw, int(custom_bw), int(remove_pcr), int(ppm)
     p.topn, p.prec, p.num_ma, p.max_ma, p.per_type, p.plain = topn, prec, len(ma), max_ma, int(per_type), int(plain)
+    p.ion_bw = float(ion_bw)
     for i, c in enumerate(ma):
         p.ma[i] = c
         p.ma_mass[i] = ma_mass[i]

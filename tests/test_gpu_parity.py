@@ -238,3 +238,64 @@ def test_mixed_tolerance_open_search(tiny_engine, oracle, mode):
     if mode:
         res = eng.search(sub, hfx_gb300.default_params(top_n=10, batch_mode=mode, tol_ppm=2, precision=1))
         _compare(res, ref, f"mixed tolerance bf16 mode={mode}")
+
+
+HIGHRES = 0.02   # Da per bin: ~10^5 bins per row, beyond shared memory
+
+
+def _highres_subset(sp, n=16):
+    sub = sp.subset(np.arange(n))
+    return sub
+
+
+def test_long_rows_preprocess_bitexact(tiny_engine, oracle):
+    """0.02 Da rows (~10^5 bins) are built sparsely; they equal the dense
+    oracle rows bit for bit, with BF16/FP16 copies."""
+    import hfx_gb300
+    eng, prot, sp = tiny_engine
+    sub = _highres_subset(sp, 12)
+    p = hfx_gb300.default_params(bin_width=HIGHRES, custom_bin_width=1)
+    xs = [oracle.preprocess(sub.mz[sub.off[i]:sub.off[i + 1]], sub.it[sub.off[i]:sub.off[i + 1]], sub.pcr[i],
+                            sub.z[i], bw=HIGHRES, custom_bw=True) for i in range(len(sub))]
+    stride = (max(len(x) for x in xs) + 15) // 16 * 16
+    assert stride > 51200
+    n = len(sub)
+    rows = torch.empty((n, stride), dtype=torch.float32, device="cuda")
+    rbf = torch.empty((n, stride), dtype=torch.bfloat16, device="cuda")
+    rh = torch.empty((n, stride), dtype=torch.float16, device="cuda")
+    lens = torch.empty(n, dtype=torch.int32, device="cuda")
+    eng.preprocess(_dev(sub), p, stride, rows, rbf, rh, lens, None)
+    rows, lens = rows.cpu().numpy(), lens.cpu().numpy()
+    rbf, rh = rbf.float().cpu().numpy(), rh.float().cpu().numpy()
+    for i, x in enumerate(xs):
+        assert lens[i] == len(x)
+        assert np.array_equal(rows[i, :len(x)].view(np.uint32), x.view(np.uint32)), i
+        assert not rows[i, len(x):].any()
+        assert np.array_equal(rbf[i, :len(x)], torch.from_numpy(x).bfloat16().float().numpy())
+        assert np.array_equal(rh[i, :len(x)], x.astype(np.float16).astype(np.float32))
+
+
+@pytest.mark.parametrize("ion_custom", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
+def test_long_rows_search(tiny_engine, oracle, precision, ion_custom):
+    """Search at 0.02 Da: 32-bit sorted ion lists, tiles gathered from L2,
+    list-based FP32 rescoring.  ion_custom bins the ions at 0.02 Da too (the
+    new switch); 0 keeps the reference's mono-width ion bins."""
+    import hfx_gb300
+    eng, prot, sp = tiny_engine
+    sub = _highres_subset(sp, 16)
+    ref = oracle.search(*_oracle_db(oracle, eng, prot), sub, topn=10, bw=HIGHRES, custom_bw=True,
+                        ion_bw=HIGHRES if ion_custom else 0.0)
+    p = hfx_gb300.default_params(top_n=10, bin_width=HIGHRES, custom_bin_width=1, batch_mode=1,
+                                 precision=precision, rescore_k=32, ion_bins_custom=ion_custom)
+    res = eng.search(sub, p)
+    _compare(res, ref, f"0.02 Da precision={precision} ion_custom={ion_custom}")
+    if ion_custom:
+        assert (ref[0][:, 0] > 0).mean() > 0.9   # the source peptides score
+
+
+def test_custom_ion_width_needs_long_rows(tiny_engine):
+    import hfx_gb300
+    eng, prot, sp = tiny_engine
+    with pytest.raises(hfx_gb300.HfxError):
+        eng.search(sp.subset(np.arange(4)), hfx_gb300.default_params(ion_bins_custom=1, batch_mode=1))
