@@ -197,7 +197,14 @@ def _bytes_per_psm(eng, rows_dtype_bytes, wb, we, lens, charges, idx_tc_tn, rng,
 
 def _okw(cfg):
     """Oracle search settings of a workload."""
-    return dict(bw=cfg["bin_width"], custom_bw=bool(cfg.get("custom_bin_width", 0)), ppm=cfg.get("tol_ppm", 0))
+    return dict(bw=cfg["bin_width"], custom_bw=bool(cfg.get("custom_bin_width", 0)), ppm=cfg.get("tol_ppm", 0),
+                ion_bw=cfg["bin_width"] if cfg.get("ion_bins_custom", 0) else 0.0)
+
+
+def _pkw(cfg):
+    """Engine search settings of a workload."""
+    return dict(bin_width=cfg["bin_width"], tol_ppm=cfg.get("tol_ppm", 0),
+                custom_bin_width=cfg.get("custom_bin_width", 0), ion_bins_custom=cfg.get("ion_bins_custom", 0))
 
 
 def _oracle_inputs(prot, cfg):
@@ -310,9 +317,8 @@ def main():
     prec, mode = a.precision, a.batch_mode
     cpu_n, agree_n, plain_n = _samples(a)
     a.cpu_sample, a.agree_sample = cpu_n, agree_n
-    p = hfx_gb300.default_params(top_n=cfg["top_n"], bin_width=cfg["bin_width"], precision=prec, batch_mode=mode,
-                                 rescore_k=32 if prec else 0, group_size=a.group_size, chunk=a.chunk,
-                                 tol_ppm=cfg.get("tol_ppm", 0), custom_bin_width=cfg.get("custom_bin_width", 0))
+    p = hfx_gb300.default_params(top_n=cfg["top_n"], precision=prec, batch_mode=mode, rescore_k=32 if prec else 0,
+                                 group_size=a.group_size, chunk=a.chunk, **_pkw(cfg))
     d = torch.device("cuda", local)
     dev = dict(mz=torch.from_numpy(sp.mz).to(d), it=torch.from_numpy(sp.it).to(d),
                off=torch.from_numpy(sp.off).to(d), pcr=torch.from_numpy(sp.pcr).to(d),
@@ -375,8 +381,9 @@ def main():
     # the plain FP32 path (one launch per spectrum) on the same spectra
     plain = None
     if not a.no_plain and not has_mods:
-        p0 = hfx_gb300.default_params(top_n=tn_, bin_width=cfg["bin_width"], precision=0, batch_mode=0,
-                                      tol_ppm=cfg.get("tol_ppm", 0), custom_bin_width=cfg.get("custom_bin_width", 0))
+        # the plain FP32 path: one launch per spectrum (rows beyond 8192 bins
+        # always take the batched list path, there in FP32)
+        p0 = hfx_gb300.default_params(top_n=tn_, precision=0, batch_mode=0, **_pkw(cfg))
         n_pl = min(ns, plain_n)
         sub = sp if n_pl == ns else sp.subset(np.arange(n_pl))
         dev0 = dev if n_pl == ns else dict(mz=torch.from_numpy(sub.mz).to(d), it=torch.from_numpy(sub.it).to(d),
@@ -412,13 +419,28 @@ def main():
     eng.find_windows(dev, p, b_dev, e_dev)
     wb = b_dev.cpu().numpy().astype(np.int64)
     we = e_dev.cpu().numpy().astype(np.int64)
-    rows = torch.empty((ns, 8192), dtype=torch.float32, device=d)
-    lens_d = torch.empty(ns, dtype=torch.int32, device=d)
-    eng.preprocess(dev, p, 8192, rows, None, None, lens_d, None)
-    lens = lens_d.cpu().numpy().astype(np.int64)
-    del rows
-    charges = np.array([_charges(z) for z in sp.z], np.int64)
-    bpp, meanU = _bytes_per_psm(eng, bsz, wb, we, lens, charges, (tc[idx], tn[idx]), rng)
+    long_rows = bool(cfg.get("custom_bin_width", 0)) and cfg["bin_width"] < 0.5
+    if not long_rows:
+        rows = torch.empty((ns, 8192), dtype=torch.float32, device=d)
+        lens_d = torch.empty(ns, dtype=torch.int32, device=d)
+        eng.preprocess(dev, p, 8192, rows, None, None, lens_d, None)
+        lens = lens_d.cpu().numpy().astype(np.int64)
+        del rows
+        charges = np.array([_charges(z) for z in sp.z], np.int64)
+        bpp, meanU = _bytes_per_psm(eng, bsz, wb, we, lens, charges, (tc[idx], tn[idx]), rng)
+        u_basis = "distinct in-range ion bins, 4000 sampled pairs"
+    else:
+        # ~10^5-bin rows: U from the run's own counters (list entries streamed
+        # per candidate hand-out), L from sampled window positions
+        lens = np.where(we > wb, 1, 0)
+        meanU = work["entries_streamed"] / max(1, work["candidates"])
+        cnt = (we - wb).astype(np.int64)
+        ok = np.nonzero(cnt > 0)[0]
+        sp_i = rng.choice(ok, 4000, p=cnt[ok] / cnt[ok].sum())
+        pos = (wb[sp_i] + (rng.random(4000) * cnt[sp_i]).astype(np.int64))
+        meanL = float(np.mean((tn[idx] - tc[idx])[pos]))
+        bpp = meanU * bsz + meanL + 16
+        u_basis = "list entries streamed per candidate (run counters)"
     # pairs scored by the dominant kernel per launch (all of the step's pairs
     # go through it, or its modified share when it is the modification scorer)
     psm_kernel = psm_step
@@ -447,7 +469,7 @@ def main():
         "gpu_launches": int(launches_per_step * a.steps),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "kernel": kern,
-                     "bytes_per_psm": bpp, "mean_distinct_bins": meanU, "peak_kind": peak_kind,
+                     "bytes_per_psm": bpp, "mean_distinct_bins": meanU, "u_basis": u_basis, "peak_kind": peak_kind,
                      "step_achieved": bpp * psm_step / (ms_step / 1000.0) / 1e9},
         "clocks": clocks,
     }

@@ -220,5 +220,6 @@ def workload(name: str, n_spectra: int | None = None):
         sp = spectra(prot, n_spectra or 100000, seed=103, charge_p={1: 0.05, 2: 0.5, 3: 0.35, 4: 0.10},
                      npeaks=(50, 400), ppm_frac=0.8)
         bw = 0.02 if name == "highres" else 1.0005079
-        return prot, sp, dict(bin_width=bw, top_n=10, tol_ppm=2, custom_bin_width=int(name == "highres"))
+        hr = int(name == "highres")
+        return prot, sp, dict(bin_width=bw, top_n=10, tol_ppm=2, custom_bin_width=hr, ion_bins_custom=hr)
     raise KeyError(name)
