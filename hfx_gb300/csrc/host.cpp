@@ -79,6 +79,7 @@ struct hfx_ctx {
     // database (residual-mass order on the device)
     uint64_t num_ions = 0, num_pep = 0;
     uint64_t ladder_residues = 0;  // sum over fragments of (tn - tc)
+    uint32_t max_ladder = 0;       // max over fragments of (tn - tc)
     DBuf d_lstart;                 // per mass-order position: 10 * prefix sum of (tn - tc)
     unsigned long long counters[8] = {0};
     float mt[26] = {0};
@@ -208,6 +209,7 @@ int32_t upload_db(hfx_ctx *ctx) {
     std::vector<float> rs(np);
     std::vector<uint32_t> tcs(np), tns(np);
     ctx->ladder_residues = 0;
+    ctx->max_ladder = 0;
     std::vector<uint32_t> lstart(np);
     for (uint64_t i = 0; i < np; ++i) {
         rs[i] = ctx->h_r[ctx->h_idx[i]];
@@ -218,6 +220,7 @@ int32_t upload_db(hfx_ctx *ctx) {
             return fail(ctx, HFX_ERR_UNSUPPORTED, "ion-list offsets exceed 32 bits");
         lstart[i] = (uint32_t)(10ull * ctx->ladder_residues);
         ctx->ladder_residues += tns[i] - tcs[i];
+        ctx->max_ladder = std::max(ctx->max_ladder, tns[i] - tcs[i]);
     }
     std::vector<uint8_t> packed;
     pack_ions(ctx->h_ascii, ctx->ma, ctx->num_ma, packed);
@@ -404,7 +407,7 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     const int32_t ns = b.nspec;
     // one 16-byte tile load per bin: 8 BF16/FP16 or 4 FP32 spectra per group
     const int32_t G = p->group_size > 0 ? p->group_size : (elem_kind == 0 ? 4 : 8);
-    const int32_t chunk = p->chunk > 0 ? p->chunk : 1024;
+    const int32_t chunk = p->chunk > 0 ? p->chunk : 4096;
     if (G != 1 && G != 2 && G != 4 && G != 8) return fail(ctx, HFX_ERR_ARG, "group_size must be 1, 2, 4 or 8");
     const int32_t K = elem_kind == 0 ? p->top_n : std::max(p->top_n, std::min(p->rescore_k > 0 ? p->rescore_k : 32,
                                                                                kMaxTopK));
@@ -513,8 +516,9 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
                                          ctx->d_err.as<uint32_t>(), ctx->stream);
         else if (!rc)
             rc = hfx_lists_generate(db, cover, npep1, kMaxWords * 32, ctx->d_lstart.as<uint32_t>(), total10,
-                                    (uint16_t *)lists, llen, p->fastdiv, stats, ctx->d_err.as<uint32_t>(),
-                                    ctx->stream);
+                                    (uint16_t *)lists, llen, (int32_t)std::min<uint64_t>(40ull * ctx->max_ladder,
+                                                                                         kMaxListLen),
+                                    p->fastdiv, stats, ctx->d_err.as<uint32_t>(), ctx->stream);
         if (rc) return cuda_fail(ctx, (cudaError_t)rc, "ion lists");
         ctx->stage_end(HFX_STAGE_LISTS, 5, 0);
         ctx->stage_begin(HFX_STAGE_SCORE);

@@ -164,7 +164,7 @@ template <bool FastDiv>
 __global__ void __launch_bounds__(256) k_gen_lists(DevDB db, const int32_t *__restrict__ cover, int64_t npep1,
                                                    int32_t nbins, const uint32_t *__restrict__ lstart,
                                                    uint64_t total10, uint16_t *__restrict__ lists,
-                                                   uint16_t *__restrict__ list_len,
+                                                   uint16_t *__restrict__ list_len, int32_t list_cap,
                                                    unsigned long long *__restrict__ stats,
                                                    uint32_t *__restrict__ err) {
     extern __shared__ __align__(16) uint8_t smem[];
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(256) k_gen_lists(DevDB db, const int32_t *__re
     const int32_t words = (nbins + 31) / 32;
     uint32_t *planes = reinterpret_cast<uint32_t *>(smem) + (size_t)warp * 3 * words;
     uint16_t *list = reinterpret_cast<uint16_t *>(reinterpret_cast<uint32_t *>(smem) + (size_t)nw * 3 * words) +
-                     (size_t)warp * kMaxListLen;
+                     (size_t)warp * list_cap;
     __shared__ unsigned long long s_stats[2];
     if (threadIdx.x < 2) s_stats[threadIdx.x] = 0ull;
     for (int32_t i = lane; i < 3 * words; i += 32) planes[i] = 0u;
@@ -199,10 +199,10 @@ __global__ void __launch_bounds__(256) k_gen_lists(DevDB db, const int32_t *__re
             }
             if (!((need >> (z - 1)) & 1u)) continue;
             const WordRange use = all.hi > all.lo ? all : WordRange{0, 0};
-            int n = compact_planes(pl, use, z == zmax, list, kMaxListLen);
-            if (n > kMaxListLen) {
+            int n = compact_planes(pl, use, z == zmax, list, list_cap);
+            if (n > list_cap) {
                 if (lane == 0) atomicOr(err, kErrListOverflow);
-                n = kMaxListLen;
+                n = list_cap;
             }
             const uint64_t off = list_offset(lstart, total10, z, p);
             for (int i = lane; i < n; i += 32) lists[off + i] = list[i];
@@ -661,11 +661,13 @@ int hfx_lists_mark(const SpecMeta *meta, const uint32_t *wb, const uint32_t *we,
 }
 
 int hfx_lists_generate(const DevDB &db, const int32_t *cover, int64_t npep1, int32_t nbins, const uint32_t *lstart,
-                       uint64_t total10, uint16_t *lists, uint16_t *list_len, int fastdiv, unsigned long long *stats,
-                       uint32_t *err, cudaStream_t st) {
+                       uint64_t total10, uint16_t *lists, uint16_t *list_len, int32_t list_cap, int fastdiv,
+                       unsigned long long *stats, uint32_t *err, cudaStream_t st) {
     const int nw = 8;
     const int32_t words = (nbins + 31) / 32;
-    const size_t smem = (size_t)nw * 3 * words * 4 + (size_t)nw * kMaxListLen * 2;
+    list_cap = std::max(32, std::min(list_cap, kMaxListLen));
+    // per warp: three bit planes and a staging list of list_cap entries
+    const size_t smem = (size_t)nw * 3 * words * 4 + (size_t)nw * list_cap * 2;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -674,7 +676,7 @@ int hfx_lists_generate(const DevDB &db, const int32_t *cover, int64_t npep1, int
     int per = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, nw * 32, smem);
     f<<<sms * (per > 0 ? per : 1), nw * 32, smem, st>>>(db, cover, npep1, nbins, lstart, total10, lists, list_len,
-                                                        stats, err);
+                                                        list_cap, stats, err);
     return (int)cudaGetLastError();
 }
 

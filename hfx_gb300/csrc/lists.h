@@ -18,8 +18,8 @@ int hfx_lists_mark(const hfx::SpecMeta *meta, const uint32_t *wb, const uint32_t
 // built, [1] list entries, [2] candidates scored, [3] entries streamed,
 // [4] peptide-spectrum pairs.
 int hfx_lists_generate(const hfx::DevDB &db, const int32_t *cover, int64_t npep1, int32_t nbins,
-                       const uint32_t *lstart, uint64_t total10, uint16_t *lists, uint16_t *list_len, int fastdiv,
-                       unsigned long long *stats, uint32_t *err, cudaStream_t st);
+                       const uint32_t *lstart, uint64_t total10, uint16_t *lists, uint16_t *list_len,
+                       int32_t list_cap, int fastdiv, unsigned long long *stats, uint32_t *err, cudaStream_t st);
 // Scorer over the lists; long_rows: 32-bit entries and group tiles read
 // from global memory (rows too long for shared memory), else 16-bit entries
 // and tiles staged in shared memory.
