@@ -342,6 +342,79 @@ template <> struct TileLoad<float, 8> {
     }
 };
 
+// acc[g] += weight(level) * tile[bin][g] for the G spectra of a group tile.
+// BF16/FP16 tiles use the mixed-precision FMA (fma.rn.f32.bf16 / .f16:
+// 16-bit multiplicands, FP32 addend and result).  The 16-bit weight and tile
+// value multiply exactly in FP32, so each step rounds once, exactly like
+// fmaf(weight, float(x), acc): bit-identical to the FP32 path, without the
+// conversions.
+__device__ __forceinline__ uint16_t level_weight_bf16(uint32_t lvl) {
+    return lvl == 3u ? (uint16_t)0x4248u : (lvl == 2u ? (uint16_t)0x41C8u : (uint16_t)0x4120u);  // 50, 25, 10
+}
+__device__ __forceinline__ uint16_t level_weight_f16(uint32_t lvl) {
+    return lvl == 3u ? (uint16_t)0x5240u : (lvl == 2u ? (uint16_t)0x4E40u : (uint16_t)0x4900u);  // 50, 25, 10
+}
+
+template <typename T, int G>
+struct TileFma {
+    __device__ __forceinline__ static void fma(const T *t, uint32_t bin, uint32_t lvl, float (&acc)[G]) {
+        const float w = level_weight(lvl);
+        float x[G];
+        TileLoad<T, G>::load(t, bin, x);
+#pragma unroll
+        for (int g = 0; g < G; ++g) acc[g] = __fmaf_rn(w, x[g], acc[g]);
+    }
+};
+
+#define HFX_MIXED_FMA8(TY)                                                                                      \
+    asm("{\n\t.reg .b16 l0, h0, l1, h1, l2, h2, l3, h3;\n\t"                                                   \
+        "mov.b32 {l0, h0}, %8;\n\tmov.b32 {l1, h1}, %9;\n\tmov.b32 {l2, h2}, %10;\n\tmov.b32 {l3, h3}, %11;\n\t" \
+        "fma.rn.f32." TY " %0, %12, l0, %0;\n\tfma.rn.f32." TY " %1, %12, h0, %1;\n\t"                          \
+        "fma.rn.f32." TY " %2, %12, l1, %2;\n\tfma.rn.f32." TY " %3, %12, h1, %3;\n\t"                          \
+        "fma.rn.f32." TY " %4, %12, l2, %4;\n\tfma.rn.f32." TY " %5, %12, h2, %5;\n\t"                          \
+        "fma.rn.f32." TY " %6, %12, l3, %6;\n\tfma.rn.f32." TY " %7, %12, h3, %7;\n\t}"                          \
+        : "+f"(acc[0]), "+f"(acc[1]), "+f"(acc[2]), "+f"(acc[3]), "+f"(acc[4]), "+f"(acc[5]), "+f"(acc[6]),    \
+          "+f"(acc[7])                                                                                          \
+        : "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w), "h"(w))
+#define HFX_MIXED_FMA4(TY)                                                                                      \
+    asm("{\n\t.reg .b16 l0, h0, l1, h1;\n\t"                                                                   \
+        "mov.b32 {l0, h0}, %4;\n\tmov.b32 {l1, h1}, %5;\n\t"                                                    \
+        "fma.rn.f32." TY " %0, %6, l0, %0;\n\tfma.rn.f32." TY " %1, %6, h0, %1;\n\t"                            \
+        "fma.rn.f32." TY " %2, %6, l1, %2;\n\tfma.rn.f32." TY " %3, %6, h1, %3;\n\t}"                            \
+        : "+f"(acc[0]), "+f"(acc[1]), "+f"(acc[2]), "+f"(acc[3])                                                \
+        : "r"(v.x), "r"(v.y), "h"(w))
+
+template <> struct TileFma<__nv_bfloat16, 8> {
+    __device__ __forceinline__ static void fma(const __nv_bfloat16 *t, uint32_t bin, uint32_t lvl, float (&acc)[8]) {
+        const uint4 v = *reinterpret_cast<const uint4 *>(t + (size_t)bin * 8);
+        const uint16_t w = level_weight_bf16(lvl);
+        HFX_MIXED_FMA8("bf16");
+    }
+};
+template <> struct TileFma<__half, 8> {
+    __device__ __forceinline__ static void fma(const __half *t, uint32_t bin, uint32_t lvl, float (&acc)[8]) {
+        const uint4 v = *reinterpret_cast<const uint4 *>(t + (size_t)bin * 8);
+        const uint16_t w = level_weight_f16(lvl);
+        HFX_MIXED_FMA8("f16");
+    }
+};
+template <> struct TileFma<__nv_bfloat16, 4> {
+    __device__ __forceinline__ static void fma(const __nv_bfloat16 *t, uint32_t bin, uint32_t lvl, float (&acc)[4]) {
+        const uint2 v = *reinterpret_cast<const uint2 *>(t + (size_t)bin * 4);
+        const uint16_t w = level_weight_bf16(lvl);
+        HFX_MIXED_FMA4("bf16");
+    }
+};
+template <> struct TileFma<__half, 4> {
+    __device__ __forceinline__ static void fma(const __half *t, uint32_t bin, uint32_t lvl, float (&acc)[4]) {
+        const uint2 v = *reinterpret_cast<const uint2 *>(t + (size_t)bin * 4);
+        const uint16_t w = level_weight_f16(lvl);
+        HFX_MIXED_FMA4("f16");
+    }
+};
+#undef HFX_MIXED_FMA8
+#undef HFX_MIXED_FMA4
+
 template <typename T, int G>
 struct TileDot {
     const T *tile;
@@ -349,11 +422,7 @@ struct TileDot {
         const int lane = threadIdx.x & 31;
         for (int i = lane; i < n; i += 32) {
             const uint32_t e = list[i];
-            const float w = level_weight(e & 3u);
-            float x[G];
-            TileLoad<T, G>::load(tile, e >> 2, x);
-#pragma unroll
-            for (int g = 0; g < G; ++g) acc[g] = __fmaf_rn(w, x[g], acc[g]);
+            TileFma<T, G>::fma(tile, e >> 2, e & 3u, acc);
         }
     }
 };

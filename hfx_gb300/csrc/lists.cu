@@ -597,13 +597,7 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const uint32_t bin = e[k] >> 2;
-                    if ((int32_t)bin < nb) {
-                        const float w = level_weight(e[k] & 3u);
-                        float x[G];
-                        TileLoad<T, G>::load(tile, bin, x);
-#pragma unroll
-                        for (int j = 0; j < G; ++j) acc[j] = __fmaf_rn(w, x[j], acc[j]);
-                    }
+                    if ((int32_t)bin < nb) TileFma<T, G>::fma(tile, bin, e[k] & 3u, acc);
                 }
             }
             const float sc = reduce_scatter<G>(acc);
