@@ -60,6 +60,7 @@ class SearchParams(C.Structure):
         ("chunk", C.c_int32),
         ("max_len", C.c_int32),
         ("ion_bins_custom", C.c_int32),
+        ("use_graph", C.c_int32),
     ]
 
 

@@ -499,6 +499,24 @@ int hfx_batched_score(const DevDB &db, const void *rows, int elem_kind, int64_t 
     }
 }
 
+// Graph replays size the work-item buffers from an earlier run: clamp the
+// item offsets to that capacity and report an overflow (the host re-plans).
+__global__ void k_clamp_items(uint32_t *__restrict__ off, int64_t n1, uint32_t cap, uint32_t *__restrict__ err) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n1) return;
+    const uint32_t v = off[i];
+    if (v > cap) {
+        off[i] = cap;
+        if (i == n1 - 1) atomicOr(err, kErrBounds);
+    }
+}
+
+int hfx_clamp_items(uint32_t *off, int64_t n1, uint32_t cap, uint32_t *err, cudaStream_t st) {
+    if (n1 <= 0) return 0;
+    k_clamp_items<<<(unsigned)((n1 + 255) / 256), 256, 0, st>>>(off, n1, cap, err);
+    return (int)cudaGetLastError();
+}
+
 int hfx_batched_merge(const float *part_s, const uint64_t *part_k, const BatchedWs &ws, const SpecMeta *meta,
                       int32_t nspec, int32_t G, int32_t K, int32_t kout, float *out_s, uint64_t *out_k,
                       cudaStream_t st) {

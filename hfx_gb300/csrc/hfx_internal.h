@@ -17,6 +17,7 @@ struct LayoutParams {
     int32_t remove_pcr; // remove-precursor-peak (Correlation.hs:69-71)
     int32_t ppm;        // 0 Da, 1 ppm, 2 per spectrum: negative = ppm (new; the reference has Da only)
     int32_t max_len;    // longest row accepted
+    int32_t flag_long;  // 1: a longer row sets kErrTooLong (graph replays with a fixed row stride)
 };
 
 // Per-spectrum metadata computed on the device (k_layout).
@@ -59,7 +60,7 @@ enum : uint32_t {
 
 int hfx_launch_layout(const float *mz, const int64_t *off, const float *pcr, const float *z,
                       const float *tol, int32_t nspec, const hfx::LayoutParams &lp,
-                      hfx::SpecMeta *meta, uint32_t *max_len, cudaStream_t st);
+                      hfx::SpecMeta *meta, uint32_t *max_len, uint32_t *err, cudaStream_t st);
 int hfx_launch_preprocess(const float *mz, const float *it, const int64_t *off, const float *pcr,
                           const hfx::LayoutParams &lp, const hfx::SpecMeta *meta, int32_t nspec,
                           int64_t stride, float *out32, __nv_bfloat16 *outbf, __half *outh, uint32_t *err,

@@ -107,15 +107,36 @@ struct hfx_ctx {
     int64_t stage_units[HFX_NSTAGES] = {0};
 
     void stage_begin(int s) {
-        if (!profile) return;
+        if (!profile || gmode == 2) return;
         if (!ev[s][0]) { cudaEventCreate(&ev[s][0]); cudaEventCreate(&ev[s][1]); }
         cudaEventRecord(ev[s][0], stream);
     }
+    // CUDA-graph replay (params.use_graph): 0 eager, 1 eager with buffers
+    // sized to the capacities, 2 capturing (no host synchronisation; sizes
+    // from the capacities; device-side overflow checks)
+    int gmode = 0;
+    int64_t cap_stride = 0;
+    uint32_t cap_groups = 0, cap_items = 0, cap_mitems = 0;
+    int64_t last_stride = 0;
+    uint32_t last_items = 0, last_mitems = 0;
+    bool graph_valid = false;
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaStream_t graph_stream = nullptr;  // captures and replays run here (never the legacy stream)
+    cudaEvent_t graph_event = nullptr;
+    std::vector<uint8_t> graph_key;
+    void graph_reset() {
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        graph_exec = nullptr;
+        graph_valid = false;
+        graph_key.clear();
+    }
+
     // HFX_DEBUG_SYNC=1: synchronize after every stage and remember the first
     // stage whose kernels reported an error (for locating device faults)
     bool debug_sync = false;
     std::string fault_stage;
     void stage_end(int s, int64_t launches, int64_t units = 0) {
+        if (gmode == 2) return;
         stage_launches[s] += launches;
         stage_units[s] += units;
         if (debug_sync && fault_stage.empty()) {
@@ -200,6 +221,7 @@ void pack_ions(const std::vector<uint8_t> &ascii, const uint8_t *ma, int num_ma,
 }
 
 int32_t upload_db(hfx_ctx *ctx) {
+    ctx->graph_reset();
     const uint64_t np = ctx->num_pep;
     ctx->h_idx.resize(np);
     std::iota(ctx->h_idx.begin(), ctx->h_idx.end(), 0u);
@@ -290,6 +312,7 @@ LayoutParams layout_params(const hfx_search_params *p) {
     lp.remove_pcr = p->remove_precursor_peak;
     lp.ppm = p->tol_ppm;
     lp.max_len = p->max_len > 0 ? p->max_len : kDefaultMaxLen;
+    lp.flag_long = 0;
     return lp;
 }
 
@@ -298,21 +321,32 @@ int32_t run_stage_a(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, in
                     SpecMeta *&meta, float *&rows, __nv_bfloat16 *&rows_bf, __half *&rows_h, bool want_bf,
                     bool want_h) {
     cudaError_t e;
-    const LayoutParams lp = layout_params(p);
+    LayoutParams lp = layout_params(p);
+    if (ctx->gmode >= 1) {
+        // graph replays keep the row stride of the capture: longer rows are errors
+        lp.max_len = (int32_t)std::min<int64_t>(lp.max_len, ctx->cap_stride);
+        lp.flag_long = 1;
+    }
     meta = ctx->buf<SpecMeta>("meta", b.nspec, e);
     if (e) return cuda_fail(ctx, e, "alloc meta");
     uint32_t *d_max = ctx->buf<uint32_t>("maxlen", 4, e);
     if (e) return cuda_fail(ctx, e, "alloc maxlen");
     HFX_CUDA(cudaMemsetAsync(d_max, 0, 4, ctx->stream), "memset");
     ctx->stage_begin(HFX_STAGE_LAYOUT);
-    int rc = hfx_launch_layout(b.mz, b.off, b.pcr, b.z, b.tol, b.nspec, lp, meta, d_max, ctx->stream);
+    int rc = hfx_launch_layout(b.mz, b.off, b.pcr, b.z, b.tol, b.nspec, lp, meta, d_max, ctx->d_err.as<uint32_t>(),
+                               ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_layout");
     ctx->stage_end(HFX_STAGE_LAYOUT, 1, b.nspec);
-    uint32_t maxlen = 0;
-    HFX_CUDA(cudaMemcpyAsync(&maxlen, d_max, 4, cudaMemcpyDeviceToHost, ctx->stream), "D2H maxlen");
-    HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
-    if (maxlen == 0) maxlen = 16;
-    stride = ((int64_t)maxlen + 15) & ~(int64_t)15;
+    if (ctx->gmode >= 1) {
+        stride = ctx->cap_stride;
+    } else {
+        uint32_t maxlen = 0;
+        HFX_CUDA(cudaMemcpyAsync(&maxlen, d_max, 4, cudaMemcpyDeviceToHost, ctx->stream), "D2H maxlen");
+        HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+        if (maxlen == 0) maxlen = 16;
+        stride = ((int64_t)maxlen + 15) & ~(int64_t)15;
+        ctx->last_stride = stride;
+    }
     rows = ctx->buf<float>("rows32", (size_t)b.nspec * stride, e);
     if (e) return cuda_fail(ctx, e, "alloc rows");
     rows_bf = nullptr;
@@ -450,11 +484,21 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     rc = hfx_batched_plan(meta, ns, wb, we, G, chunk, ws, ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "plan");
     ctx->stage_end(HFX_STAGE_WINDOWS, 6, ns);  // k_windows + 5 planning kernels
-    uint32_t hs[4];
-    HFX_CUDA(cudaMemcpyAsync(hs, scal, 16, cudaMemcpyDeviceToHost, ctx->stream), "D2H plan");
-    HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
-    const uint32_t ngroups = hs[1];
-    const uint32_t total_items = hs[2];
+    uint32_t ngroups = 0, total_items = 0;
+    if (ctx->gmode >= 1) {
+        // capacities of the graph; a batch that needs more is reported (k_clamp_items)
+        ngroups = ctx->cap_groups;
+        total_items = ctx->cap_items;
+        rc = hfx_clamp_items(ws.item_off, (int64_t)ns + 1, total_items, ctx->d_err.as<uint32_t>(), ctx->stream);
+        if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_clamp_items");
+    } else {
+        uint32_t hs[4];
+        HFX_CUDA(cudaMemcpyAsync(hs, scal, 16, cudaMemcpyDeviceToHost, ctx->stream), "D2H plan");
+        HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+        ngroups = hs[1];
+        total_items = hs[2];
+        ctx->last_items = total_items;
+    }
     const size_t esz = elem_kind == 0 ? 4 : 2;
     void *tiles = ctx->buf<uint8_t>("tiles", (size_t)ngroups * stride * G * esz + 64, e);
     if (e) return cuda_fail(ctx, e, "alloc tiles");
@@ -568,9 +612,16 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
                                     ctx->stream);
         if (rc) return cuda_fail(ctx, (cudaError_t)rc, "modification plan");
         uint32_t mtotal = 0;
-        if (n_gm > 0) {
+        if (ctx->gmode >= 1) {
+            mtotal = ctx->cap_mitems;
+            if (n_gm > 0) {
+                rc = hfx_clamp_items(mitem_off, (int64_t)n_gm + 1, mtotal, ctx->d_err.as<uint32_t>(), ctx->stream);
+                if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_clamp_items");
+            }
+        } else if (n_gm > 0) {
             HFX_CUDA(cudaMemcpyAsync(&mtotal, mitem_off + n_gm, 4, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
             HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+            ctx->last_mitems = mtotal;
         }
         ms = ctx->buf<float>("m_part_s", (size_t)mtotal * G * K + 1, e);
         if (e) return cuda_fail(ctx, e, "alloc mod parts");
@@ -620,13 +671,11 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     return HFX_OK;
 }
 
-int32_t search_device(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, float *out_s, uint64_t *out_k,
-                      uint32_t *out_pep, int64_t *out_ncand) {
-    int32_t rc = check_params(ctx, p);
-    if (rc) return rc;
-    if (b.nspec <= 0) return HFX_OK;
-    HFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
-    HFX_CUDA(ctx->d_err.ensure(16), "alloc err");
+// Everything a search enqueues, from clearing the error word to the last
+// kernel; in gmode 2 this is what the CUDA graph captures.
+int32_t search_enqueue(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, float *out_s, uint64_t *out_k,
+                       uint32_t *out_pep, int64_t *out_ncand) {
+    int32_t rc = 0;
     HFX_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, 4, ctx->stream), "memset err");
     int64_t stride = 0;
     SpecMeta *meta = nullptr;
@@ -645,14 +694,114 @@ int32_t search_device(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, 
         return fail(ctx, HFX_ERR_UNSUPPORTED, "per-spectrum launches use FP32 rows only");
     else
         rc = search_plain_per_spectrum(ctx, p, b, meta, rows, stride, out_s, out_k, out_pep, out_ncand);
-    if (rc) return rc;
+    return rc;
+}
+
+// Waits for the search and turns the device error word into a status.
+int32_t search_finish(hfx_ctx *ctx, uint32_t *herr_out = nullptr) {
     uint32_t herr = 0;
     HFX_CUDA(cudaMemcpyAsync(&herr, ctx->d_err.p, 4, cudaMemcpyDeviceToHost, ctx->stream), "D2H err");
     HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
     ctx->stage_collect();
+    if (herr_out) *herr_out = herr;
     if (herr & kErrTimeout) return fail(ctx, HFX_ERR_TIMEOUT, "device wait timed out");
     if (herr) return fail(ctx, HFX_ERR_UNSUPPORTED, "device error word " + std::to_string(herr));
     return HFX_OK;
+}
+
+// CUDA-graph search: the first call for a batch shape runs eagerly to learn
+// the sizes, again with buffers at 1.25x those sizes, and then captures the
+// whole enqueue sequence (no host synchronisation inside) into a graph;
+// later calls with the same shape, buffers and parameters replay it.  A
+// replay whose batch needs more than the capacities is reported on the
+// device (row stride, work items) and re-planned eagerly.
+int32_t search_graph(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, float *out_s, uint64_t *out_k,
+                     uint32_t *out_pep, int64_t *out_ncand) {
+    std::vector<uint8_t> key(sizeof(hfx_search_params) + sizeof(Batch) + 4 * sizeof(void *));
+    uint8_t *kp = key.data();
+    std::memcpy(kp, p, sizeof(hfx_search_params));
+    kp += sizeof(hfx_search_params);
+    std::memcpy(kp, &b, sizeof(Batch));
+    kp += sizeof(Batch);
+    const void *outs[4] = {out_s, out_k, out_pep, out_ncand};
+    std::memcpy(kp, outs, sizeof(outs));
+    // all graph work runs on the context's own graph stream, after the work
+    // already queued on the caller's stream
+    if (!ctx->graph_stream) {
+        HFX_CUDA(cudaStreamCreateWithFlags(&ctx->graph_stream, cudaStreamNonBlocking), "graph stream");
+        HFX_CUDA(cudaEventCreateWithFlags(&ctx->graph_event, cudaEventDisableTiming), "graph event");
+    }
+    HFX_CUDA(cudaEventRecord(ctx->graph_event, ctx->stream), "event");
+    HFX_CUDA(cudaStreamWaitEvent(ctx->graph_stream, ctx->graph_event, 0), "wait event");
+    struct StreamSwap {
+        hfx_ctx *c;
+        cudaStream_t saved;
+        explicit StreamSwap(hfx_ctx *c_) : c(c_), saved(c_->stream) { c->stream = c->graph_stream; }
+        ~StreamSwap() { c->stream = saved; }
+    } swap(ctx);
+    if (ctx->graph_valid && key == ctx->graph_key) {
+        HFX_CUDA(cudaGraphLaunch(ctx->graph_exec, ctx->stream), "cudaGraphLaunch");
+        uint32_t herr = 0;
+        const int32_t rc = search_finish(ctx, &herr);
+        if (!(herr & (kErrBounds | kErrTooLong))) return rc;
+    }
+    ctx->graph_reset();  // no graph yet, another shape, or the batch outgrew the capture
+    const bool prof = ctx->profile;
+    ctx->profile = false;
+    auto restore = [&](int32_t rc) {
+        ctx->gmode = 0;
+        ctx->profile = prof;
+        return rc;
+    };
+    ctx->gmode = 0;
+    int32_t rc = search_enqueue(ctx, p, b, out_s, out_k, out_pep, out_ncand);
+    if (!rc) rc = search_finish(ctx);
+    if (rc) return restore(rc);
+    const int32_t G = p->group_size > 0 ? p->group_size : (p->precision == 0 ? 4 : 8);
+    ctx->cap_stride = ctx->last_stride;
+    ctx->cap_groups = (uint32_t)((b.nspec + G - 1) / G + 24);  // <= one partial group per class
+    ctx->cap_items = ctx->last_items + ctx->last_items / 4 + 64;
+    ctx->cap_mitems = ctx->last_mitems + ctx->last_mitems / 4 + 64;
+    ctx->gmode = 1;
+    rc = search_enqueue(ctx, p, b, out_s, out_k, out_pep, out_ncand);
+    if (!rc) rc = search_finish(ctx);
+    if (rc) return restore(rc);
+    ctx->gmode = 2;
+    cudaGraph_t graph = nullptr;
+    HFX_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed), "capture");
+    rc = search_enqueue(ctx, p, b, out_s, out_k, out_pep, out_ncand);
+    const cudaError_t ec = cudaStreamEndCapture(ctx->stream, &graph);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return restore(rc);
+    }
+    if (ec != cudaSuccess) return restore(cuda_fail(ctx, ec, "cudaStreamEndCapture"));
+    const cudaError_t ei = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+        ctx->graph_exec = nullptr;
+        return restore(cuda_fail(ctx, ei, "cudaGraphInstantiate"));
+    }
+    ctx->graph_valid = true;
+    ctx->graph_key = key;
+    return restore(HFX_OK);
+}
+
+int32_t search_device(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, float *out_s, uint64_t *out_k,
+                      uint32_t *out_pep, int64_t *out_ncand) {
+    int32_t rc = check_params(ctx, p);
+    if (rc) return rc;
+    if (b.nspec <= 0) return HFX_OK;
+    HFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    HFX_CUDA(ctx->d_err.ensure(16), "alloc err");
+    if (p->use_graph) {
+        if (!p->batch_mode && !(p->search_mods && ctx->num_mod > 0))
+            return fail(ctx, HFX_ERR_UNSUPPORTED, "graph replay needs a batched mode (batch_mode 1 or 2)");
+        return search_graph(ctx, p, b, out_s, out_k, out_pep, out_ncand);
+    }
+    rc = search_enqueue(ctx, p, b, out_s, out_k, out_pep, out_ncand);
+    if (rc) return rc;
+    return search_finish(ctx);
 }
 
 }  // namespace
@@ -676,6 +825,7 @@ void hfx_default_params(hfx_search_params *p) {
     p->chunk = 0;
     p->max_len = 0;
     p->ion_bins_custom = 0;
+    p->use_graph = 0;
 }
 
 int32_t hfx_ctx_create(int32_t device, hfx_ctx **out) {
@@ -700,6 +850,12 @@ int32_t hfx_ctx_destroy(hfx_ctx *ctx) {
     if (!ctx) return HFX_ERR_ARG;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    ctx->graph_reset();
+    if (ctx->graph_stream) {
+        cudaStreamSynchronize(ctx->graph_stream);
+        cudaStreamDestroy(ctx->graph_stream);
+    }
+    if (ctx->graph_event) cudaEventDestroy(ctx->graph_event);
     for (auto &kv : ctx->ws) kv.second.release();
     ctx->d_ions.release();
     ctx->d_r.release();
@@ -880,6 +1036,7 @@ int32_t hfx_set_mods(hfx_ctx *ctx, int32_t num_ma, const uint8_t *ma, const floa
                      int32_t per_type) {
     if (!ctx || num_ma < 0 || num_ma > 7 || (num_ma > 0 && (!ma || !ma_mass)))
         return fail(ctx, HFX_ERR_ARG, "num_ma must be 0..7 (3-bit field, utils.h:97)");
+    ctx->graph_reset();
     ctx->num_ma = num_ma;
     ctx->max_ma = max_ma;
     ctx->per_type = per_type;
@@ -977,7 +1134,7 @@ int32_t hfx_preprocess(hfx_ctx *ctx, const hfx_search_params *p, const float *mz
     float *tol = ctx->buf<float>("tol0", nspec, e);
     if (e) return cuda_fail(ctx, e, "alloc");
     HFX_CUDA(cudaMemsetAsync(tol, 0, 4ull * nspec, ctx->stream), "memset");
-    int rc = hfx_launch_layout(mz, off, pcr, z, tol, nspec, lp, meta, d_max, ctx->stream);
+    int rc = hfx_launch_layout(mz, off, pcr, z, tol, nspec, lp, meta, d_max, nullptr, ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_layout");
     HFX_CUDA(ctx->d_err.ensure(16), "alloc err");
     HFX_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, 4, ctx->stream), "memset err");
@@ -1010,7 +1167,7 @@ int32_t hfx_find_windows(hfx_ctx *ctx, const hfx_search_params *p, const float *
     if (e) return cuda_fail(ctx, e, "alloc");
     uint32_t *d_max = ctx->buf<uint32_t>("maxlen", 4, e);
     if (e) return cuda_fail(ctx, e, "alloc");
-    int rc = hfx_launch_layout(mz, off, pcr, z, tol, nspec, lp, meta, d_max, ctx->stream);
+    int rc = hfx_launch_layout(mz, off, pcr, z, tol, nspec, lp, meta, d_max, nullptr, ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_layout");
     rc = hfx_launch_windows(ctx->d_r.as<float>(), (uint32_t)ctx->num_pep, meta, nspec, begin, end, ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_windows");

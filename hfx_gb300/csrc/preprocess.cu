@@ -30,7 +30,7 @@ __device__ __forceinline__ float spec_cutoff(float last_mz, float pcr, float z) 
 __global__ void k_layout(const float *__restrict__ mz, const int64_t *__restrict__ off,
                          const float *__restrict__ pcr, const float *__restrict__ z,
                          const float *__restrict__ tol, int32_t nspec, LayoutParams lp,
-                         SpecMeta *__restrict__ meta, uint32_t *__restrict__ max_len) {
+                         SpecMeta *__restrict__ meta, uint32_t *__restrict__ max_len, uint32_t *__restrict__ err) {
     const int32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nspec) return;
     SpecMeta m;
@@ -47,6 +47,7 @@ __global__ void k_layout(const float *__restrict__ mz, const int64_t *__restrict
         const float c = lp.custom_bw ? __fdiv_rn(m.cutoff, lp.bw) : m.cutoff;
         const double len = 75.0 + ceil((double)c);
         if (!(len >= 76.0) || len > (double)lp.max_len) {
+            if (lp.flag_long && len > (double)lp.max_len && err) atomicOr(err, kErrTooLong);
             m.status = 2;
         } else {
             m.len = (int32_t)len;
@@ -349,9 +350,9 @@ using namespace hfx;
 
 int hfx_launch_layout(const float *mz, const int64_t *off, const float *pcr, const float *z,
                       const float *tol, int32_t nspec, const LayoutParams &lp, SpecMeta *meta,
-                      uint32_t *max_len, cudaStream_t st) {
+                      uint32_t *max_len, uint32_t *err, cudaStream_t st) {
     if (nspec <= 0) return 0;
-    k_layout<<<(nspec + 127) / 128, 128, 0, st>>>(mz, off, pcr, z, tol, nspec, lp, meta, max_len);
+    k_layout<<<(nspec + 127) / 128, 128, 0, st>>>(mz, off, pcr, z, tol, nspec, lp, meta, max_len, err);
     return (int)cudaGetLastError();
 }
 

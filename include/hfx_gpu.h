@@ -51,6 +51,8 @@ typedef struct hfx_search_params {
     int32_t ion_bins_custom;       /* 1: ion bins use bin_width too (new; the reference bins
                                       ions with the mono width, ion_series.cu:68); rows longer
                                       than 8,192 bins only                                     */
+    int32_t use_graph;             /* 1: replay the search as one CUDA graph while the batch
+                                      shape, buffers and parameters repeat (batched modes)     */
 } hfx_search_params;
 
 /* Fill p with the engine defaults (reference behaviour where it has one). */

@@ -299,3 +299,26 @@ def test_custom_ion_width_needs_long_rows(tiny_engine):
     eng, prot, sp = tiny_engine
     with pytest.raises(hfx_gb300.HfxError):
         eng.search(sp.subset(np.arange(4)), hfx_gb300.default_params(ion_bins_custom=1, batch_mode=1))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_graph_replay_matches_eager(full_engine, oracle, precision):
+    """use_graph: the first call plans and captures, later calls replay the
+    CUDA graph.  A second batch of the same shape replays the same graph (or
+    re-plans if it needs more work items); every result equals the eager
+    search's."""
+    import hfx_gb300
+    eng, prot, sp = full_engine
+    a = sp.subset(np.arange(0, 120))
+    b = sp.subset(np.arange(120, 240))
+    pe = hfx_gb300.default_params(top_n=10, batch_mode=1, precision=precision)
+    pg = hfx_gb300.default_params(top_n=10, batch_mode=1, precision=precision, use_graph=1)
+    ra, rb = eng.search(a, pe), eng.search(b, pe)
+    for rep in range(3):
+        for sub, ref in ((a, ra), (b, rb)):
+            res = eng.search(sub, pg)
+            assert np.array_equal(res.key, ref.key), rep
+            assert np.array_equal(res.score.view(np.uint32), ref.score.view(np.uint32)), rep
+            assert np.array_equal(res.ncand, ref.ncand), rep
+    # the graph path is still the oracle's search
+    _compare(eng.search(a, pg), oracle.search(*_oracle_db(oracle, eng, prot), a, topn=10), "graph")
