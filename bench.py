@@ -72,6 +72,9 @@ def _args():
     ap.add_argument("--out", default="")
     ap.add_argument("--group-size", type=int, default=0, help="spectra per batched work item (0 = default)")
     ap.add_argument("--chunk", type=int, default=0, help="candidates per batched work item (0 = default)")
+    ap.add_argument("--no-graph", action="store_true", help="eager launches instead of CUDA-graph replays")
+    ap.add_argument("--tune", default="auto", choices=["auto", "on", "off"],
+                    help="hfx_autotune of group size and work-item size before the warm-up (auto: 'full' only)")
     return ap.parse_args()
 
 
@@ -317,8 +320,13 @@ def main():
     prec, mode = a.precision, a.batch_mode
     cpu_n, agree_n, plain_n = _samples(a)
     a.cpu_sample, a.agree_sample = cpu_n, agree_n
+    graph = int(mode != 0 and not a.no_graph)
     p = hfx_gb300.default_params(top_n=cfg["top_n"], precision=prec, batch_mode=mode, rescore_k=32 if prec else 0,
-                                 group_size=a.group_size, chunk=a.chunk, **_pkw(cfg))
+                                 group_size=a.group_size, chunk=a.chunk, use_graph=graph, **_pkw(cfg))
+    # stage events and work counters need the eager launches
+    p_prof = hfx_gb300.default_params(top_n=cfg["top_n"], precision=prec, batch_mode=mode,
+                                      rescore_k=32 if prec else 0, group_size=a.group_size, chunk=a.chunk,
+                                      **_pkw(cfg))
     d = torch.device("cuda", local)
     dev = dict(mz=torch.from_numpy(sp.mz).to(d), it=torch.from_numpy(sp.it).to(d),
                off=torch.from_numpy(sp.off).to(d), pcr=torch.from_numpy(sp.pcr).to(d),
@@ -332,6 +340,12 @@ def main():
                     ncand=torch.empty(ns, dtype=torch.int64, device=d))
     out = outputs()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=d)
+    tuned = None
+    if mode != 0 and a.group_size == 0 and a.chunk == 0 and (
+            a.tune == "on" or (a.tune == "auto" and a.workload in ("full", "tiny"))):
+        ms_t = eng.autotune(dev, p, out, reps=2)
+        p_prof.group_size, p_prof.chunk = p.group_size, p.chunk
+        tuned = {"group_size": p.group_size, "chunk": p.chunk, "ms": ms_t}
     for _ in range(a.warmup):
         eng.search_device(dev, p, out)
     torch.cuda.synchronize()
@@ -353,7 +367,7 @@ def main():
     eng.set_profiling(True)
     eng.stage_stats(reset=True)
     eng.counters(reset=True)
-    _timed(eng, dev, p, out, a.steps, flush, stream)
+    _timed(eng, dev, p_prof, out, a.steps, flush, stream)
     stats = eng.stage_stats(reset=True)
     work = {k: v // a.steps for k, v in eng.counters(reset=True).items()}
     eng.set_profiling(False)
@@ -462,6 +476,8 @@ def main():
                    "psm_per_step": psm_step,
                    "precision": ["fp32", "bf16 store + fp32 rescore", "fp16 store + fp32 rescore"][prec],
                    "batch_mode": ["per-spectrum launches", "batched over ion lists", "batched fused"][mode],
+                   "launch": "one CUDA-graph replay per step" if graph else "eager launches",
+                   "autotuned": tuned,
                    "l2": "flushed between timed steps (512 MB write)",
                    "stage_ms_per_step": {k: v[0] / a.steps for k, v in stats.items() if v[1]},
                    "work_per_step": work},

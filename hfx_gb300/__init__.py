@@ -28,7 +28,7 @@ BIN_WIDTH_AVG = 1.0011413
 
 EXPORTED = [
     "hfx_default_params", "hfx_ctx_create", "hfx_ctx_destroy", "hfx_set_stream",
-    "hfx_last_error", "hfx_build_db", "hfx_upload_db", "hfx_db_info", "hfx_db_export",
+    "hfx_last_error", "hfx_build_db", "hfx_upload_db", "hfx_db_info", "hfx_db_export", "hfx_autotune",
     "hfx_set_mods", "hfx_mod_table", "hfx_search_host", "hfx_search_device",
     "hfx_preprocess", "hfx_find_windows", "hfx_ion_bins", "hfx_mod_isoforms", "hfx_digest", "hfx_pack_ions",
     "hfx_set_profiling", "hfx_stage_stats", "hfx_search_counters",
@@ -91,6 +91,8 @@ def load_library(path: str = LIB_PATH):
         "hfx_mod_table": (i32, [P, C.POINTER(i32), P, P, i32]),
         "hfx_search_host": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, P, i32, P, P, P, P]),
         "hfx_search_device": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, P, i32, P, P, P, P]),
+        "hfx_autotune": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, P, i32, P, P, P, P, i32,
+                               C.POINTER(C.c_float)]),
         "hfx_preprocess": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, i32, C.c_int64, P, P, P, P, P]),
         "hfx_find_windows": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, i32, P, P]),
         "hfx_ion_bins": (i32, [P, P, P, P, i32, i32, i32, P, P, P]),
@@ -285,6 +287,16 @@ class Engine:
             self.h, C.byref(params), _ptr(dev["mz"]), _ptr(dev["it"]), _ptr(dev["off"]), _ptr(dev["pcr"]),
             _ptr(dev["z"]), _ptr(dev["tol"]), int(dev["pcr"].numel()), _ptr(out["score"]), _ptr(out["key"]),
             _ptr(out["pep"]), _ptr(out.get("ncand"))))
+
+    def autotune(self, dev, params: SearchParams, out, reps: int = 2):
+        """hfx_autotune: picks group_size and chunk for this batch (in place);
+        returns the best milliseconds per search."""
+        ms = C.c_float()
+        self._check(self.lib.hfx_autotune(
+            self.h, C.byref(params), _ptr(dev["mz"]), _ptr(dev["it"]), _ptr(dev["off"]), _ptr(dev["pcr"]),
+            _ptr(dev["z"]), _ptr(dev["tol"]), int(dev["pcr"].numel()), _ptr(out["score"]), _ptr(out["key"]),
+            _ptr(out["pep"]), _ptr(out.get("ncand")), reps, C.byref(ms)))
+        return ms.value
 
     def preprocess(self, dev, params: SearchParams, stride: int, rows, rows_bf16=None, rows_fp16=None,
                    lens=None, masses=None):

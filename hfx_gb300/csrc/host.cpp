@@ -1075,6 +1075,57 @@ int32_t hfx_search_device(hfx_ctx *ctx, const hfx_search_params *p, const float 
     return search_device(ctx, p, b, out_s, out_k, out_pep, out_ncand);
 }
 
+int32_t hfx_autotune(hfx_ctx *ctx, hfx_search_params *p, const float *mz, const float *it, const int64_t *off,
+                     const float *pcr, const float *z, const float *tol, int32_t nspec, float *out_s,
+                     uint64_t *out_k, uint32_t *out_pep, int64_t *out_ncand, int32_t reps, float *ms_out) {
+    if (!ctx || !p || nspec <= 0) return fail(ctx, HFX_ERR_ARG, "bad hfx_autotune arguments");
+    if (p->batch_mode == 0) return fail(ctx, HFX_ERR_ARG, "hfx_autotune tunes the batched modes");
+    HFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    Batch b{mz, it, pcr, z, tol, off, nspec};
+    hfx_search_params q = *p;
+    q.use_graph = 0;
+    // one 16-byte shared-memory load per bin: 8 BF16/FP16 or 4 FP32 spectra
+    // per group are the natural sizes; half of that is the alternative
+    const int32_t gs[2] = {p->precision == 0 ? 4 : 8, p->precision == 0 ? 2 : 4};
+    const int32_t chunks[5] = {1024, 2048, 4096, 8192, 16384};
+    cudaEvent_t e0, e1;
+    HFX_CUDA(cudaEventCreate(&e0), "event");
+    HFX_CUDA(cudaEventCreate(&e1), "event");
+    float best = 1e30f;
+    int32_t best_g = gs[0], best_c = chunks[2];
+    int32_t rc = HFX_OK;
+    for (int gi = 0; gi < 2 && rc == HFX_OK; ++gi) {
+        for (int ci = 0; ci < 5 && rc == HFX_OK; ++ci) {
+            q.group_size = gs[gi];
+            q.chunk = chunks[ci];
+            rc = search_device(ctx, &q, b, out_s, out_k, out_pep, out_ncand);
+            float tot = 0.0f;
+            for (int r = 0; r < std::max(1, reps) && rc == HFX_OK; ++r) {
+                cudaEventRecord(e0, ctx->stream);
+                rc = search_device(ctx, &q, b, out_s, out_k, out_pep, out_ncand);
+                cudaEventRecord(e1, ctx->stream);
+                cudaEventSynchronize(e1);
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                tot += ms;
+            }
+            const float avg = tot / std::max(1, reps);
+            if (rc == HFX_OK && avg < best) {
+                best = avg;
+                best_g = gs[gi];
+                best_c = chunks[ci];
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    p->group_size = best_g;
+    p->chunk = best_c;
+    if (ms_out) *ms_out = best;
+    return HFX_OK;
+}
+
 int32_t hfx_search_host(hfx_ctx *ctx, const hfx_search_params *p, const float *mz, const float *it,
                         const int64_t *off, const float *pcr, const float *z, const float *tol, int32_t nspec,
                         float *out_s, uint64_t *out_k, uint32_t *out_pep, int64_t *out_ncand) {

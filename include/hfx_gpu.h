@@ -147,6 +147,15 @@ int32_t hfx_search_device(hfx_ctx *ctx, const hfx_search_params *p, const float 
                           const int64_t *off, const float *pcr, const float *z, const float *tol,
                           int32_t nspec, float *out_score, uint64_t *out_key, uint32_t *out_pep,
                           int64_t *out_ncand);
+/* Autotuner (new): times the batched search of this batch (device buffers,
+ * as hfx_search_device) for each spectra-per-group size G and work-item
+ * size (candidates per item) it supports, `reps` timed runs each after one
+ * warm-up, and writes the fastest into p->group_size and p->chunk.  The
+ * outputs hold the last search's results.  ms_out (nullable) receives the
+ * best time per search. */
+int32_t hfx_autotune(hfx_ctx *ctx, hfx_search_params *p, const float *mz, const float *it, const int64_t *off,
+                     const float *pcr, const float *z, const float *tol, int32_t nspec, float *out_score,
+                     uint64_t *out_key, uint32_t *out_pep, int64_t *out_ncand, int32_t reps, float *ms_out);
 
 /* Stage (a) alone, device buffers: Correlation.hs:37-109 sequestXCorr.
  * rows[nspec][stride] FP32 (+ optional BF16 / FP16 copies), lens[nspec]

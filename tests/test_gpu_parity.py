@@ -322,3 +322,24 @@ def test_graph_replay_matches_eager(full_engine, oracle, precision):
             assert np.array_equal(res.ncand, ref.ncand), rep
     # the graph path is still the oracle's search
     _compare(eng.search(a, pg), oracle.search(*_oracle_db(oracle, eng, prot), a, topn=10), "graph")
+
+
+def test_autotune_picks_a_valid_shape(full_engine):
+    """hfx_autotune times the batched search over group and work-item sizes
+    and writes the fastest into the parameters; the tuned search returns the
+    same results as the default one."""
+    import hfx_gb300
+    eng, prot, sp = full_engine
+    sub = sp.subset(np.arange(120))
+    p = hfx_gb300.default_params(top_n=10, batch_mode=1, precision=1)
+    ref = eng.search(sub, p)
+    dev = _dev(sub)
+    out = dict(score=torch.empty((120, 10), dtype=torch.float32, device="cuda"),
+               key=torch.empty((120, 10), dtype=torch.int64, device="cuda"),
+               pep=torch.empty((120, 10), dtype=torch.int32, device="cuda"),
+               ncand=torch.empty(120, dtype=torch.int64, device="cuda"))
+    ms = eng.autotune(dev, p, out, reps=1)
+    assert ms > 0 and p.group_size in (4, 8) and p.chunk in (1024, 2048, 4096, 8192, 16384)
+    res = eng.search(sub, p)
+    assert np.array_equal(res.key, ref.key)
+    assert np.array_equal(res.score.view(np.uint32), ref.score.view(np.uint32))
