@@ -28,7 +28,8 @@ BIN_WIDTH_AVG = 1.0011413
 
 EXPORTED = [
     "hfx_default_params", "hfx_ctx_create", "hfx_ctx_destroy", "hfx_set_stream",
-    "hfx_last_error", "hfx_build_db", "hfx_upload_db", "hfx_db_info", "hfx_db_export", "hfx_autotune",
+    "hfx_last_error", "hfx_build_db", "hfx_upload_db", "hfx_db_info", "hfx_db_export", "hfx_autotune", "hfx_match_peptide",
+    "hfx_set_protein_segments",
     "hfx_set_mods", "hfx_mod_table", "hfx_search_host", "hfx_search_device",
     "hfx_preprocess", "hfx_find_windows", "hfx_ion_bins", "hfx_mod_isoforms", "hfx_digest", "hfx_pack_ions",
     "hfx_set_profiling", "hfx_stage_stats", "hfx_search_counters",
@@ -93,6 +94,9 @@ def load_library(path: str = LIB_PATH):
         "hfx_search_device": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, P, i32, P, P, P, P]),
         "hfx_autotune": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, P, i32, P, P, P, P, i32,
                                C.POINTER(C.c_float)]),
+        "hfx_match_peptide": (i32, [P, u64, C.c_uint32, C.c_char_p, i32, C.POINTER(C.c_float),
+                                    C.POINTER(i32)]),
+        "hfx_set_protein_segments": (i32, [P, P, i32]),
         "hfx_preprocess": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, i32, C.c_int64, P, P, P, P, P]),
         "hfx_find_windows": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, i32, P, P]),
         "hfx_ion_bins": (i32, [P, P, P, P, i32, i32, i32, P, P, P]),
@@ -287,6 +291,15 @@ class Engine:
             self.h, C.byref(params), _ptr(dev["mz"]), _ptr(dev["it"]), _ptr(dev["off"]), _ptr(dev["pcr"]),
             _ptr(dev["z"]), _ptr(dev["tol"]), int(dev["pcr"].numel()), _ptr(out["score"]), _ptr(out["key"]),
             _ptr(out["pep"]), _ptr(out.get("ncand"))))
+
+    def match(self, key: int, pep: int):
+        """hfx_match_peptide: (peptide text "X.PEPTIDE.Y" with '*' after
+        modified residues, (M+H)+, protein index) of one result entry."""
+        buf = C.create_string_buffer(512)
+        mh = C.c_float()
+        prot = C.c_int32()
+        self._check(self.lib.hfx_match_peptide(self.h, int(key), int(pep), buf, 512, C.byref(mh), C.byref(prot)))
+        return buf.value.decode(), mh.value, prot.value
 
     def autotune(self, dev, params: SearchParams, out, reps: int = 2):
         """hfx_autotune: picks group_size and chunk for this batch (in place);

@@ -84,6 +84,7 @@ struct hfx_ctx {
     unsigned long long counters[8] = {0};
     float mt[26] = {0};
     std::vector<uint8_t> h_ascii;
+    std::vector<uint32_t> h_seg;   // protein residue starts (+ end); one segment if unknown
     std::vector<float> h_r;        // fragment order
     std::vector<uint32_t> h_tc, h_tn;
     std::vector<uint32_t> h_idx;   // mass order -> fragment
@@ -990,6 +991,7 @@ int32_t hfx_build_db(hfx_ctx *ctx, const uint8_t *seq, const uint32_t *seg, int3
     if (nf < 0) return fail(ctx, HFX_ERR_ARG, "digest failed");
     if (nf >= (1ll << 27)) return fail(ctx, HFX_ERR_UNSUPPORTED, "more than 2^27 fragments");
     ctx->h_ascii.assign(seq, seq + nion);
+    ctx->h_seg.assign(seg, seg + nprot + 1);
     ctx->h_r.resize(nf);
     ctx->h_tc.resize(nf);
     ctx->h_tn.resize(nf);
@@ -1005,6 +1007,7 @@ int32_t hfx_upload_db(hfx_ctx *ctx, const uint8_t *ions, uint64_t num_ions, cons
     if (!ctx || !ions || !r || !tc || !tn || !mt26) return fail(ctx, HFX_ERR_ARG, "bad hfx_upload_db arguments");
     if (num_pep >= (1ull << 27)) return fail(ctx, HFX_ERR_UNSUPPORTED, "more than 2^27 fragments");
     ctx->h_ascii.assign(ions, ions + num_ions);
+    ctx->h_seg = {0u, (uint32_t)num_ions};
     ctx->h_r.assign(r, r + num_pep);
     ctx->h_tc.assign(tc, tc + num_pep);
     ctx->h_tn.assign(tn, tn + num_pep);
@@ -1073,6 +1076,87 @@ int32_t hfx_search_device(hfx_ctx *ctx, const hfx_search_params *p, const float 
     if (!ctx) return HFX_ERR_ARG;
     Batch b{mz, it, pcr, z, tol, off, nspec};
     return search_device(ctx, p, b, out_s, out_k, out_pep, out_ncand);
+}
+
+int32_t hfx_set_protein_segments(hfx_ctx *ctx, const uint32_t *seg, int32_t nprot) {
+    if (!ctx || !seg || nprot < 1 || seg[0] != 0 || seg[nprot] != ctx->h_ascii.size())
+        return fail(ctx, HFX_ERR_ARG, "segments must start at 0 and end at the residue count");
+    for (int32_t i = 0; i < nprot; ++i)
+        if (seg[i + 1] < seg[i]) return fail(ctx, HFX_ERR_ARG, "segments must ascend");
+    ctx->h_seg.assign(seg, seg + nprot + 1);
+    return HFX_OK;
+}
+
+int32_t hfx_match_peptide(hfx_ctx *ctx, uint64_t key, uint32_t pep, char *text, int32_t cap, float *mh,
+                          int32_t *protein) {
+    if (!ctx || !text || cap < 8) return fail(ctx, HFX_ERR_ARG, "bad hfx_match_peptide arguments");
+    if (pep >= ctx->num_pep) return fail(ctx, HFX_ERR_ARG, "fragment index out of range");
+    // Location.hs:42-58 lookup: the protein holding the fragment, its
+    // residues [c, n] (n itself unless it is the database's last residue),
+    // the flanking residues or '-', and (M+H)+ = residual + H + H2O
+    const uint32_t c = ctx->h_tc[pep], n = ctx->h_tn[pep];
+    const uint32_t nion = (uint32_t)ctx->h_ascii.size();
+    const size_t pi = (size_t)(std::upper_bound(ctx->h_seg.begin(), ctx->h_seg.end(), c) - ctx->h_seg.begin()) - 1;
+    const uint32_t a = ctx->h_seg[pi], b = ctx->h_seg[pi + 1];
+    const uint32_t ntake = n < nion ? n - c + 1 : n - c;
+    std::string s;
+    s.push_back(c > a ? (char)ctx->h_ascii[c - 1] : '-');
+    s.push_back('.');
+    for (uint32_t i = 0; i < ntake; ++i) s.push_back((char)ctx->h_ascii[c + i]);
+    s.push_back('.');
+    s.push_back(n + 1 < b ? (char)ctx->h_ascii[n + 1] : '-');
+    float mass = (ctx->h_r[pep] + kHostH) + kHostH2O;
+    if (key != ~0ull && (key >> 63)) {
+        // Fragment.hs:84-106 modifyFragment: mass + sum(count * mass), and a
+        // '*' after the i-th occurrence of each modified acid (i from the
+        // isoform's unrank row; occurrences of that acid in the peptide text)
+        const int32_t mu = (int32_t)((key >> 54) & 511u);
+        const uint32_t pos = (uint32_t)((key >> 27) & ((1u << 27) - 1u));
+        const uint32_t rank = (uint32_t)(key & ((1u << 27) - 1u));
+        if (mu >= ctx->num_mod || pos >= ctx->num_pep || ctx->h_idx[pos] != pep)
+            return fail(ctx, HFX_ERR_ARG, "modified key does not match the fragment");
+        const int32_t *cnt = ctx->mod_counts.data() + (size_t)mu * ctx->num_ma;
+        float add = 0.0f;
+        for (int32_t i = 0; i < ctx->num_ma; ++i) add = add + (float)cnt[i] * ctx->ma_mass[i];
+        mass = mass + add;
+        // the unrank row, computed on the device by the enumeration kernel
+        cudaError_t e;
+        uint32_t *q = ctx->buf<uint32_t>("mq", 16, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        uint32_t hq[16] = {pos, (uint32_t)mu, rank};
+        HFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+        HFX_CUDA(cudaMemcpy(q, hq, 12, cudaMemcpyHostToDevice), "H2D");
+        uint8_t *mod = ctx->buf<uint8_t>("mq_mod", 64, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        int rc = hfx_mods_isoforms(ctx->devdb(), ctx->devmods(), q, (const int32_t *)(q + 1), q + 2, 1, 64, q + 4,
+                                   q + 8, mod, ctx->stream);
+        if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_mod_isoforms");
+        HFX_CUDA(cudaMemcpyAsync(hq, q, 64, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+        HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+        if (rank >= hq[4]) return fail(ctx, HFX_ERR_ARG, "isoform rank out of range");
+        std::vector<uint8_t> star(s.size(), 0);
+        int32_t u = 0;
+        for (int32_t i = 0; i < ctx->num_ma; ++i) {
+            std::vector<size_t> occ;
+            for (size_t j = 2; j + 2 < s.size(); ++j)
+                if ((uint8_t)s[j] == ctx->ma[i]) occ.push_back(j);
+            for (int32_t t = 0; t < cnt[i]; ++t, ++u) {
+                const uint32_t ith = u < 8 ? hq[8 + u] : ~0u;
+                if (ith < occ.size()) star[occ[ith]] = 1;
+            }
+        }
+        std::string m;
+        for (size_t j = 0; j < s.size(); ++j) {
+            m.push_back(s[j]);
+            if (star[j]) m.push_back('*');
+        }
+        s.swap(m);
+    }
+    if ((int32_t)s.size() >= cap) return fail(ctx, HFX_ERR_ARG, "text buffer too small");
+    std::memcpy(text, s.c_str(), s.size() + 1);
+    if (mh) *mh = mass;
+    if (protein) *protein = (int32_t)pi;
+    return HFX_OK;
 }
 
 int32_t hfx_autotune(hfx_ctx *ctx, hfx_search_params *p, const float *mz, const float *it, const int64_t *off,

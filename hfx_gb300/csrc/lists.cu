@@ -599,6 +599,8 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
                     const uint32_t bin = e[k] >> 2;
                     if ((int32_t)bin < nb) TileFma<T, G>::fma(tile, bin, e[k] & 3u, acc);
                 }
+                // lists ascend: once an entry lies beyond the tile, so do the rest
+                if ((__shfl_sync(kFullMask, e[3], 31) >> 2) >= (uint32_t)nb) break;
             }
             const float sc = reduce_scatter<G>(acc);
             const bool want =

@@ -147,6 +147,17 @@ int32_t hfx_search_device(hfx_ctx *ctx, const hfx_search_params *p, const float 
                           const int64_t *off, const float *pcr, const float *z, const float *tol,
                           int32_t nspec, float *out_score, uint64_t *out_key, uint32_t *out_pep,
                           int64_t *out_ncand);
+/* Result record of one match (Match.hs:17-27): Location.hs:42-58 lookup --
+ * the peptide text "X.PEPTIDE.Y" with its flanking residues ('-' at a
+ * protein end) and (M+H)+ = residual + H + H2O (host masses) -- and for a
+ * modified key Fragment.hs:84-106 modifyFragment: the combination's mass
+ * added and '*' after each modified residue (the i-th occurrence of its acid
+ * in the text, i from the isoform's unrank row).  key/pep as returned by the
+ * search; protein (nullable) receives the protein index.  Proteins come from
+ * hfx_build_db's segments (hfx_set_protein_segments after hfx_upload_db). */
+int32_t hfx_match_peptide(hfx_ctx *ctx, uint64_t key, uint32_t pep, char *text, int32_t cap, float *mh,
+                          int32_t *protein);
+int32_t hfx_set_protein_segments(hfx_ctx *ctx, const uint32_t *seg, int32_t nprot);
 /* Autotuner (new): times the batched search of this batch (device buffers,
  * as hfx_search_device) for each spectra-per-group size G and work-item
  * size (candidates per item) it supports, `reps` timed runs each after one

@@ -178,3 +178,63 @@ def test_search_mods_edge_charges(mods_tiny, oracle):
         res = eng.search(sub, hfx_gb300.default_params(top_n=10, batch_mode=mode))
         _compare(res, ref, f"mods edges mode={mode}")
     assert (res.score[2][res.key[2] != np.iinfo(np.uint64).max] == 0).all()
+
+
+def _ref_match(prot, r, tc, tn, k, ions, counts=None, rank=None, per_type=False, oracle=None):
+    """Location.hs:42-58 lookup and Fragment.hs:84-106 modifyFragment,
+    transcribed independently: peptide text with flanks, (M+H)+, '*' after
+    the i-th occurrence of each modified acid."""
+    seq = bytes(prot.seq)
+    c, n = int(tc[k]), int(tn[k])
+    pi = int(np.searchsorted(prot.seg, c, side="right")) - 1
+    a, b = int(prot.seg[pi]), int(prot.seg[pi + 1])
+    ntake = n - c + 1 if n < len(seq) else n - c
+    text = (chr(seq[c - 1]) if c > a else "-") + "." + seq[c:c + ntake].decode() + "." + \
+        (chr(seq[n + 1]) if n < b - 1 else "-")
+    mass = np.float32(np.float32(np.float32(r[k]) + np.float32(1.007276)) + np.float32(18.010565))
+    if counts is None:
+        return text, float(mass), pi
+    add = np.float32(0.0)
+    for i, m in enumerate(MA_MASS):
+        add = np.float32(add + np.float32(np.float32(counts[i]) * np.float32(m)))
+    mass = np.float32(mass + add)
+    _, un, _ = oracle.mod_isoform(ions, c, n, MA, counts, rank=rank, per_type=per_type)
+    star, u = set(), 0
+    for i, acid in enumerate(MA.decode()):
+        occ = [j for j in range(2, len(text) - 2) if text[j] == acid]
+        for _ in range(int(counts[i])):
+            star.add(occ[int(un[u])])
+            u += 1
+    out = "".join(ch + ("*" if j in star else "") for j, ch in enumerate(text))
+    return out, float(mass), pi
+
+
+def test_match_records(mods_tiny, oracle):
+    """hfx_match_peptide: the result record of plain and modified matches."""
+    import hfx_gb300
+    eng, prot, sp = mods_tiny
+    ions, mt, r, tc, tn, idx = _oracle_db(oracle, eng, prot)
+    n, counts, _ = eng.mod_table()
+    counts = counts[: n * 4].reshape(n, 4)
+    res = eng.search(sp.subset(np.arange(20)), hfx_gb300.default_params(top_n=10, batch_mode=1))
+    pos_of = np.empty(len(idx), np.int64)
+    pos_of[idx] = np.arange(len(idx))
+    seen_mod = seen_plain = 0
+    for key, pep in zip(res.key.ravel(), res.pep.ravel()):
+        if key == np.iinfo(np.uint64).max:
+            continue
+        key = int(key)
+        q = int(pos_of[pep])
+        text, mh, pi = eng.match(key, int(pep))
+        if key >> 63:
+            mu, rank = (key >> 54) & 511, key & ((1 << 27) - 1)
+            assert (key >> 27) & ((1 << 27) - 1) == q
+            ref = _ref_match(prot, r, tc, tn, int(pep), ions, counts[mu], rank, oracle=oracle)
+            seen_mod += 1
+        else:
+            assert key == q
+            ref = _ref_match(prot, r, tc, tn, int(pep), ions)
+            seen_plain += 1
+        assert (text, pi) == (ref[0], ref[2]), (text, ref)
+        assert np.float32(mh) == np.float32(ref[1])
+    assert seen_mod > 20 and seen_plain > 20
