@@ -25,6 +25,10 @@
 
 namespace hfx {
 
+// Warps per CTA of the modification scorer: the isoform state (masks, counts,
+// suffix products) needs ~120 registers per thread.
+constexpr int kModWarps = 16;
+
 // filter_by_mod.cu:72-80: lower_bound((m - eps) - delta), upper_bound((m + eps) - delta)
 __global__ void k_mod_windows(const float *__restrict__ r_sorted, uint32_t n, const SpecMeta *__restrict__ meta,
                               int32_t nspec, const float *__restrict__ delta, int32_t num_mod,
@@ -81,7 +85,7 @@ __global__ void k_mod_groups(const GroupInfo *__restrict__ groups, const uint32_
 }
 
 template <bool FastDiv, typename T, int G>
-__global__ void __launch_bounds__(768, 1)
+__global__ void __launch_bounds__(kModWarps * 32, 1)
 k_score_mods(DevDB db, DevMods mods, const T *__restrict__ tiles, int64_t stride, const uint32_t *__restrict__ mb,
              const uint32_t *__restrict__ me, const int32_t *__restrict__ perm,
              const GroupInfo *__restrict__ groups, const uint32_t *__restrict__ mlo, const uint32_t *__restrict__ mhi,
@@ -178,7 +182,9 @@ k_score_mods(DevDB db, DevMods mods, const T *__restrict__ tiles, int64_t stride
             uint32_t D[kMaxMa];
             modable_counts(db.ions, tc, tn, mods.num_ma, D);
             bool modable = true;
-            for (int i = 0; i < mods.num_ma; ++i) modable &= D[i] >= (uint32_t)dcount[i];  // filter_by_mod.cu:251-261
+#pragma unroll
+            for (int i = 0; i < kMaxMa; ++i)  // filter_by_mod.cu:251-261
+                if (i < mods.num_ma) modable &= D[i] >= (uint32_t)dcount[i];
             if (!modable) continue;
             uint32_t scan[kMaxMa];
             const uint32_t niso = isoform_count(D, dcount, mods.num_ma, scan);
@@ -365,7 +371,7 @@ static int launch_mods_t(const DevDB &db, const DevMods &m, const void *tiles, i
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    const int nw = fused_warps(stride, sizeof(T), G, K, 8, (size_t)smem_max);
+    const int nw = std::min(kModWarps, fused_warps(stride, sizeof(T), G, K, 8, (size_t)smem_max));
     if (nw < 1) return (int)cudaErrorInvalidValue;
     const size_t smem = fused_smem_bytes(stride, sizeof(T), G, nw, K, 8);
     auto fn = k_score_mods<F, T, G>;

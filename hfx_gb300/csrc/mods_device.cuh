@@ -85,10 +85,16 @@ __device__ __forceinline__ void modable_counts(const uint8_t *__restrict__ ions,
 // Isoform count and suffix products (calc_mod_cands.cu:49-66).
 __device__ __forceinline__ uint32_t isoform_count(const uint32_t (&D)[kMaxMa], const int32_t *__restrict__ dcount,
                                                   int num_ma, uint32_t (&scan)[kMaxMa]) {
+    // fully unrolled over the acid slots so that D and scan stay in registers
     uint32_t num = 1u;
-    for (int i = num_ma - 1; i >= 0; --i) {
-        num *= choose_dev(D[i], (uint32_t)dcount[i]);
-        scan[i] = num;
+#pragma unroll
+    for (int i = kMaxMa - 1; i >= 0; --i) {
+        if (i < num_ma) {
+            num *= choose_dev(D[i], (uint32_t)dcount[i]);
+            scan[i] = num;
+        } else {
+            scan[i] = 1u;
+        }
     }
     return num;
 }
