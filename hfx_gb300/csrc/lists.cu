@@ -583,17 +583,15 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
             my_cand += 1u;
             my_entries += (uint32_t)n;
             my_psm += (uint32_t)__popc(cur.act);
-            uint32_t e[4];
+            // entries [i0, i0+128) in e, the next 128 already in flight in f
+            uint32_t e[4], f[4];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) e[k] = cur.e[k];
+            for (int k = 0; k < 4; ++k) {
+                e[k] = cur.e[k];
+                const int i = 128 + 32 * k + lane;
+                f[k] = i < n ? (uint32_t)__ldg(cur.lp + i) : 0xFFFFFFFFu;
+            }
             for (int i0 = 0; i0 < n; i0 += 128) {
-                if (i0 > 0) {
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const int i = i0 + 32 * k + lane;
-                        e[k] = i < n ? (uint32_t)__ldg(cur.lp + i) : 0xFFFFFFFFu;
-                    }
-                }
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const uint32_t bin = e[k] >> 2;
@@ -601,6 +599,12 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
                 }
                 // lists ascend: once an entry lies beyond the tile, so do the rest
                 if ((__shfl_sync(kFullMask, e[3], 31) >> 2) >= (uint32_t)nb) break;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    e[k] = f[k];
+                    const int i = i0 + 256 + 32 * k + lane;
+                    f[k] = i < n ? (uint32_t)__ldg(cur.lp + i) : 0xFFFFFFFFu;
+                }
             }
             const float sc = reduce_scatter<G>(acc);
             const bool want =
