@@ -534,32 +534,47 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
         const uint32_t my_b = lane < G ? s_wb[lane] : 0u, my_e = lane < G ? s_we[lane] : 0u;
         const int z = (int)gi.charges;
         const uint16_t *llen = list_len + (size_t)(z >= 1 ? z - 1 : 0) * num_pep;
-        // Software pipeline over the warp's candidates: the next active
-        // candidate is claimed and its list length, offset and first 128
-        // entries are loaded before the current one is scored.
+        // Three-stage software pipeline over the warp's candidates: while
+        // candidate i is scored, candidate i+1's first 128 list entries are
+        // in flight and candidate i+2 is claimed with its list length and
+        // offset loads in flight, so no stage waits on a dependent load.
+        struct Meta {
+            uint32_t p, act, n, ls;
+        };
         struct Cand {
             uint32_t p, act;
             int n;
             const E *lp;
             uint32_t e[4];
         };
-        auto next_active = [&]() {
-            Cand c;
-            c.act = 0u;
-            c.n = 0;
-            c.lp = lists;
+        auto claim = [&]() {
+            Meta m;
+            m.act = 0u;
+            m.n = 0u;
+            m.ls = 0u;
             while (true) {
                 uint32_t q = 0;
                 if (lane == 0) q = atomicAdd(&s_next, 1u);
-                c.p = __shfl_sync(kFullMask, q, 0);
-                if (c.p >= p1) break;
-                c.act = __ballot_sync(kFullMask, lane < G && my_b <= c.p && c.p < my_e) & ((1u << G) - 1u);
-                if (c.act) break;
+                m.p = __shfl_sync(kFullMask, q, 0);
+                if (m.p >= p1) break;
+                m.act = __ballot_sync(kFullMask, lane < G && my_b <= m.p && m.p < my_e) & ((1u << G) - 1u);
+                if (m.act) break;
             }
-            if (c.p < p1 && z >= 1) {
-                c.n = llen[c.p];
-                const uint64_t off = list_offset(lstart, total10, z, c.p);
-                if (c.p >= num_pep || off + (uint64_t)c.n > list_total) {
+            if (m.p < p1 && z >= 1 && m.p < num_pep) {
+                m.n = llen[m.p];
+                m.ls = lstart[m.p];
+            }
+            return m;
+        };
+        auto issue = [&](const Meta &m) {
+            Cand c;
+            c.p = m.p;
+            c.act = m.act;
+            c.n = (int)m.n;
+            c.lp = lists;
+            if (m.p < p1 && z >= 1) {
+                const uint64_t off = total10 * (uint64_t)(z * (z - 1) / 2) + (uint64_t)z * m.ls;
+                if (m.p >= num_pep || off + (uint64_t)c.n > list_total) {
                     if (lane == 0) atomicOr(err, kErrBounds);
                     c.n = 0;
                 } else {
@@ -573,9 +588,13 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
             }
             return c;
         };
-        Cand cur = next_active();
-        while (cur.p < p1) {
-            const Cand nxt = next_active();
+        Meta ahead = claim();
+        Cand nxt = issue(ahead);
+        if (nxt.p < p1) ahead = claim();
+        while (nxt.p < p1) {
+            const Cand cur = nxt;
+            nxt = issue(ahead);
+            if (nxt.p < p1) ahead = claim();
             float acc[G];
 #pragma unroll
             for (int j = 0; j < G; ++j) acc[j] = 0.0f;
@@ -611,7 +630,6 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
                 ((cur.act >> my_slot) & 1u) && score_order(sc) >= *(volatile uint32_t *)(thr_u + my_slot);
             const uint32_t ins = __ballot_sync(kFullMask, want) & slot_owner_mask<G>();
             if (ins) slots.offer(sc, cur.p, ins, K, thr_u);
-            cur = nxt;
         }
         __syncthreads();  // every warp is done with the tile: its region takes the survivors
         slots.flush(thr_u, cnt, buf_s, buf_k, cap, K);
