@@ -510,7 +510,7 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     const DevDB db = ctx->devdb();
     const void *src_rows = elem_kind == 0 ? (const void *)rows : rows_lo;
     const bool plain_on = p->search_plain != 0;
-    const uint32_t *lists32 = nullptr;  // long rows: the lists the rescoring reads
+    const void *lists_out = nullptr;  // the step's lists, which the FP32 rescoring reads
     const uint16_t *llen_out = nullptr;
     uint64_t total10_out = 0;
     const bool mods_on = p->search_mods != 0 && ctx->num_mod > 0;
@@ -542,7 +542,7 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
         void *lists = long_rows ? (void *)ctx->buf<uint32_t>("l_lists32", total10 * 10 + 64, e)
                                 : (void *)ctx->buf<uint16_t>("l_lists", total10 * 10 + 64, e);
         if (e) return cuda_fail(ctx, e, "alloc lists");
-        lists32 = long_rows ? (const uint32_t *)lists : nullptr;
+        lists_out = lists;
         llen_out = llen;
         total10_out = total10;
         unsigned long long *stats = nullptr;
@@ -655,8 +655,10 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     } else {
         ctx->stage_end(HFX_STAGE_TOPN, 1, ns);
         ctx->stage_begin(HFX_STAGE_RESCORE);
-        if (long_rows)
-            rc = hfx_rescore_lists(lists32, ctx->d_lstart.as<uint32_t>(), total10_out, llen_out,
+        // unmodified keys only: rescore from the step's lists; modified keys
+        // (and the fused mode, which keeps no lists) rebuild their ions
+        if (lists_out && (long_rows || !mods_on))
+            rc = hfx_rescore_lists(lists_out, long_rows, ctx->d_lstart.as<uint32_t>(), total10_out, llen_out,
                                    (uint32_t)ctx->num_pep, ctx->d_idx.as<uint32_t>(), rows, stride, meta, kk, ns, K,
                                    p->top_n, out_s, out_k, out_pep, ctx->d_err.as<uint32_t>(), ctx->stream);
         else

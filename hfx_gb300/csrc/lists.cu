@@ -390,7 +390,8 @@ __global__ void __launch_bounds__(256) k_gen_lists_long(DevDB db, const int32_t 
 // FP32 rescoring of kept unmodified candidates from their lists and the
 // FP32 row in global memory (long rows), canonical order: entry i by lane
 // i % 32, XOR butterfly.  One CTA per spectrum.
-__global__ void __launch_bounds__(256) k_rescore_lists(const uint32_t *__restrict__ lists,
+template <typename E>
+__global__ void __launch_bounds__(256) k_rescore_lists(const E *__restrict__ lists,
                                                        const uint32_t *__restrict__ lstart, uint64_t total10,
                                                        const uint16_t *__restrict__ list_len, uint32_t num_pep,
                                                        const uint32_t *__restrict__ idx_sorted,
@@ -414,9 +415,9 @@ __global__ void __launch_bounds__(256) k_rescore_lists(const uint32_t *__restric
             if (!(kk >> 63) && z >= 1 && kk < num_pep) {
                 const uint32_t p = (uint32_t)kk;
                 const int n = list_len[(size_t)(z - 1) * num_pep + p];
-                const uint32_t *lp = lists + list_offset(lstart, total10, z, p);
+                const E *lp = lists + list_offset(lstart, total10, z, p);
                 for (int i = lane; i < n; i += 32) {
-                    const uint32_t e = __ldg(lp + i);
+                    const uint32_t e = (uint32_t)__ldg(lp + i);
                     const uint32_t bin = e >> 2;
                     if ((int32_t)bin < m.len) acc = __fmaf_rn(level_weight(e & 3u), __ldg(row + bin), acc);
                 }
@@ -779,12 +780,19 @@ int hfx_lists_generate_long(const DevDB &db, const int32_t *cover, int64_t npep1
     return (int)cudaGetLastError();
 }
 
-int hfx_rescore_lists(const uint32_t *lists, const uint32_t *lstart, uint64_t total10, const uint16_t *list_len,
-                      uint32_t num_pep, const uint32_t *idx_sorted, const float *rows32, int64_t stride,
-                      const SpecMeta *meta, const uint64_t *kept_k, int32_t nspec, int32_t K, int32_t topn,
-                      float *out_s, uint64_t *out_k, uint32_t *out_pep, uint32_t *err, cudaStream_t st) {
+int hfx_rescore_lists(const void *lists, int long_rows, const uint32_t *lstart, uint64_t total10,
+                      const uint16_t *list_len, uint32_t num_pep, const uint32_t *idx_sorted, const float *rows32,
+                      int64_t stride, const SpecMeta *meta, const uint64_t *kept_k, int32_t nspec, int32_t K,
+                      int32_t topn, float *out_s, uint64_t *out_k, uint32_t *out_pep, uint32_t *err,
+                      cudaStream_t st) {
     if (nspec <= 0) return 0;
-    k_rescore_lists<<<nspec, 256, 0, st>>>(lists, lstart, total10, list_len, num_pep, idx_sorted, rows32, stride,
-                                           meta, kept_k, K, topn, out_s, out_k, out_pep, err);
+    if (long_rows)
+        k_rescore_lists<uint32_t><<<nspec, 256, 0, st>>>((const uint32_t *)lists, lstart, total10, list_len, num_pep,
+                                                         idx_sorted, rows32, stride, meta, kept_k, K, topn, out_s,
+                                                         out_k, out_pep, err);
+    else
+        k_rescore_lists<uint16_t><<<nspec, 256, 0, st>>>((const uint16_t *)lists, lstart, total10, list_len, num_pep,
+                                                         idx_sorted, rows32, stride, meta, kept_k, K, topn, out_s,
+                                                         out_k, out_pep, err);
     return (int)cudaGetLastError();
 }

@@ -33,7 +33,10 @@ int hfx_lists_generate_long(const hfx::DevDB &db, const int32_t *cover, int64_t 
                             const uint32_t *lstart, uint64_t total10, uint32_t *lists, uint16_t *list_len,
                             int fastdiv, float ion_bw, unsigned long long *stats, uint32_t *err,
                             cudaStream_t st);
-int hfx_rescore_lists(const uint32_t *lists, const uint32_t *lstart, uint64_t total10, const uint16_t *list_len,
-                      uint32_t num_pep, const uint32_t *idx_sorted, const float *rows32, int64_t stride,
-                      const hfx::SpecMeta *meta, const uint64_t *kept_k, int32_t nspec, int32_t K, int32_t topn,
-                      float *out_s, uint64_t *out_k, uint32_t *out_pep, uint32_t *err, cudaStream_t st);
+// FP32 rescoring of kept unmodified candidates from the step's lists (32-bit
+// entries for long rows, else 16-bit) and the FP32 rows.
+int hfx_rescore_lists(const void *lists, int long_rows, const uint32_t *lstart, uint64_t total10,
+                      const uint16_t *list_len, uint32_t num_pep, const uint32_t *idx_sorted, const float *rows32,
+                      int64_t stride, const hfx::SpecMeta *meta, const uint64_t *kept_k, int32_t nspec, int32_t K,
+                      int32_t topn, float *out_s, uint64_t *out_k, uint32_t *out_pep, uint32_t *err,
+                      cudaStream_t st);
