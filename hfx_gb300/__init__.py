@@ -215,7 +215,7 @@ class Engine:
         """Work counters of the batched list path (see hfx_search_counters)."""
         c = np.zeros(8, np.uint64)
         self._check(self.lib.hfx_search_counters(self.h, _ptr(c), int(reset)))
-        names = ["lists", "list_entries", "candidates", "entries_streamed", "pairs"]
+        names = ["lists", "list_entries", "candidates", "entries_streamed", "pairs", "positions_claimed"]
         return {n: int(c[i]) for i, n in enumerate(names)}
 
     def set_stream(self, stream_ptr: int):

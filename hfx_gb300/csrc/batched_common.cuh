@@ -197,6 +197,161 @@ struct WarpSlots {
     }
 };
 
+// CTA-wide top-K of every member slot with batched admission.  The CTA
+// keeps one list per slot in shared memory (entry i at lane i, best first:
+// higher score, then lower key).  An offer that passes the slot's threshold
+// is appended by the slot's lane to its warp's queue of kQ entries; a full
+// queue is sorted across the warp (bitonic) and merged into the slot's list
+// under the slot's lock, after which the threshold is the list's K-th score.
+// The list is the top-K of everything offered, as with one insertion per
+// offer.
+template <int G, typename Key = uint32_t>
+struct CtaSlots {
+    static constexpr int kQ = 16;
+    static constexpr Key kNone = ~Key(0);
+    float *ls;       // [G][32] scores of the CTA's lists
+    Key *lk;         // [G][32] keys
+    uint32_t *lock;  // [G]
+    uint32_t *thr;   // [G] score_order of each list's K-th (0 = none yet)
+    float *qs;       // this warp's queues: [G][kQ] scores, then [G][kQ] keys
+    Key *qk;
+    uint32_t qn;     // slot lanes: entries queued for the lane's slot
+    uint32_t *err;
+
+    __host__ __device__ static constexpr size_t warp_bytes() { return (size_t)G * kQ * (4 + sizeof(Key)); }
+
+    __device__ __forceinline__ void bind(float *ls_, Key *lk_, uint32_t *lock_, uint32_t *thr_, uint8_t *queue,
+                                         uint32_t *err_) {
+        ls = ls_;
+        lk = lk_;
+        lock = lock_;
+        thr = thr_;
+        qs = reinterpret_cast<float *>(queue);
+        qk = reinterpret_cast<Key *>(queue + (size_t)G * kQ * 4);
+        qn = 0u;
+        err = err_;
+    }
+    // Item start, by threads [0, 32 G) of the CTA (a barrier must follow).
+    __device__ __forceinline__ void reset_shared() {
+        for (int t = threadIdx.x; t < G * 32; t += blockDim.x) {
+            ls[t] = -INFINITY;
+            lk[t] = kNone;
+        }
+        if (threadIdx.x < G) {
+            lock[threadIdx.x] = 0u;
+            thr[threadIdx.x] = 0u;
+        }
+    }
+
+    __device__ __forceinline__ static bool better(float a, Key ka, float b, Key kb) {
+        return a > b || (a == b && ka < kb);
+    }
+    // Compare-exchange with lane ^ d: the lower lane keeps the better entry
+    // when `desc`, the worse one otherwise.
+    __device__ __forceinline__ static void cx(float &v, Key &kv, int d, bool desc) {
+        const int lane = threadIdx.x & 31;
+        const float ov = __shfl_xor_sync(kFullMask, v, d);
+        const Key ok = __shfl_xor_sync(kFullMask, kv, d);
+        const bool lower = (lane & d) == 0;
+        const bool mine = better(v, kv, ov, ok);
+        if (mine != (lower == desc)) {
+            v = ov;
+            kv = ok;
+        }
+    }
+
+    // Merge the first `cnt` queued entries of slot j (warp-wide).
+    __device__ __forceinline__ void merge(int j, int cnt, int K) {
+        const int lane = threadIdx.x & 31;
+        float ns = -INFINITY;
+        Key nk = kNone;
+        if (lane < cnt) {
+            ns = qs[j * kQ + lane];
+            nk = qk[j * kQ + lane];
+        }
+        // lanes 0..kQ-1 sorted best first; lanes kQ..31 hold nothing
+#pragma unroll
+        for (int b = 2; b <= kQ; b <<= 1)
+#pragma unroll
+            for (int d = b >> 1; d > 0; d >>= 1) cx(ns, nk, d, (lane & b) == 0);
+        const float rs = __shfl_sync(kFullMask, ns, 31 - lane);
+        const Key rk = __shfl_sync(kFullMask, nk, 31 - lane);
+        uint32_t got = 0u;
+        if (lane == 0) {
+            for (uint32_t i = 0; i < kLockLimit; ++i)
+                if (atomicCAS(lock + j, 0u, 1u) == 0u) {
+                    got = 1u;
+                    break;
+                }
+        }
+        got = __shfl_sync(kFullMask, got, 0);
+        if (!got) {
+            if (lane == 0) atomicOr(err, kErrTimeout);
+            return;
+        }
+        __threadfence_block();
+        float ws = *(volatile float *)(ls + j * 32 + lane);
+        Key wk = *(volatile Key *)(lk + j * 32 + lane);
+        // the top 32 of both lists as a bitonic sequence, then sorted best first
+        if (better(rs, rk, ws, wk)) {
+            ws = rs;
+            wk = rk;
+        }
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) cx(ws, wk, d, true);
+        *(volatile float *)(ls + j * 32 + lane) = ws;
+        *(volatile Key *)(lk + j * 32 + lane) = wk;
+        const float kth = __shfl_sync(kFullMask, ws, K - 1);
+        if (lane == 0 && kth != -INFINITY) *(volatile uint32_t *)(thr + j) = score_order(kth);
+        __threadfence_block();
+        __syncwarp();
+        if (lane == 0) atomicExch(lock + j, 0u);
+    }
+
+    // Offer candidate `key`: the lane of slot `my_slot` appends (sc, key) to
+    // the slot's queue when `want`; full queues are merged.
+    __device__ __forceinline__ void offer(bool want, float sc, Key key, int my_slot, int K) {
+        if (want) {
+            qs[my_slot * kQ + qn] = sc;
+            qk[my_slot * kQ + qn] = key;
+            ++qn;
+        }
+        uint32_t full = __ballot_sync(kFullMask, want && qn == (uint32_t)kQ);
+        while (full) {
+            const int l = __ffs(full) - 1;
+            full &= full - 1u;
+            __syncwarp();
+            merge(l / (32 / G), kQ, K);
+            if ((threadIdx.x & 31) == l) qn = 0u;
+        }
+    }
+
+    // Item end: merge what is still queued.
+    __device__ __forceinline__ void drain(int K) {
+        uint32_t own = 0u;
+#pragma unroll
+        for (int j = 0; j < G; ++j) own |= 1u << slot_lane<G>(j);
+        uint32_t pend = __ballot_sync(kFullMask, qn != 0u) & own;
+        __syncwarp();
+        while (pend) {
+            const int l = __ffs(pend) - 1;
+            pend &= pend - 1u;
+            merge(l / (32 / G), (int)__shfl_sync(kFullMask, qn, l), K);
+        }
+        qn = 0u;
+    }
+
+    // After a barrier: slot j's top-K (lanes < K; warp-wide).
+    __device__ __forceinline__ void result(int j, int K, float *out_s, uint64_t *out_k) const {
+        const int lane = threadIdx.x & 31;
+        if (lane < K) {
+            const Key k = lk[j * 32 + lane];
+            out_s[lane] = ls[j * 32 + lane];
+            out_k[lane] = k == kNone ? ~0ull : (uint64_t)k;
+        }
+    }
+};
+
 // Item end, step 2 (one warp per slot): the slot's top-K from its buffer.
 template <typename Key>
 __device__ __forceinline__ void slot_merge(const float *bs, const Key *bk, uint32_t n, int K, float *out_s,

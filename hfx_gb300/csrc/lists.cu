@@ -463,31 +463,30 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
               const GroupInfo *__restrict__ groups, const uint32_t *__restrict__ item_off,
               const uint32_t *__restrict__ ngroups_p, int32_t K, uint32_t *__restrict__ counter,
               float *__restrict__ part_s, uint64_t *__restrict__ part_k, unsigned long long *__restrict__ stats,
-              uint32_t *__restrict__ err) {
+              uint32_t qoff, uint32_t *__restrict__ err) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     T *stile = reinterpret_cast<T *>(smem + 128);
-    // after an item's candidates the tile region holds the warps' surviving entries
-    const int cap = nw * K;
-    float *buf_s = reinterpret_cast<float *>(smem + 128);
-    uint32_t *buf_k = reinterpret_cast<uint32_t *>(buf_s + (size_t)G * cap);
     const T *tile = stile;
     __shared__ int32_t s_item;
     __shared__ uint32_t s_next;
     __shared__ uint32_t s_wb[G], s_we[G];
-    __shared__ uint32_t thr_u[G], cnt[G];
-    __shared__ unsigned long long s_stats[3];
+    __shared__ uint32_t thr_u[G], s_lock[G];
+    __shared__ float s_ls[G * 32];
+    __shared__ uint32_t s_lk[G * 32];
+    __shared__ unsigned long long s_stats[4];
 
     const int32_t ngroups = (int32_t)*ngroups_p;
     const uint32_t total = item_off[ngroups];
     if (threadIdx.x == 0) mbar_init(bar, 1);
-    if (threadIdx.x < 3) s_stats[threadIdx.x] = 0ull;
+    if (threadIdx.x < 4) s_stats[threadIdx.x] = 0ull;
     __syncthreads();
     const int my_slot = reduce_slot_of_lane<G>(lane);
-    uint32_t my_cand = 0, my_entries = 0, my_psm = 0;
+    uint32_t my_cand = 0, my_entries = 0, my_psm = 0, my_claims = 0;
     uint32_t phase = 0;
-    WarpSlots<G> slots;
+    CtaSlots<G> slots;
+    slots.bind(s_ls, s_lk, s_lock, thr_u, smem + qoff + (size_t)warp * CtaSlots<G>::warp_bytes(), err);
     while (true) {
         if (threadIdx.x == 0) s_item = (int32_t)atomicAdd(counter, 1u);
         __syncthreads();
@@ -508,14 +507,15 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
             }
             s_wb[j] = b;
             s_we[j] = e;
-            thr_u[j] = 0u;
-            cnt[j] = 0u;
         }
-        if (threadIdx.x == 0) s_next = p0;
+        slots.reset_shared();
+        if (threadIdx.x == 0) {
+            s_next = p0;
+            my_claims += p1 - p0;
+        }
         const int32_t nb = tile_bins(gi.maxlen);
         if constexpr (kGlobal) {
             tile = tiles + (size_t)g * stride * G;
-            slots.init();
             __syncthreads();
         } else {
             if (threadIdx.x == 0) {
@@ -524,7 +524,6 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
                 mbar_arrive_expect_tx(bar, bytes);
                 bulk_g2s(stile, tiles + (size_t)g * stride * G, bytes, bar);
             }
-            slots.init();
             __syncthreads();
             if (!mbar_wait(bar, phase, kWaitLimit)) {
                 if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
@@ -627,18 +626,15 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
                 }
             }
             const float sc = reduce_scatter<G>(acc);
-            const bool want =
-                ((cur.act >> my_slot) & 1u) && score_order(sc) >= *(volatile uint32_t *)(thr_u + my_slot);
-            const uint32_t ins = __ballot_sync(kFullMask, want) & slot_owner_mask<G>();
-            if (ins) slots.offer(sc, cur.p, ins, K, thr_u);
+            const bool want = (lane & (32 / G - 1)) == 0 && ((cur.act >> my_slot) & 1u) &&
+                              score_order(sc) >= *(volatile uint32_t *)(thr_u + my_slot);
+            slots.offer(want, sc, cur.p, my_slot, K);
         }
-        __syncthreads();  // every warp is done with the tile: its region takes the survivors
-        slots.flush(thr_u, cnt, buf_s, buf_k, cap, K);
-        __syncthreads();
+        slots.drain(K);
+        __syncthreads();  // every warp has merged its queues
         for (int j = warp; j < cnt_members; j += nw) {
             const size_t o = ((size_t)item * G + j) * K;
-            slot_merge(buf_s + (size_t)j * cap, buf_k + (size_t)j * cap, min(cnt[j], (uint32_t)cap), K, part_s + o,
-                       part_k + o);
+            slots.result(j, K, part_s + o, part_k + o);
         }
         __syncthreads();
     }
@@ -647,12 +643,14 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
             atomicAdd(&s_stats[0], (unsigned long long)my_cand);
             atomicAdd(&s_stats[1], (unsigned long long)my_entries);
             atomicAdd(&s_stats[2], (unsigned long long)my_psm);
+            atomicAdd(&s_stats[3], (unsigned long long)my_claims);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
             atomicAdd(&stats[2], s_stats[0]);
             atomicAdd(&stats[3], s_stats[1]);
             atomicAdd(&stats[4], s_stats[2]);
+            atomicAdd(&stats[5], s_stats[3]);
         }
     }
 }
@@ -711,9 +709,9 @@ static int launch_lists_t(const E *lists, const uint32_t *lstart, uint64_t total
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (nw <= 0) nw = 16;
     const size_t tile = kGlobal ? 0 : (((size_t)stride * G * sizeof(T) + 15) & ~(size_t)15);
-    // the tile region doubles as the item-end buffer of the warps' survivors
-    const size_t survivors = (size_t)G * nw * K * 8;
-    const size_t smem = 128 + std::max(tile, survivors);
+    // the warps' admission queues follow the tile
+    const size_t qoff = 128 + tile;
+    const size_t smem = qoff + (size_t)nw * CtaSlots<G>::warp_bytes();
     if (smem > (size_t)smem_max) return (int)cudaErrorInvalidValue;
     auto fn = k_score_lists<T, G, E, kGlobal>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -724,7 +722,7 @@ static int launch_lists_t(const E *lists, const uint32_t *lstart, uint64_t total
     cudaMemsetAsync(ws.counter, 0, 4, st);
     fn<<<grid, nw * 32, smem, st>>>(lists, lstart, total10, total10 * 10, list_len, num_pep, (const T *)tiles,
                                     stride, wb, we, ws.perm, ws.groups, ws.item_off, ws.ngroups, K,
-                                    ws.counter, part_s, part_k, stats, err);
+                                    ws.counter, part_s, part_k, stats, (uint32_t)qoff, err);
     return (int)cudaGetLastError();
 }
 

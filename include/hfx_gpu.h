@@ -86,7 +86,8 @@ int32_t hfx_set_profiling(hfx_ctx *ctx, int32_t on);
 int32_t hfx_stage_stats(hfx_ctx *ctx, double *ms, int64_t *launches, int64_t *units, int32_t reset);
 /* Work counters of the batched list path, accumulated while profiling is on:
  * [0] ion lists built, [1] list entries built, [2] candidates scored,
- * [3] list entries streamed by the scorer, [4] peptide-spectrum pairs. */
+ * [3] list entries streamed by the scorer, [4] peptide-spectrum pairs,
+ * [5] candidate positions in the scorer's work items (active or not). */
 int32_t hfx_search_counters(hfx_ctx *ctx, uint64_t *out8, int32_t reset);
 
 /* Digest proteins into the search database and upload it.  Replaces
