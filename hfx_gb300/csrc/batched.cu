@@ -559,7 +559,8 @@ static int pack_tiles_g(int32_t G, const void *rows, int64_t stride, const SpecM
                         void *tiles, uint32_t ngroups, cudaStream_t st) {
     if (ngroups == 0) return 0;
     const T *r = (const T *)rows;
-    if (G == 8) hfx_pack_tiles_launch<T, 8>(r, stride, meta, ws, (T *)tiles, ngroups, st);
+    if (G == 16) hfx_pack_tiles_launch<T, 16>(r, stride, meta, ws, (T *)tiles, ngroups, st);
+    else if (G == 8) hfx_pack_tiles_launch<T, 8>(r, stride, meta, ws, (T *)tiles, ngroups, st);
     else if (G == 4) hfx_pack_tiles_launch<T, 4>(r, stride, meta, ws, (T *)tiles, ngroups, st);
     else if (G == 2) hfx_pack_tiles_launch<T, 2>(r, stride, meta, ws, (T *)tiles, ngroups, st);
     else if (G == 1) hfx_pack_tiles_launch<T, 1>(r, stride, meta, ws, (T *)tiles, ngroups, st);

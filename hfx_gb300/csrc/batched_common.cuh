@@ -205,9 +205,9 @@ struct WarpSlots {
 // under the slot's lock, after which the threshold is the list's K-th score.
 // The list is the top-K of everything offered, as with one insertion per
 // offer.
-template <int G, typename Key = uint32_t>
+template <int G, typename Key = uint32_t, int Q = (G >= 16 ? 8 : 16)>
 struct CtaSlots {
-    static constexpr int kQ = 16;
+    static constexpr int kQ = Q;
     static constexpr Key kNone = ~Key(0);
     float *ls;       // [G][32] scores of the CTA's lists
     Key *lk;         // [G][32] keys
@@ -376,7 +376,8 @@ __device__ __forceinline__ void slot_merge(const float *bs, const Key *bk, uint3
 template <int G>
 __device__ __forceinline__ uint32_t slot_owner_mask() {
     // one lane per slot among the lanes that hold the same reduced slot
-    if constexpr (G == 8) return 0x11111111u;
+    if constexpr (G == 16) return 0x55555555u;
+    else if constexpr (G == 8) return 0x11111111u;
     else if constexpr (G == 4) return 0x01010101u;
     else if constexpr (G == 2) return 0x00010001u;
     else return 0x1u;

@@ -398,6 +398,41 @@ template <> struct TileFma<__half, 8> {
         HFX_MIXED_FMA8("f16");
     }
 };
+// 16 spectra: two 16-byte loads, the same per-element FMAs.
+template <> struct TileFma<__nv_bfloat16, 16> {
+    __device__ __forceinline__ static void fma(const __nv_bfloat16 *t, uint32_t bin, uint32_t lvl, float (&a)[16]) {
+        const uint4 v0 = *reinterpret_cast<const uint4 *>(t + (size_t)bin * 16);
+        const uint4 v1 = *reinterpret_cast<const uint4 *>(t + (size_t)bin * 16 + 8);
+        const uint16_t w = level_weight_bf16(lvl);
+        {
+            float(&acc)[8] = *reinterpret_cast<float(*)[8]>(&a[0]);
+            const uint4 v = v0;
+            HFX_MIXED_FMA8("bf16");
+        }
+        {
+            float(&acc)[8] = *reinterpret_cast<float(*)[8]>(&a[8]);
+            const uint4 v = v1;
+            HFX_MIXED_FMA8("bf16");
+        }
+    }
+};
+template <> struct TileFma<__half, 16> {
+    __device__ __forceinline__ static void fma(const __half *t, uint32_t bin, uint32_t lvl, float (&a)[16]) {
+        const uint4 v0 = *reinterpret_cast<const uint4 *>(t + (size_t)bin * 16);
+        const uint4 v1 = *reinterpret_cast<const uint4 *>(t + (size_t)bin * 16 + 8);
+        const uint16_t w = level_weight_f16(lvl);
+        {
+            float(&acc)[8] = *reinterpret_cast<float(*)[8]>(&a[0]);
+            const uint4 v = v0;
+            HFX_MIXED_FMA8("f16");
+        }
+        {
+            float(&acc)[8] = *reinterpret_cast<float(*)[8]>(&a[8]);
+            const uint4 v = v1;
+            HFX_MIXED_FMA8("f16");
+        }
+    }
+};
 template <> struct TileFma<__nv_bfloat16, 4> {
     __device__ __forceinline__ static void fma(const __nv_bfloat16 *t, uint32_t bin, uint32_t lvl, float (&acc)[4]) {
         const uint2 v = *reinterpret_cast<const uint2 *>(t + (size_t)bin * 4);
@@ -494,13 +529,15 @@ __device__ __forceinline__ void butterfly_all(float (&acc)[G]) {
 }
 
 // The same sums as butterfly_all, as a reduce-scatter: at offsets 16, 8, 4
-// each lane keeps half of its accumulators and receives its partner's copy
-// of them, so every addition pairs the same operands as the full butterfly.
-// Returns the sum of accumulator slot_of_lane(lane); lanes differing only in
-// bits 0-1 (G = 8), 0-2 (G = 4), 0-3 (G = 2) hold the same slot.
+// (and 2 for G = 16) each lane keeps half of its accumulators and receives
+// its partner's copy of them, so every addition pairs the same operands as
+// the full butterfly.  Returns the sum of accumulator slot_of_lane(lane);
+// lanes differing only in bit 0 (G = 16), bits 0-1 (G = 8), 0-2 (G = 4),
+// 0-3 (G = 2) hold the same slot.
 template <int G>
 __device__ __forceinline__ int reduce_slot_of_lane(int lane) {
-    if constexpr (G == 8) return ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
+    if constexpr (G == 16) return ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
+    else if constexpr (G == 8) return ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
     else if constexpr (G == 4) return ((lane >> 4) & 1) * 2 + ((lane >> 3) & 1);
     else if constexpr (G == 2) return (lane >> 4) & 1;
     else return 0;
@@ -514,7 +551,7 @@ __device__ __forceinline__ float reduce_scatter(float (&acc)[G]) {
     int n = G;
     int off = 16;
 #pragma unroll
-    for (int step = 0; step < 3; ++step) {
+    for (int step = 0; step < 4; ++step) {
         if (n == 1) break;
         const int half = n / 2;
         const bool hi = (lane & off) != 0;

@@ -441,15 +441,24 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     cudaError_t e;
     const int32_t ns = b.nspec;
     // one 16-byte tile load per bin: 8 BF16/FP16 or 4 FP32 spectra per group
-    const int32_t G = p->group_size > 0 ? p->group_size : (elem_kind == 0 ? 4 : 8);
+    int32_t G = p->group_size > 0 ? p->group_size : (elem_kind == 0 ? 4 : 8);
     const int32_t chunk = p->chunk > 0 ? p->chunk : 4096;
-    if (G != 1 && G != 2 && G != 4 && G != 8) return fail(ctx, HFX_ERR_ARG, "group_size must be 1, 2, 4 or 8");
+    if (G != 1 && G != 2 && G != 4 && G != 8 && G != 16)
+        return fail(ctx, HFX_ERR_ARG, "group_size must be 1, 2, 4, 8 or 16");
     const int32_t K = elem_kind == 0 ? p->top_n : std::max(p->top_n, std::min(p->rescore_k > 0 ? p->rescore_k : 32,
                                                                                kMaxTopK));
     // rows longer than the shared-memory bit planes: 32-bit sorted lists,
     // tiles read from global memory, list-based rescoring; no fused or
     // modification scoring
     const bool long_rows = stride > (int64_t)kMaxWords * 32;
+    if (G == 16) {
+        // two 16-byte loads per bin: list scoring of BF16/FP16 rows only
+        if (elem_kind == 0 || (p->batch_mode != 1 && !long_rows) || (p->search_mods != 0 && ctx->num_mod > 0))
+            return fail(ctx, HFX_ERR_UNSUPPORTED,
+                        "group_size 16 needs BF16/FP16 rows, list scoring and no modification search");
+        // a 16-spectrum tile of the longest row must fit in shared memory
+        if (!hfx_lists_group_fits(16, long_rows ? 1 : 0, stride, 2)) G = 8;
+    }
     if (long_rows && p->search_mods && ctx->num_mod > 0)
         return fail(ctx, HFX_ERR_UNSUPPORTED, "modification search on rows longer than 8192 bins");
     if (p->ion_bins_custom && !long_rows)
@@ -1171,8 +1180,11 @@ int32_t hfx_autotune(hfx_ctx *ctx, hfx_search_params *p, const float *mz, const 
     hfx_search_params q = *p;
     q.use_graph = 0;
     // one 16-byte shared-memory load per bin: 8 BF16/FP16 or 4 FP32 spectra
-    // per group are the natural sizes; half of that is the alternative
-    const int32_t gs[2] = {p->precision == 0 ? 4 : 8, p->precision == 0 ? 2 : 4};
+    // per group are the natural sizes; half of that is the alternative, and
+    // BF16/FP16 list scoring without modifications also tries 16
+    const bool g16 = p->precision != 0 && p->batch_mode == 1 && !(p->search_mods != 0 && ctx->num_mod > 0);
+    const int32_t gs[3] = {p->precision == 0 ? 4 : 8, p->precision == 0 ? 2 : 4, 16};
+    const int ngs = g16 ? 3 : 2;
     const int32_t chunks[5] = {1024, 2048, 4096, 8192, 16384};
     cudaEvent_t e0, e1;
     HFX_CUDA(cudaEventCreate(&e0), "event");
@@ -1180,7 +1192,7 @@ int32_t hfx_autotune(hfx_ctx *ctx, hfx_search_params *p, const float *mz, const 
     float best = 1e30f;
     int32_t best_g = gs[0], best_c = chunks[2];
     int32_t rc = HFX_OK;
-    for (int gi = 0; gi < 2 && rc == HFX_OK; ++gi) {
+    for (int gi = 0; gi < ngs && rc == HFX_OK; ++gi) {
         for (int ci = 0; ci < 5 && rc == HFX_OK; ++ci) {
             q.group_size = gs[gi];
             q.chunk = chunks[ci];

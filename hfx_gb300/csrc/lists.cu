@@ -116,36 +116,40 @@ __global__ void k_mark_levels(const SpecMeta *__restrict__ meta, const uint32_t 
 
 // Warp-cooperative compaction of plane words [wr.lo, wr.hi) into the
 // ascending distinct-bin list `list` (entries (bin << 2) | level); clears the
-// words when `clear`.  Returns the number of distinct bins (may exceed cap;
-// entries beyond cap are dropped).
+// words when `clear`.  Lane l takes k = ceil(words / 32) consecutive words,
+// so one scan places every lane's entries and the serial bit loop runs as
+// long as the fullest lane's k words, not a 32-word stripe's fullest word
+// per stripe.  Returns the number of distinct bins (may exceed cap; entries
+// beyond cap are dropped).
 __device__ __forceinline__ int compact_planes(const Planes &pl, WordRange wr, bool clear, uint16_t *list, int cap) {
     const int lane = threadIdx.x & 31;
-    int n = 0;
-    for (int w0 = wr.lo; w0 < wr.hi; w0 += 32) {
-        const int w = w0 + lane;
-        uint32_t a = 0, h = 0, tt = 0;
-        if (w < wr.hi) {
-            h = pl.H[w];
-            tt = pl.T[w];
-            a = pl.A[w] | h;
-            if (clear) {
-                pl.A[w] = 0u;
-                pl.H[w] = 0u;
-                pl.T[w] = 0u;
-            }
+    const int nwords = wr.hi - wr.lo;
+    if (nwords <= 0) return 0;
+    const int k = (nwords + 31) >> 5;
+    const int w0 = wr.lo + lane * k;
+    const int w1 = min(w0 + k, wr.hi);
+    int pc = 0;
+    for (int w = w0; w < w1; ++w) pc += __popc(pl.A[w] | pl.H[w]);
+    const int incl = warp_incl_scan(pc);
+    int pos = incl - pc;
+    for (int w = w0; w < w1; ++w) {
+        const uint32_t h = pl.H[w], tt = pl.T[w];
+        uint32_t a = pl.A[w] | h;
+        if (clear) {
+            pl.A[w] = 0u;
+            pl.H[w] = 0u;
+            pl.T[w] = 0u;
         }
-        const int pc = __popc(a);
-        const int incl = warp_incl_scan(pc);
-        int pos = n + incl - pc;
+        const uint32_t base = (uint32_t)w << 7 | 1u;  // (w * 32) << 2, level 1
         while (a) {
             const int b = __ffs(a) - 1;
             a &= a - 1u;
-            const uint32_t l3 = ((tt >> b) & 1u) ? 3u : (((h >> b) & 1u) ? 2u : 1u);
-            if (pos < cap) list[pos] = (uint16_t)((((uint32_t)w << 5 | (uint32_t)b) << 2) | l3);
+            const uint32_t key = base + ((uint32_t)b << 2) + ((h >> b) & 1u) + ((tt >> b) & 1u);
+            if (pos < cap) list[pos] = (uint16_t)key;
             ++pos;
         }
-        n += __shfl_sync(kFullMask, incl, 31);
     }
+    const int n = __shfl_sync(kFullMask, incl, 31);
     __syncwarp();
     return n;
 }
@@ -697,6 +701,16 @@ int hfx_lists_generate(const DevDB &db, const int32_t *cover, int64_t npep1, int
     return (int)cudaGetLastError();
 }
 
+// Warps per list-scorer CTA: 16 (two CTAs per SM) up to 8 spectra per
+// group, 32 (one CTA per SM, the tile taking most of shared memory) for 16.
+constexpr int list_warps(int G) { return G >= 16 ? 32 : 16; }
+
+// Dynamic shared memory of the list scorer: an mbarrier, the group tile
+// (none when it is read from global memory), then the warps' queues.
+static size_t lists_queue_offset(bool global_tile, int64_t stride, int G, size_t elem_bytes) {
+    return 128 + (global_tile ? 0 : (((size_t)stride * G * elem_bytes + 15) & ~(size_t)15));
+}
+
 template <typename T, int G, typename E, bool kGlobal>
 static int launch_lists_t(const E *lists, const uint32_t *lstart, uint64_t total10, const uint16_t *list_len,
                           uint32_t num_pep, int64_t stride, const uint32_t *wb, const uint32_t *we,
@@ -707,10 +721,8 @@ static int launch_lists_t(const E *lists, const uint32_t *lstart, uint64_t total
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (nw <= 0) nw = 16;
-    const size_t tile = kGlobal ? 0 : (((size_t)stride * G * sizeof(T) + 15) & ~(size_t)15);
-    // the warps' admission queues follow the tile
-    const size_t qoff = 128 + tile;
+    if (nw <= 0) nw = list_warps(G);
+    const size_t qoff = lists_queue_offset(kGlobal, stride, G, sizeof(T));
     const size_t smem = qoff + (size_t)nw * CtaSlots<G>::warp_bytes();
     if (smem > (size_t)smem_max) return (int)cudaErrorInvalidValue;
     auto fn = k_score_lists<T, G, E, kGlobal>;
@@ -724,6 +736,21 @@ static int launch_lists_t(const E *lists, const uint32_t *lstart, uint64_t total
                                     stride, wb, we, ws.perm, ws.groups, ws.item_off, ws.ngroups, K,
                                     ws.counter, part_s, part_k, stats, (uint32_t)qoff, err);
     return (int)cudaGetLastError();
+}
+
+int hfx_lists_group_fits(int32_t G, int long_rows, int64_t stride, int elem_bytes) {
+    if (G != 16) return 1;
+    int dev = 0, smem_max = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa{};
+    const cudaError_t e =
+        long_rows ? cudaFuncGetAttributes(&fa, k_score_lists<__nv_bfloat16, 16, uint32_t, true>)
+                  : cudaFuncGetAttributes(&fa, k_score_lists<__nv_bfloat16, 16, uint16_t, false>);
+    if (e != cudaSuccess) return 0;
+    const size_t smem = lists_queue_offset(long_rows != 0, stride, 16, (size_t)elem_bytes) +
+                        (size_t)list_warps(16) * CtaSlots<16>::warp_bytes();
+    return smem + fa.sharedSizeBytes <= (size_t)smem_max ? 1 : 0;
 }
 
 int hfx_lists_score(const void *lists, int long_rows, const uint32_t *lstart, uint64_t total10,
@@ -747,11 +774,13 @@ int hfx_lists_score(const void *lists, int long_rows, const uint32_t *lstart, ui
         if (G == 1) HFX_L(float, 1);
     } else if (elem_kind == 1) {
         if (G == 8) HFX_L(__nv_bfloat16, 8);
+        if (G == 16) HFX_L(__nv_bfloat16, 16);
         if (G == 4) HFX_L(__nv_bfloat16, 4);
         if (G == 2) HFX_L(__nv_bfloat16, 2);
         if (G == 1) HFX_L(__nv_bfloat16, 1);
     } else {
         if (G == 8) HFX_L(__half, 8);
+        if (G == 16) HFX_L(__half, 16);
         if (G == 4) HFX_L(__half, 4);
         if (G == 2) HFX_L(__half, 2);
         if (G == 1) HFX_L(__half, 1);

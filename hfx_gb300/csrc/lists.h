@@ -27,6 +27,9 @@ int hfx_lists_score(const void *lists, int long_rows, const uint32_t *lstart, ui
                     const uint16_t *list_len, uint32_t num_pep, int elem_kind, int64_t stride, const uint32_t *wb,
                     const uint32_t *we, const hfx::BatchedWs &ws, void *tiles, int32_t G, int32_t K, int nw,
                     float *part_s, uint64_t *part_k, unsigned long long *stats, uint32_t *err, cudaStream_t st);
+// Whether a G-spectrum group tile of rows `stride` bins long (and the
+// scorer's queues) fits in shared memory; always 1 for G <= 8.
+int hfx_lists_group_fits(int32_t G, int long_rows, int64_t stride, int elem_bytes);
 // Long rows: 32-bit lists built by sorting each (peptide, level)'s ion keys,
 // and FP32 rescoring of kept unmodified candidates from those lists.
 int hfx_lists_generate_long(const hfx::DevDB &db, const int32_t *cover, int64_t npep1, int32_t nbins,

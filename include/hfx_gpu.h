@@ -45,7 +45,8 @@ typedef struct hfx_search_params {
     int32_t fastdiv;               /* 1: __fdividef in ion m/z, as ion_series.cu:59-69         */
     int32_t search_plain;          /* score unmodified candidates                              */
     int32_t search_mods;           /* score variable-modification isoforms (needs hfx_set_mods) */
-    int32_t group_size;            /* spectra per batched work item (1..8), 0 = default       */
+    int32_t group_size;            /* spectra per work item: 1, 2, 4, 8, or 16 (BF16/FP16 list
+                                      scoring without modifications); 0 = default               */
     int32_t chunk;                 /* candidates per batched work item, 0 = default            */
     int32_t max_len;               /* longest spectrum row accepted, 0 = default (262,144)     */
     int32_t ion_bins_custom;       /* 1: ion bins use bin_width too (new; the reference bins

@@ -147,6 +147,14 @@ def test_search_mods_lowp_rescore(mods_full, oracle, precision):
     _compare(res, ref, f"mods precision {precision}")
 
 
+def test_group16_refused_with_mods(mods_tiny):
+    import hfx_gb300
+    eng, prot, sp = mods_tiny
+    with pytest.raises(hfx_gb300.HfxError):
+        eng.search(sp.subset(np.arange(8)), hfx_gb300.default_params(top_n=10, batch_mode=1, precision=1,
+                                                                     group_size=16))
+
+
 def test_search_mods_only_and_per_type(gpulib, tiny, oracle):
     """Modified candidates alone (no unmodified search) and the per-acid
     i-th counter."""

@@ -212,6 +212,29 @@ def test_batched_lowp_rescore_matches_fp32(full_engine, oracle, precision, mode)
     _compare(res, ref, f"precision {precision} mode {mode}")
 
 
+@pytest.mark.parametrize("chunk", [512, 4096])
+@pytest.mark.parametrize("precision", [1, 2])
+def test_group16_lowp_rescore(full_engine, oracle, precision, chunk):
+    """16-spectrum groups (two 16-byte tile loads per bin, reduce-scatter
+    over 16 slots): the FP32-rescored top-10 equals the oracle's."""
+    import hfx_gb300
+    eng, prot, sp = full_engine
+    ref = oracle.search(*_oracle_db(oracle, eng, prot), sp, topn=10)
+    res = eng.search(sp, hfx_gb300.default_params(top_n=10, batch_mode=1, precision=precision, rescore_k=32,
+                                                  group_size=16, chunk=chunk))
+    _compare(res, ref, f"G=16 precision {precision} chunk {chunk}")
+
+
+def test_group16_needs_lowp_lists(full_engine):
+    """group_size 16 is refused for FP32 rows and for the fused batch mode."""
+    import hfx_gb300
+    eng, prot, sp = full_engine
+    sub = sp.subset(np.arange(8))
+    for kw in (dict(precision=0, batch_mode=1), dict(precision=1, batch_mode=2)):
+        with pytest.raises(hfx_gb300.HfxError):
+            eng.search(sub, hfx_gb300.default_params(top_n=10, group_size=16, **kw))
+
+
 def test_batched_tiny_and_edges(tiny_engine, oracle):
     import hfx_gb300
     eng, prot, sp = tiny_engine
@@ -290,6 +313,10 @@ def test_long_rows_search(tiny_engine, oracle, precision, ion_custom):
                                  precision=precision, rescore_k=32, ion_bins_custom=ion_custom)
     res = eng.search(sub, p)
     _compare(res, ref, f"0.02 Da precision={precision} ion_custom={ion_custom}")
+    if precision:
+        p.group_size = 16
+        res = eng.search(sub, p)
+        _compare(res, ref, f"0.02 Da G=16 precision={precision} ion_custom={ion_custom}")
     if ion_custom:
         assert (ref[0][:, 0] > 0).mean() > 0.9   # the source peptides score
 
@@ -339,7 +366,7 @@ def test_autotune_picks_a_valid_shape(full_engine):
                pep=torch.empty((120, 10), dtype=torch.int32, device="cuda"),
                ncand=torch.empty(120, dtype=torch.int64, device="cuda"))
     ms = eng.autotune(dev, p, out, reps=1)
-    assert ms > 0 and p.group_size in (4, 8) and p.chunk in (1024, 2048, 4096, 8192, 16384)
+    assert ms > 0 and p.group_size in (4, 8, 16) and p.chunk in (1024, 2048, 4096, 8192, 16384)
     res = eng.search(sub, p)
     assert np.array_equal(res.key, ref.key)
     assert np.array_equal(res.score.view(np.uint32), ref.score.view(np.uint32))
