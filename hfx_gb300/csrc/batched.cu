@@ -151,8 +151,14 @@ __global__ void k_groups(const uint32_t *__restrict__ bucket_off, const uint32_t
     if (gi.hi <= gi.lo) {
         gi.lo = gi.hi = 0;
     }
-    // wide windows (open search) are cut into at most ~16 items per group
-    gi.chunk = group_chunk(gi.hi - gi.lo, chunk);
+    // wide windows (open search) are cut into at most ~16 items per group;
+    // the groups dispensed last take shorter items (the last quarter 1/4,
+    // the last sixteenth 1/16 of the chunk), so the grid ends evenly
+    const uint32_t ng = grp_start[kClasses];
+    const int32_t cg = (uint32_t)g >= ng - ng / 16 ? max(chunk / 16, 256)
+                       : (uint32_t)g >= ng - ng / 4 ? max(chunk / 4, 256)
+                                                    : chunk;
+    gi.chunk = group_chunk(gi.hi - gi.lo, cg);
     groups[g] = gi;
     nchunks[g] = (gi.hi - gi.lo + gi.chunk - 1) / gi.chunk;
 }
