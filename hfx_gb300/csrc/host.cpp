@@ -79,6 +79,7 @@ struct hfx_ctx {
     // database (residual-mass order on the device)
     uint64_t num_ions = 0, num_pep = 0;
     uint64_t ladder_residues = 0;  // sum over fragments of (tn - tc)
+    uint64_t list_units = 0;       // sum over fragments of 10 (tn - tc) rounded up to 8 entries
     uint32_t max_ladder = 0;       // max over fragments of (tn - tc)
     DBuf d_lstart;                 // per mass-order position: 10 * prefix sum of (tn - tc)
     unsigned long long counters[8] = {0};
@@ -232,19 +233,24 @@ int32_t upload_db(hfx_ctx *ctx) {
     std::vector<float> rs(np);
     std::vector<uint32_t> tcs(np), tns(np);
     ctx->ladder_residues = 0;
+    ctx->list_units = 0;
     ctx->max_ladder = 0;
+    // list slots: 10 entries per prefix, rounded up to 8 entries so that every
+    // (level, fragment) slot starts on a 16-byte boundary
     std::vector<uint32_t> lstart(np);
     for (uint64_t i = 0; i < np; ++i) {
         rs[i] = ctx->h_r[ctx->h_idx[i]];
         tcs[i] = ctx->h_tc[ctx->h_idx[i]];
         tns[i] = ctx->h_tn[ctx->h_idx[i]];
         if (tns[i] < tcs[i] || tns[i] > ctx->num_ions) return fail(ctx, HFX_ERR_ARG, "fragment outside the residues");
-        if (10ull * ctx->ladder_residues > 0xFFFFFFFFull)
+        if (ctx->list_units > 0xFFFFFFFFull)
             return fail(ctx, HFX_ERR_UNSUPPORTED, "ion-list offsets exceed 32 bits");
-        lstart[i] = (uint32_t)(10ull * ctx->ladder_residues);
+        lstart[i] = (uint32_t)ctx->list_units;
         ctx->ladder_residues += tns[i] - tcs[i];
+        ctx->list_units += (10ull * (tns[i] - tcs[i]) + 7ull) & ~7ull;
         ctx->max_ladder = std::max(ctx->max_ladder, tns[i] - tcs[i]);
     }
+    if (ctx->list_units > 0xFFFFFFFFull) return fail(ctx, HFX_ERR_UNSUPPORTED, "ion-list offsets exceed 32 bits");
     std::vector<uint8_t> packed;
     pack_ions(ctx->h_ascii, ctx->ma, ctx->num_ma, packed);
     HFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
@@ -546,8 +552,9 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
         if (e) return cuda_fail(ctx, e, "alloc");
         uint16_t *llen = ctx->buf<uint16_t>("l_len", (size_t)kLevels * ctx->num_pep, e);
         if (e) return cuda_fail(ctx, e, "alloc");
-        // static slots: 10 ions per prefix and charge, levels 1..4 (1+2+3+4)
-        const uint64_t total10 = 10ull * ctx->ladder_residues;
+        // static slots: 10 ions per prefix and charge (rounded up to 8
+        // entries per fragment), levels 1..4 (1+2+3+4)
+        const uint64_t total10 = ctx->list_units;
         void *lists = long_rows ? (void *)ctx->buf<uint32_t>("l_lists32", total10 * 10 + 64, e)
                                 : (void *)ctx->buf<uint16_t>("l_lists", total10 * 10 + 64, e);
         if (e) return cuda_fail(ctx, e, "alloc lists");
@@ -569,7 +576,8 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
                                          p->ion_bins_custom ? p->bin_width : 0.0f, stats,
                                          ctx->d_err.as<uint32_t>(), ctx->stream);
         else if (!rc)
-            rc = hfx_lists_generate(db, cover, npep1, kMaxWords * 32, ctx->d_lstart.as<uint32_t>(), total10,
+            rc = hfx_lists_generate(db, cover, npep1, (int32_t)std::min<int64_t>(stride, kMaxWords * 32),
+                                    ctx->d_lstart.as<uint32_t>(), total10,
                                     (uint16_t *)lists, llen, (int32_t)std::min<uint64_t>(40ull * ctx->max_ladder,
                                                                                          kMaxListLen),
                                     p->fastdiv, stats, ctx->d_err.as<uint32_t>(), ctx->stream);

@@ -155,7 +155,8 @@ __device__ __forceinline__ int compact_planes(const Planes &pl, WordRange wr, bo
 }
 
 // Offset of the list of (level z, mass-order position p): every level has a
-// static region; position p's slot holds up to 10 * z * (tn - tc) entries.
+// static region; position p's slot holds z * (10 (tn - tc) rounded up to 8)
+// entries and starts on a 16-byte boundary.
 __device__ __forceinline__ uint64_t list_offset(const uint32_t *__restrict__ lstart, uint64_t total10, int z,
                                                 uint32_t p) {
     return total10 * (uint64_t)(z * (z - 1) / 2) + (uint64_t)z * lstart[p];
@@ -208,8 +209,12 @@ __global__ void __launch_bounds__(256) k_gen_lists(DevDB db, const int32_t *__re
                 if (lane == 0) atomicOr(err, kErrListOverflow);
                 n = list_cap;
             }
+            // 16-byte copies: the slot and the staging list start on 16-byte
+            // boundaries and hold n rounded up to 8 entries
             const uint64_t off = list_offset(lstart, total10, z, p);
-            for (int i = lane; i < n; i += 32) lists[off + i] = list[i];
+            const uint4 *src = reinterpret_cast<const uint4 *>(list);
+            uint4 *dst = reinterpret_cast<uint4 *>(lists + off);
+            for (int i = lane; i < ((n + 7) >> 3); i += 32) dst[i] = src[i];
             if (lane == 0) list_len[(size_t)(z - 1) * db.num_pep + p] = (uint16_t)n;
             my_lists += 1;
             my_entries += (unsigned long long)n;
@@ -686,7 +691,7 @@ int hfx_lists_generate(const DevDB &db, const int32_t *cover, int64_t npep1, int
                        unsigned long long *stats, uint32_t *err, cudaStream_t st) {
     const int nw = 8;
     const int32_t words = (nbins + 31) / 32;
-    list_cap = std::max(32, std::min(list_cap, kMaxListLen));
+    list_cap = (std::max(32, std::min(list_cap, kMaxListLen)) + 7) & ~7;  // 16-byte staging lists
     // per warp: three bit planes and a staging list of list_cap entries
     const size_t smem = (size_t)nw * 3 * words * 4 + (size_t)nw * list_cap * 2;
     int dev = 0, sms = 0;
