@@ -16,8 +16,9 @@ struct LayoutParams {
     int32_t custom_bw;  // 1: custom width, the length formula divides the cutoff
     int32_t remove_pcr; // remove-precursor-peak (Correlation.hs:69-71)
     int32_t ppm;        // 0 Da, 1 ppm, 2 per spectrum: negative = ppm (new; the reference has Da only)
-    int32_t max_len;    // longest row accepted
-    int32_t flag_long;  // 1: a longer row sets kErrTooLong (graph replays with a fixed row stride)
+    int32_t max_len;    // longest row accepted (longer spectra get status 2 and score nothing)
+    int32_t cap_len;    // > 0: an accepted row longer than this sets kErrTooLong (graph replays,
+                        // whose row stride is fixed at capture)
 };
 
 // Per-spectrum metadata computed on the device (k_layout).

@@ -137,6 +137,7 @@ struct hfx_ctx {
     // stage whose kernels reported an error (for locating device faults)
     bool debug_sync = false;
     std::string fault_stage;
+    std::string err_stage;  // with debug_sync: the first stage after which the device error word was set
     void stage_end(int s, int64_t launches, int64_t units = 0) {
         if (gmode == 2) return;
         stage_launches[s] += launches;
@@ -146,6 +147,10 @@ struct hfx_ctx {
                                                      "rescore", "mods", "lists", "pack"};
             const cudaError_t e = cudaStreamSynchronize(stream);
             if (e != cudaSuccess) fault_stage = names[s];
+            uint32_t w = 0;
+            if (e == cudaSuccess && err_stage.empty() && d_err.p &&
+                cudaMemcpy(&w, d_err.p, 4, cudaMemcpyDeviceToHost) == cudaSuccess && w)
+                err_stage = std::string(names[s]) + " (word " + std::to_string(w) + ")";
         }
         if (!profile) return;
         cudaEventRecord(ev[s][1], stream);
@@ -201,6 +206,7 @@ int32_t cuda_fail(hfx_ctx *c, cudaError_t e, const char *where) {
         return fail(c, HFX_ERR_OOM, std::string(where) + ": " + cudaGetErrorString(e));
     std::string msg = std::string(where) + ": " + cudaGetErrorString(e);
     if (c && !c->fault_stage.empty()) msg += " (first failing stage: " + c->fault_stage + ")";
+    if (c && !c->err_stage.empty()) msg += " (error word first set after stage: " + c->err_stage + ")";
     return fail(c, HFX_ERR_CUDA, msg);
 }
 #define HFX_CUDA(call, where)                         \
@@ -319,7 +325,7 @@ LayoutParams layout_params(const hfx_search_params *p) {
     lp.remove_pcr = p->remove_precursor_peak;
     lp.ppm = p->tol_ppm;
     lp.max_len = p->max_len > 0 ? p->max_len : kDefaultMaxLen;
-    lp.flag_long = 0;
+    lp.cap_len = 0;
     return lp;
 }
 
@@ -330,9 +336,9 @@ int32_t run_stage_a(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, in
     cudaError_t e;
     LayoutParams lp = layout_params(p);
     if (ctx->gmode >= 1) {
-        // graph replays keep the row stride of the capture: longer rows are errors
-        lp.max_len = (int32_t)std::min<int64_t>(lp.max_len, ctx->cap_stride);
-        lp.flag_long = 1;
+        // graph replays keep the row stride of the capture: longer accepted
+        // rows are reported (and the batch re-planned)
+        lp.cap_len = (int32_t)std::min<int64_t>(lp.max_len, ctx->cap_stride);
     }
     meta = ctx->buf<SpecMeta>("meta", b.nspec, e);
     if (e) return cuda_fail(ctx, e, "alloc meta");

@@ -47,7 +47,9 @@ __global__ void k_layout(const float *__restrict__ mz, const int64_t *__restrict
         const float c = lp.custom_bw ? __fdiv_rn(m.cutoff, lp.bw) : m.cutoff;
         const double len = 75.0 + ceil((double)c);
         if (!(len >= 76.0) || len > (double)lp.max_len) {
-            if (lp.flag_long && len > (double)lp.max_len && err) atomicOr(err, kErrTooLong);
+            m.status = 2;
+        } else if (lp.cap_len > 0 && len > (double)lp.cap_len) {
+            if (err) atomicOr(err, kErrTooLong);
             m.status = 2;
         } else {
             m.len = (int32_t)len;

@@ -351,6 +351,46 @@ def test_graph_replay_matches_eager(full_engine, oracle, precision):
     _compare(eng.search(a, pg), oracle.search(*_oracle_db(oracle, eng, prot), a, topn=10), "graph")
 
 
+@pytest.mark.parametrize("mixed", [False, True])
+def test_graph_replay_long_rows(tiny_engine, mixed):
+    """use_graph at 0.02 Da (32-bit lists, tiles read from L2), with and
+    without wide windows: replays equal the eager search."""
+    import hfx_gb300
+    eng, prot, sp = tiny_engine
+    sub = _highres_subset(sp, 24)
+    kw = dict(top_n=10, bin_width=HIGHRES, custom_bin_width=1, batch_mode=1, precision=1, rescore_k=32,
+              ion_bins_custom=1)
+    if mixed:
+        sub.tol[:] = -10.0
+        sub.tol[::4] = 500.0
+        kw["tol_ppm"] = 2
+    ref = eng.search(sub, hfx_gb300.default_params(**kw))
+    pg = hfx_gb300.default_params(use_graph=1, **kw)
+    for rep in range(3):
+        res = eng.search(sub, pg)
+        assert np.array_equal(res.key, ref.key), rep
+        assert np.array_equal(res.score.view(np.uint32), ref.score.view(np.uint32)), rep
+
+
+def test_graph_replay_skips_rows_beyond_max_len(full_engine, oracle):
+    """Spectra whose rows exceed max_len score nothing in eager searches;
+    graph replays treat them the same way (no error)."""
+    import hfx_gb300
+    eng, prot, sp = full_engine
+    sub = sp.subset(np.arange(0, 64))
+    lens = [len(oracle.preprocess(sub.mz[sub.off[i]:sub.off[i + 1]], sub.it[sub.off[i]:sub.off[i + 1]], sub.pcr[i],
+                                  sub.z[i])) for i in range(len(sub))]
+    cut = int(np.median(lens))
+    kw = dict(top_n=10, batch_mode=1, precision=1, max_len=cut)
+    ref = eng.search(sub, hfx_gb300.default_params(**kw))
+    assert (ref.ncand == 0).sum() > 5 and (ref.ncand > 0).sum() > 5
+    pg = hfx_gb300.default_params(use_graph=1, **kw)
+    for rep in range(3):
+        res = eng.search(sub, pg)
+        assert np.array_equal(res.key, ref.key), rep
+        assert np.array_equal(res.ncand, ref.ncand), rep
+
+
 def test_autotune_picks_a_valid_shape(full_engine):
     """hfx_autotune times the batched search over group and work-item sizes
     and writes the fastest into the parameters; the tuned search returns the
