@@ -97,19 +97,20 @@ k_score_mods(DevDB db, DevMods mods, const T *__restrict__ tiles, int64_t stride
     const int32_t words_cap = (int32_t)((stride + 31) / 32);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     T *stile = reinterpret_cast<T *>(smem + 128);
-    // after an item's isoforms the tile region holds the warps' survivors
-    const int cap = nw * K;
-    uint64_t *buf_k = reinterpret_cast<uint64_t *>(smem + 128);
-    float *buf_s = reinterpret_cast<float *>(buf_k + (size_t)G * cap);
     uint8_t *wbase = smem + 128 + fused_region_bytes(stride, sizeof(T), G, nw, K, 8) +
                      (size_t)warp * fused_warp_bytes(words_cap);
+    // the warps' admission queues follow the fused layout
+    uint8_t *my_queue = smem + fused_smem_bytes(stride, sizeof(T), G, nw, K, 8) +
+                        (size_t)warp * CtaSlots<G, uint64_t>::warp_bytes();
     uint32_t *planes = reinterpret_cast<uint32_t *>(wbase);
     uint16_t *list = reinterpret_cast<uint16_t *>(planes + 3 * words_cap);
     __shared__ int32_t s_item;
     __shared__ uint32_t s_next;
     __shared__ uint32_t s_wb[G], s_we[G];
     __shared__ int32_t s_spec[G];
-    __shared__ uint32_t thr_u[G], cnt[G];
+    __shared__ uint32_t thr_u[G], s_lock[G];
+    __shared__ float s_ls[G * 32];
+    __shared__ uint64_t s_lk[G * 32];
 
     const uint32_t total = item_off[n_gm];
     if (threadIdx.x == 0) mbar_init(bar, 1);
@@ -124,7 +125,8 @@ k_score_mods(DevDB db, DevMods mods, const T *__restrict__ tiles, int64_t stride
     iso.per_type = mods.per_type;
 #pragma unroll
     for (int i = 0; i < kMaxMa; ++i) iso.ma_mass[i] = mods.ma_mass[i];
-    WarpSlots<G, uint64_t> slots;
+    CtaSlots<G, uint64_t> slots;
+    slots.bind(s_ls, s_lk, s_lock, thr_u, my_queue, err);
 
     while (true) {
         if (threadIdx.x == 0) s_item = (int32_t)atomicAdd(counter, 1u);
@@ -149,10 +151,8 @@ k_score_mods(DevDB db, DevMods mods, const T *__restrict__ tiles, int64_t stride
             s_wb[j] = b;
             s_we[j] = e;
             s_spec[j] = s;
-            thr_u[j] = 0u;
-            cnt[j] = 0u;
         }
-        slots.init();
+        slots.reset_shared();
         if (threadIdx.x == 0) s_next = p0;
         const int32_t nb = tile_bins(gi.maxlen);
         if (threadIdx.x == 0) {
@@ -207,19 +207,16 @@ k_score_mods(DevDB db, DevMods mods, const T *__restrict__ tiles, int64_t stride
                 float acc[G];
                 planes_accumulate<G>(pl, list, wr, dot, acc);
                 const float sc = reduce_scatter<G>(acc);
-                const bool want =
-                    ((act >> my_slot) & 1u) && score_order(sc) >= *(volatile uint32_t *)(thr_u + my_slot);
-                const uint32_t ins = __ballot_sync(kFullMask, want) & slot_owner_mask<G>();
-                if (ins) slots.offer(sc, mod_key(mu, p, rank), ins, K, thr_u);
+                const bool want = (lane & (32 / G - 1)) == 0 && ((act >> my_slot) & 1u) &&
+                                  score_order(sc) >= *(volatile uint32_t *)(thr_u + my_slot);
+                slots.offer(want, sc, mod_key(mu, p, rank), my_slot, K);
             }
         }
-        __syncthreads();  // every warp is done with the tile: its region takes the survivors
-        slots.flush(thr_u, cnt, buf_s, buf_k, cap, K);
-        __syncthreads();
+        slots.drain(K);
+        __syncthreads();  // every warp has merged its queues
         for (int j = warp; j < cnt_members; j += nw) {
             const size_t o = ((size_t)item * G + j) * K;
-            slot_merge(buf_s + (size_t)j * cap, buf_k + (size_t)j * cap, min(cnt[j], (uint32_t)cap), K, part_s + o,
-                       part_k + o);
+            slots.result(j, K, part_s + o, part_k + o);
         }
         __syncthreads();
     }
@@ -371,9 +368,12 @@ static int launch_mods_t(const DevDB &db, const DevMods &m, const void *tiles, i
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    const int nw = std::min(kModWarps, fused_warps(stride, sizeof(T), G, K, 8, (size_t)smem_max));
+    // the fused layout plus every warp's admission queue
+    const size_t qb = CtaSlots<G, uint64_t>::warp_bytes();
+    int nw = std::min(kModWarps, fused_warps(stride, sizeof(T), G, K, 8, (size_t)smem_max));
+    while (nw >= 1 && fused_smem_bytes(stride, sizeof(T), G, nw, K, 8) + (size_t)nw * qb > (size_t)smem_max) --nw;
     if (nw < 1) return (int)cudaErrorInvalidValue;
-    const size_t smem = fused_smem_bytes(stride, sizeof(T), G, nw, K, 8);
+    const size_t smem = fused_smem_bytes(stride, sizeof(T), G, nw, K, 8) + (size_t)nw * qb;
     auto fn = k_score_mods<F, T, G>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
