@@ -175,18 +175,18 @@ k_score_batched(DevDB db, const T *__restrict__ tiles, int64_t stride, const uin
     const int32_t words_cap = (int32_t)((stride + 31) / 32);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     T *stile = reinterpret_cast<T *>(smem + 128);
-    // after an item's candidates the tile region holds the warps' survivors
-    const int cap = nw * K;
-    float *buf_s = reinterpret_cast<float *>(smem + 128);
-    uint32_t *buf_k = reinterpret_cast<uint32_t *>(buf_s + (size_t)G * cap);
-    uint8_t *wbase = smem + 128 + fused_region_bytes(stride, sizeof(T), G, nw, K, 4) +
-                     (size_t)warp * fused_warp_bytes(words_cap);
+    constexpr size_t kQueue = CtaSlots<G>::warp_bytes();
+    uint8_t *wbase = smem + 128 + fused_tile_bytes(stride, sizeof(T), G) +
+                     (size_t)warp * fused_warp_bytes(words_cap, kQueue);
+    uint8_t *my_queue = wbase + fused_queue_offset(words_cap);
     uint32_t *planes = reinterpret_cast<uint32_t *>(wbase);
     uint16_t *list = reinterpret_cast<uint16_t *>(planes + 3 * words_cap);
     __shared__ int32_t s_item;
     __shared__ uint32_t s_next;
     __shared__ uint32_t s_wb[G], s_we[G];
-    __shared__ uint32_t thr_u[G], cnt[G];
+    __shared__ uint32_t thr_u[G], s_lock[G];
+    __shared__ float s_ls[G * 32];
+    __shared__ uint32_t s_lk[G * 32];
 
     const int32_t ngroups = (int32_t)*ngroups_p;
     const uint32_t total = item_off[ngroups];
@@ -197,7 +197,8 @@ k_score_batched(DevDB db, const T *__restrict__ tiles, int64_t stride, const uin
     const float mt_lane = db.mt[lane];
     const int my_slot = reduce_slot_of_lane<G>(lane);
     uint32_t phase = 0;
-    WarpSlots<G> slots;
+    CtaSlots<G> slots;
+    slots.bind(s_ls, s_lk, s_lock, thr_u, my_queue, err);
 
     while (true) {
         if (threadIdx.x == 0) s_item = (int32_t)atomicAdd(counter, 1u);
@@ -219,10 +220,8 @@ k_score_batched(DevDB db, const T *__restrict__ tiles, int64_t stride, const uin
             }
             s_wb[j] = b;
             s_we[j] = e;
-            thr_u[j] = 0u;
-            cnt[j] = 0u;
         }
-        slots.init();
+        slots.reset_shared();
         if (threadIdx.x == 0) s_next = p0;
         const int32_t nb = tile_bins(gi.maxlen);
         if (threadIdx.x == 0) {
@@ -253,17 +252,15 @@ k_score_batched(DevDB db, const T *__restrict__ tiles, int64_t stride, const uin
             float acc[G];
             planes_accumulate<G>(pl, list, wr, dot, acc);
             const float sc = reduce_scatter<G>(acc);
-            const bool want = ((act >> my_slot) & 1u) && score_order(sc) >= *(volatile uint32_t *)(thr_u + my_slot);
-            const uint32_t ins = __ballot_sync(kFullMask, want) & slot_owner_mask<G>();
-            if (ins) slots.offer(sc, p, ins, K, thr_u);
+            const bool want = (lane & (32 / G - 1)) == 0 && ((act >> my_slot) & 1u) &&
+                              score_order(sc) >= *(volatile uint32_t *)(thr_u + my_slot);
+            slots.offer(want, sc, p, my_slot, K);
         }
-        __syncthreads();  // every warp is done with the tile: its region takes the survivors
-        slots.flush(thr_u, cnt, buf_s, buf_k, cap, K);
-        __syncthreads();
+        slots.drain(K);
+        __syncthreads();  // every warp has merged its queues
         for (int j = warp; j < cnt_members; j += nw) {
             const size_t o = ((size_t)item * G + j) * K;
-            slot_merge(buf_s + (size_t)j * cap, buf_k + (size_t)j * cap, min(cnt[j], (uint32_t)cap), K, part_s + o,
-                       part_k + o);
+            slots.result(j, K, part_s + o, part_k + o);
         }
         __syncthreads();
     }
@@ -419,7 +416,8 @@ __global__ void k_ncand(const uint32_t *__restrict__ wb, const uint32_t *__restr
 using namespace hfx;
 
 size_t hfx_batched_smem(int64_t stride, int elem_bytes, int G, int nw, int K) {
-    return fused_smem_bytes(stride, elem_bytes, G, nw, K, 4);
+    (void)K;
+    return fused_smem_bytes(stride, elem_bytes, G, nw, cta_queue_bytes(G, 4));
 }
 
 int hfx_batched_plan(const SpecMeta *meta, int32_t nspec, const uint32_t *wb, const uint32_t *we, int32_t G,
@@ -449,10 +447,13 @@ static int launch_batched_t(const DevDB &db, const T *rows, int64_t stride, cons
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (nw <= 0) nw = fused_warps(stride, sizeof(T), G, K, 4, (size_t)smem_max);
+    auto fn = k_score_batched<F, T, G>;
+    cudaFuncAttributes fa{};
+    cudaFuncGetAttributes(&fa, fn);  // static shared memory counts against the same limit
+    const size_t avail = (size_t)smem_max > fa.sharedSizeBytes ? (size_t)smem_max - fa.sharedSizeBytes : 0;
+    if (nw <= 0) nw = std::min(fused_warps(stride, sizeof(T), G, cta_queue_bytes(G, 4), avail), 24);
     if (nw < 1) return (int)cudaErrorInvalidValue;
     const size_t smem = hfx_batched_smem(stride, sizeof(T), G, nw, K);
-    auto fn = k_score_batched<F, T, G>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
     if (grid <= 0) {

@@ -73,47 +73,27 @@ __global__ void k_pack_tiles(const T *__restrict__ rows, int64_t stride, const S
     }
 }
 
-// Warp-cooperative insert into a sorted shared-memory list (entry i at
-// lane i); returns the new K-th score (the admission threshold).
-__device__ __forceinline__ float smem_topk_insert(float *ks, uint64_t *kk, float ns, uint64_t nk, int K) {
-    const int lane = threadIdx.x & 31;
-    const float cs = lane < K ? ks[lane] : -INFINITY;
-    const uint64_t ck = lane < K ? kk[lane] : ~0ull;
-    const bool mine_better = (lane < K) && better(cs, ck, ns, nk);
-    const int pos = __popc(__ballot_sync(kFullMask, mine_better));
-    const float us = __shfl_up_sync(kFullMask, cs, 1);
-    const uint64_t uk = __shfl_up_sync(kFullMask, ck, 1);
-    float out = cs;
-    __syncwarp();
-    if (pos < K) {
-        if (lane == pos) { ks[lane] = ns; kk[lane] = nk; out = ns; }
-        else if (lane > pos && lane < K) { ks[lane] = us; kk[lane] = uk; out = us; }
-    }
-    __syncwarp();
-    return __shfl_sync(kFullMask, out, K - 1);
-}
-
 // Shared-memory layout of the fused scorers (unmodified and modified): an
-// mbarrier, the group tile -- which after an item holds the warps'
-// surviving top-K entries -- and per warp three bit planes and a list.
-__host__ __device__ __forceinline__ size_t fused_warp_bytes(int32_t words) {
+// mbarrier, the group tile, and per warp three bit planes, a list and the
+// warp's admission queue (queue_bytes).
+__host__ __device__ __forceinline__ size_t fused_queue_offset(int32_t words) {
     return ((size_t)3 * words * 4 + (size_t)kListCap * 2 + 15) & ~(size_t)15;
 }
-__host__ __device__ __forceinline__ size_t fused_region_bytes(int64_t stride, int elem_bytes, int G, int nw, int K,
-                                                              int key_bytes) {
-    const size_t tile = ((size_t)stride * G * elem_bytes + 15) & ~(size_t)15;
-    const size_t surv = ((size_t)G * nw * K * (4 + key_bytes) + 15) & ~(size_t)15;
-    return tile > surv ? tile : surv;
+__host__ __device__ __forceinline__ size_t fused_warp_bytes(int32_t words, size_t queue_bytes) {
+    return (fused_queue_offset(words) + queue_bytes + 15) & ~(size_t)15;
 }
-__host__ __device__ __forceinline__ size_t fused_smem_bytes(int64_t stride, int elem_bytes, int G, int nw, int K,
-                                                            int key_bytes) {
-    return 128 + fused_region_bytes(stride, elem_bytes, G, nw, K, key_bytes) +
-           (size_t)nw * fused_warp_bytes((int32_t)((stride + 31) / 32));
+__host__ __device__ __forceinline__ size_t fused_tile_bytes(int64_t stride, int elem_bytes, int G) {
+    return ((size_t)stride * G * elem_bytes + 15) & ~(size_t)15;
+}
+__host__ __device__ __forceinline__ size_t fused_smem_bytes(int64_t stride, int elem_bytes, int G, int nw,
+                                                            size_t queue_bytes) {
+    return 128 + fused_tile_bytes(stride, elem_bytes, G) +
+           (size_t)nw * fused_warp_bytes((int32_t)((stride + 31) / 32), queue_bytes);
 }
 // Largest warp count (<= 24) whose layout fits in smem_max bytes, 0 if none.
-inline int fused_warps(int64_t stride, int elem_bytes, int G, int K, int key_bytes, size_t smem_max) {
+inline int fused_warps(int64_t stride, int elem_bytes, int G, size_t queue_bytes, size_t smem_max) {
     for (int nw = 24; nw >= 1; --nw)
-        if (fused_smem_bytes(stride, elem_bytes, G, nw, K, key_bytes) <= smem_max) return nw;
+        if (fused_smem_bytes(stride, elem_bytes, G, nw, queue_bytes) <= smem_max) return nw;
     return 0;
 }
 
@@ -126,86 +106,13 @@ __device__ __forceinline__ uint32_t score_order(float s) {
 // Lane that holds member slot j's score after reduce_scatter<G>.
 template <int G> __host__ __device__ constexpr int slot_lane(int j) { return j * (32 / G); }
 
-// Per-warp top-K of every member slot, in registers (lane i holds entry i
-// of each slot, best first).  A shared per-slot admission threshold -- the
-// best K-th score any warp of the CTA has reached, a lower bound of the
-// CTA's K-th -- filters the offers, so warps share what they learn without
-// locks; the CTA's top-K is the top-K of the union of the warps' lists.
-template <int G, typename Key = uint32_t>
-struct WarpSlots {
-    static constexpr Key kNone = ~Key(0);
-    float s[G];
-    Key k[G];
+// Queue entries per member slot of a warp, and a warp's queue bytes.
+__host__ __device__ constexpr int cta_queue_len(int G) { return G >= 16 ? 8 : 16; }
+__host__ __device__ constexpr size_t cta_queue_bytes(int G, int key_bytes) {
+    return (size_t)G * cta_queue_len(G) * (4 + key_bytes);
+}
 
-    __device__ __forceinline__ void init() {
-#pragma unroll
-        for (int j = 0; j < G; ++j) {
-            s[j] = -INFINITY;
-            k[j] = kNone;
-        }
-    }
-
-    // Offer candidate `key`: slot j's score sits in lane slot_lane<G>(j) of
-    // sc; ins has that lane's bit set when slot j takes the offer.
-    __device__ __forceinline__ void offer(float sc, Key key, uint32_t ins, int K, uint32_t *thr_u) {
-        const int lane = threadIdx.x & 31;
-#pragma unroll
-        for (int j = 0; j < G; ++j) {
-            if (ins & (1u << slot_lane<G>(j))) {
-                const float ns = __shfl_sync(kFullMask, sc, slot_lane<G>(j));
-                const bool mb = lane < K && (s[j] > ns || (s[j] == ns && k[j] < key));
-                const int pos = __popc(__ballot_sync(kFullMask, mb));
-                const float us = __shfl_up_sync(kFullMask, s[j], 1);
-                const Key uk = __shfl_up_sync(kFullMask, k[j], 1);
-                if (pos < K) {
-                    if (lane == pos) {
-                        s[j] = ns;
-                        k[j] = key;
-                    } else if (lane > pos && lane < K) {
-                        s[j] = us;
-                        k[j] = uk;
-                    }
-                    const float kth = __shfl_sync(kFullMask, s[j], K - 1);
-                    if (lane == 0 && kth != -INFINITY) {
-                        const uint32_t o = score_order(kth);
-                        if (o > *(volatile uint32_t *)(thr_u + j)) atomicMax(thr_u + j, o);
-                    }
-                }
-            }
-        }
-    }
-
-    // Item end, step 1: append the entries that can still be in the CTA's
-    // top-K (score order >= the final threshold) to the slot's buffer.
-    __device__ __forceinline__ void flush(const uint32_t *thr_u, uint32_t *cnt, float *buf_s, Key *buf_k, int cap,
-                                          int K) {
-        const int lane = threadIdx.x & 31;
-#pragma unroll
-        for (int j = 0; j < G; ++j) {
-            const bool keep = lane < K && k[j] != kNone && score_order(s[j]) >= thr_u[j];
-            const uint32_t bal = __ballot_sync(kFullMask, keep);
-            if (!bal) continue;
-            uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(cnt + j, (uint32_t)__popc(bal));
-            base = __shfl_sync(kFullMask, base, 0);
-            const uint32_t at = base + __popc(bal & ((1u << lane) - 1u));
-            if (keep && at < (uint32_t)cap) {
-                buf_s[j * cap + at] = s[j];
-                buf_k[j * cap + at] = k[j];
-            }
-        }
-    }
-};
-
-// CTA-wide top-K of every member slot with batched admission.  The CTA
-// keeps one list per slot in shared memory (entry i at lane i, best first:
-// higher score, then lower key).  An offer that passes the slot's threshold
-// is appended by the slot's lane to its warp's queue of kQ entries; a full
-// queue is sorted across the warp (bitonic) and merged into the slot's list
-// under the slot's lock, after which the threshold is the list's K-th score.
-// The list is the top-K of everything offered, as with one insertion per
-// offer.
-template <int G, typename Key = uint32_t, int Q = (G >= 16 ? 8 : 16)>
+template <int G, typename Key = uint32_t, int Q = cta_queue_len(G)>
 struct CtaSlots {
     static constexpr int kQ = Q;
     static constexpr Key kNone = ~Key(0);
@@ -218,7 +125,8 @@ struct CtaSlots {
     uint32_t qn;     // slot lanes: entries queued for the lane's slot
     uint32_t *err;
 
-    __host__ __device__ static constexpr size_t warp_bytes() { return (size_t)G * kQ * (4 + sizeof(Key)); }
+    __host__ __device__ static constexpr size_t warp_bytes() { return cta_queue_bytes(G, (int)sizeof(Key)); }
+    static_assert(Q == cta_queue_len(G), "queue length and cta_queue_bytes disagree");
 
     __device__ __forceinline__ void bind(float *ls_, Key *lk_, uint32_t *lock_, uint32_t *thr_, uint8_t *queue,
                                          uint32_t *err_) {
@@ -351,38 +259,6 @@ struct CtaSlots {
         }
     }
 };
-
-// Item end, step 2 (one warp per slot): the slot's top-K from its buffer.
-template <typename Key>
-__device__ __forceinline__ void slot_merge(const float *bs, const Key *bk, uint32_t n, int K, float *out_s,
-                                           uint64_t *out_k) {
-    const int lane = threadIdx.x & 31;
-    WarpTopK tk;
-    tk.init();
-    for (uint32_t b0 = 0; b0 < n; b0 += 32) {
-        const uint32_t i = b0 + lane;
-        const float es = i < n ? bs[i] : -INFINITY;
-        const Key ek = i < n ? bk[i] : ~Key(0);
-        const uint32_t m = min(32u, n - b0);
-        for (uint32_t t = 0; t < m; ++t)
-            tk.insert(__shfl_sync(kFullMask, es, t), (uint64_t)__shfl_sync(kFullMask, ek, t), K);
-    }
-    if (lane < K) {
-        out_s[lane] = tk.s;
-        out_k[lane] = tk.k;
-    }
-}
-
-template <int G>
-__device__ __forceinline__ uint32_t slot_owner_mask() {
-    // one lane per slot among the lanes that hold the same reduced slot
-    if constexpr (G == 16) return 0x55555555u;
-    else if constexpr (G == 8) return 0x11111111u;
-    else if constexpr (G == 4) return 0x01010101u;
-    else if constexpr (G == 2) return 0x00010001u;
-    else return 0x1u;
-}
-
 
 }  // namespace hfx
 

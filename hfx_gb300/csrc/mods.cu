@@ -97,11 +97,10 @@ k_score_mods(DevDB db, DevMods mods, const T *__restrict__ tiles, int64_t stride
     const int32_t words_cap = (int32_t)((stride + 31) / 32);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     T *stile = reinterpret_cast<T *>(smem + 128);
-    uint8_t *wbase = smem + 128 + fused_region_bytes(stride, sizeof(T), G, nw, K, 8) +
-                     (size_t)warp * fused_warp_bytes(words_cap);
-    // the warps' admission queues follow the fused layout
-    uint8_t *my_queue = smem + fused_smem_bytes(stride, sizeof(T), G, nw, K, 8) +
-                        (size_t)warp * CtaSlots<G, uint64_t>::warp_bytes();
+    constexpr size_t kQueue = CtaSlots<G, uint64_t>::warp_bytes();
+    uint8_t *wbase = smem + 128 + fused_tile_bytes(stride, sizeof(T), G) +
+                     (size_t)warp * fused_warp_bytes(words_cap, kQueue);
+    uint8_t *my_queue = wbase + fused_queue_offset(words_cap);
     uint32_t *planes = reinterpret_cast<uint32_t *>(wbase);
     uint16_t *list = reinterpret_cast<uint16_t *>(planes + 3 * words_cap);
     __shared__ int32_t s_item;
@@ -368,13 +367,14 @@ static int launch_mods_t(const DevDB &db, const DevMods &m, const void *tiles, i
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    // the fused layout plus every warp's admission queue
     const size_t qb = CtaSlots<G, uint64_t>::warp_bytes();
-    int nw = std::min(kModWarps, fused_warps(stride, sizeof(T), G, K, 8, (size_t)smem_max));
-    while (nw >= 1 && fused_smem_bytes(stride, sizeof(T), G, nw, K, 8) + (size_t)nw * qb > (size_t)smem_max) --nw;
-    if (nw < 1) return (int)cudaErrorInvalidValue;
-    const size_t smem = fused_smem_bytes(stride, sizeof(T), G, nw, K, 8) + (size_t)nw * qb;
     auto fn = k_score_mods<F, T, G>;
+    cudaFuncAttributes fa{};
+    cudaFuncGetAttributes(&fa, fn);  // static shared memory counts against the same limit
+    const size_t avail = (size_t)smem_max > fa.sharedSizeBytes ? (size_t)smem_max - fa.sharedSizeBytes : 0;
+    const int nw = std::min(kModWarps, fused_warps(stride, sizeof(T), G, qb, avail));
+    if (nw < 1) return (int)cudaErrorInvalidValue;
+    const size_t smem = fused_smem_bytes(stride, sizeof(T), G, nw, qb);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
     int occ = 0;
