@@ -13,20 +13,35 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _declared(header):
+    """Function names declared by a public header (return type, name, '(')."""
     text = open(os.path.join(ROOT, "include", header)).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(hfx_[a-z0-9_]+)\s*\(", text)))
+    ret = r"(?:void|u?int(?:8|16|32|64)_t|size_t|const char|char|float|double)"
+    return sorted(set(re.findall(ret + r"\s*\**\s+\**([A-Za-z_]\w*)\s*\(", text)))
 
 
 def test_library_exports_every_declared_symbol(gpulib):
     import hfx_gb300
     nm = subprocess.run(["nm", "-D", "--defined-only", hfx_gb300.LIB_PATH], capture_output=True, text=True).stdout
-    exported = set(re.findall(r"\bT (hfx_[a-z0-9_]+)\b", nm))
-    for h in sorted(os.listdir(os.path.join(ROOT, "include"))):
-        for sym in _declared(h):
+    exported = set(re.findall(r"\bT (\w+)\b", nm))
+    headers = sorted(os.listdir(os.path.join(ROOT, "include")))
+    assert "hfx_legacy.h" in headers
+    for h in headers:
+        syms = _declared(h)
+        assert syms, h
+        for sym in syms:
             assert sym in exported, (h, sym)
             assert hasattr(gpulib, sym)
     assert set(hfx_gb300.EXPORTED) <= exported
+
+
+def test_legacy_header_matches_the_reference_abi():
+    """The per-stage symbols the reference's Haskell host binds (Algorithms.hs
+    foreign imports of algorithms.h), every one declared with the C ABI."""
+    want = {"prepare_ions", "findIndicesInRange_f", "findSpecCandsByMass", "findBeginEnd_f",
+            "findModablePeptides", "calcTotalModCands", "prepareGenMod", "genModCands", "addModIons", "addIons",
+            "prepare_scoring", "sort_val_f", "sort_idx_f", "sort_rf", "sort_idx_rf", "sort_b40c_f", "mvm_ff"}
+    assert want <= set(_declared("hfx_legacy.h"))
 
 
 def test_product_digest_matches_oracle(gpulib, oracle, tiny):
