@@ -3,8 +3,9 @@ algorithms.h symbols), called through ctypes with device pointers the way
 the reference's Haskell host calls them.  Integer and ordering outputs are
 compared exactly with the oracle or with numpy restatements of the
 reference's semantics; the dense theoretical spectra use the reference's
-__fdividef ion arithmetic, so they are compared exactly with this library's
-fast-division ion bins and, row by row, with the oracle's IEEE bins."""
+__fdividef ion arithmetic, so they are compared row by row with the
+oracle's IEEE bins: equal except where fast division moves a bin that sits
+at a half-bin edge."""
 import ctypes as C
 import math
 
