@@ -30,7 +30,7 @@ EXPORTED = [
     "hfx_default_params", "hfx_ctx_create", "hfx_ctx_destroy", "hfx_set_stream",
     "hfx_last_error", "hfx_build_db", "hfx_upload_db", "hfx_db_info", "hfx_db_export", "hfx_autotune", "hfx_match_peptide",
     "hfx_set_protein_segments",
-    "hfx_set_mods", "hfx_mod_table", "hfx_search_host", "hfx_search_device",
+    "hfx_set_mods", "hfx_mod_table", "hfx_search_host", "hfx_search_device", "hfx_search_evalues",
     "hfx_preprocess", "hfx_find_windows", "hfx_ion_bins", "hfx_mod_isoforms", "hfx_digest", "hfx_pack_ions",
     "hfx_set_profiling", "hfx_stage_stats", "hfx_search_counters",
 ]
@@ -92,6 +92,8 @@ def load_library(path: str = LIB_PATH):
         "hfx_mod_table": (i32, [P, C.POINTER(i32), P, P, i32]),
         "hfx_search_host": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, P, i32, P, P, P, P]),
         "hfx_search_device": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, P, i32, P, P, P, P]),
+        "hfx_search_evalues": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, P, i32, i32, C.c_float, P, P, P, P,
+                                     P, P]),
         "hfx_autotune": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, P, i32, P, P, P, P, i32,
                                C.POINTER(C.c_float)]),
         "hfx_match_peptide": (i32, [P, u64, C.c_uint32, C.c_char_p, i32, C.POINTER(C.c_float),
@@ -291,6 +293,15 @@ class Engine:
             self.h, C.byref(params), _ptr(dev["mz"]), _ptr(dev["it"]), _ptr(dev["off"]), _ptr(dev["pcr"]),
             _ptr(dev["z"]), _ptr(dev["tol"]), int(dev["pcr"].numel()), _ptr(out["score"]), _ptr(out["key"]),
             _ptr(out["pep"]), _ptr(out.get("ncand"))))
+
+    def search_evalues(self, dev, params: SearchParams, out, bin_width: int = 350, cutoff_perc: float = 3.0):
+        """hfx_search_evalues: the device-buffer search plus E-values; out
+        also holds "ev" [nspec, top_n] and "fit" [nspec, 3] float64 tensors."""
+        self._check(self.lib.hfx_search_evalues(
+            self.h, C.byref(params), _ptr(dev["mz"]), _ptr(dev["it"]), _ptr(dev["off"]), _ptr(dev["pcr"]),
+            _ptr(dev["z"]), _ptr(dev["tol"]), int(dev["pcr"].numel()), int(bin_width), float(cutoff_perc),
+            _ptr(out["score"]), _ptr(out["key"]), _ptr(out["pep"]), _ptr(out.get("ncand")), _ptr(out["ev"]),
+            _ptr(out["fit"])))
 
     def match(self, key: int, pep: int):
         """hfx_match_peptide: (peptide text "X.PEPTIDE.Y" with '*' after

@@ -11,6 +11,7 @@
 #include "batched.h"
 #include "lists.h"
 #include "mods.h"
+#include "evalues.h"
 #include "../../include/hfx_gpu.h"
 
 #include <algorithm>
@@ -1101,6 +1102,95 @@ int32_t hfx_search_device(hfx_ctx *ctx, const hfx_search_params *p, const float 
     if (!ctx) return HFX_ERR_ARG;
     Batch b{mz, it, pcr, z, tol, off, nspec};
     return search_device(ctx, p, b, out_s, out_k, out_pep, out_ncand);
+}
+
+int32_t hfx_search_evalues(hfx_ctx *ctx, const hfx_search_params *p, const float *mz, const float *it,
+                           const int64_t *off, const float *pcr, const float *z, const float *tol, int32_t nspec,
+                           int32_t bin_width, float cutoff_perc, float *out_s, uint64_t *out_k, uint32_t *out_pep,
+                           int64_t *out_ncand, double *out_ev, double *out_fit) {
+    if (!ctx || !p || nspec < 0 || !out_s || !out_k || !out_ev || !out_fit)
+        return fail(ctx, HFX_ERR_ARG, "bad hfx_search_evalues arguments");
+    if (bin_width < 1 || !(cutoff_perc >= 0.0f && cutoff_perc <= 100.0f))
+        return fail(ctx, HFX_ERR_ARG, "E-value bin width must be >= 1 and the cut-off 0..100 %");
+    if (p->search_mods && ctx->num_mod > 0)
+        return fail(ctx, HFX_ERR_UNSUPPORTED, "E-values cover unmodified candidates only");
+    if (nspec == 0) return HFX_OK;
+    // the search over the step's ion lists, eagerly
+    hfx_search_params q = *p;
+    q.batch_mode = 1;
+    q.use_graph = 0;
+    Batch b{mz, it, pcr, z, tol, off, nspec};
+    int32_t rc = search_device(ctx, &q, b, out_s, out_k, out_pep, out_ncand);
+    if (rc) return rc;
+    // every candidate's FP32 score, from the step's lists and the FP32 rows
+    cudaError_t e;
+    const int32_t ns = nspec;
+    const int64_t stride = ctx->last_stride;
+    const bool long_rows = stride > (int64_t)kMaxWords * 32;
+    const int32_t G = 4, K = p->top_n;
+    const int32_t chunk = p->chunk > 0 ? p->chunk : 4096;
+    SpecMeta *meta = ctx->buf<SpecMeta>("meta", ns, e);
+    float *rows = ctx->buf<float>("rows32", (size_t)ns * stride, e);
+    uint32_t *wb = ctx->buf<uint32_t>("wb", ns, e);
+    uint32_t *we = ctx->buf<uint32_t>("we", ns, e);
+    uint64_t *size = ctx->buf<uint64_t>("e_size", ns, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    uint64_t *soff = ctx->buf<uint64_t>("e_off", ns, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    uint64_t *send = ctx->buf<uint64_t>("e_end", ns, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    HFX_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, 4, ctx->stream), "memset err");
+    rc = hfx_evalue_offsets(wb, we, ns, size, soff, send, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "E-value offsets");
+    uint64_t total = 0;
+    HFX_CUDA(cudaMemcpyAsync(&total, send + ns - 1, 8, cudaMemcpyDeviceToHost, ctx->stream), "D2H total");
+    HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    float *sink = ctx->buf<float>("e_sink", total + 1, e);
+    if (e) return cuda_fail(ctx, e, "alloc E-value scores");
+    float *sorted = ctx->buf<float>("e_sorted", total + 1, e);
+    if (e) return cuda_fail(ctx, e, "alloc E-value scores");
+    // re-plan with FP32 groups of 4 over the search's workspace
+    BatchedWs ws;
+    ws.hist = ctx->buf<uint32_t>("b_hist", kBucketCount + 1, e);
+    ws.cursor = ctx->buf<uint32_t>("b_cursor", kBucketCount, e);
+    uint32_t *scal = ctx->buf<uint32_t>("b_scal", 8, e);
+    ws.n_sorted = scal;
+    ws.ngroups = scal + 1;
+    ws.total_items = scal + 2;
+    ws.counter = scal + 3;
+    ws.perm = ctx->buf<int32_t>("b_perm", ns, e);
+    ws.groups = ctx->buf<GroupInfo>("b_groups", ns, e);
+    ws.item_off = ctx->buf<uint32_t>("b_itemoff", ns + 1, e);
+    ws.group_of = ctx->buf<int32_t>("b_groupof", ns, e);
+    ws.slot_of = ctx->buf<int32_t>("b_slotof", ns, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    rc = hfx_batched_plan(meta, ns, wb, we, G, chunk, ws, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "plan");
+    uint32_t hs[4];
+    HFX_CUDA(cudaMemcpyAsync(hs, scal, 16, cudaMemcpyDeviceToHost, ctx->stream), "D2H plan");
+    HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    const uint32_t ngroups = hs[1], items = hs[2];
+    void *tiles = ctx->buf<uint8_t>("e_tiles", (size_t)ngroups * stride * G * 4 + 64, e);
+    if (e) return cuda_fail(ctx, e, "alloc tiles");
+    float *ps = ctx->buf<float>("e_ps", (size_t)items * G * K + 1, e);
+    uint64_t *pk = ctx->buf<uint64_t>("e_pk", (size_t)items * G * K + 1, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    rc = hfx_pack_tiles(rows, 0, stride, meta, ws, tiles, ngroups, G, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_pack_tiles");
+    const uint64_t total10 = ctx->list_units;
+    const void *lists = long_rows ? (const void *)ctx->buf<uint32_t>("l_lists32", total10 * 10 + 64, e)
+                                  : (const void *)ctx->buf<uint16_t>("l_lists", total10 * 10 + 64, e);
+    const uint16_t *llen = ctx->buf<uint16_t>("l_len", (size_t)kLevels * ctx->num_pep, e);
+    if (e) return cuda_fail(ctx, e, "lists");
+    rc = hfx_lists_score(lists, long_rows, ctx->d_lstart.as<uint32_t>(), total10, llen, (uint32_t)ctx->num_pep, 0,
+                         stride, wb, we, ws, tiles, G, K, 0, ps, pk, nullptr, ctx->d_err.as<uint32_t>(), ctx->stream,
+                         sink, soff);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_lists (all pairs)");
+    rc = hfx_evalue_sort(sink, sorted, total, soff, send, ns, ctx->stream);
+    if (!rc) rc = hfx_evalue_fit(sorted, soff, size, ns, bin_width, cutoff_perc, out_fit, ctx->stream);
+    if (!rc) rc = hfx_evalue_apply(out_s, out_k, out_fit, ns, p->top_n, out_ev, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "E-values");
+    return search_finish(ctx);
 }
 
 int32_t hfx_set_protein_segments(hfx_ctx *ctx, const uint32_t *seg, int32_t nprot) {

@@ -472,7 +472,8 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
               const GroupInfo *__restrict__ groups, const uint32_t *__restrict__ item_off,
               const uint32_t *__restrict__ ngroups_p, int32_t K, uint32_t *__restrict__ counter,
               float *__restrict__ part_s, uint64_t *__restrict__ part_k, unsigned long long *__restrict__ stats,
-              uint32_t qoff, uint32_t *__restrict__ err) {
+              float *__restrict__ sink, const uint64_t *__restrict__ sink_off, uint32_t qoff,
+              uint32_t *__restrict__ err) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
@@ -481,6 +482,7 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
     __shared__ int32_t s_item;
     __shared__ uint32_t s_next;
     __shared__ uint32_t s_wb[G], s_we[G];
+    __shared__ uint64_t s_off[G];  // with a sink: where each member's window starts in it
     __shared__ uint32_t thr_u[G], s_lock[G];
     __shared__ float s_ls[G * 32];
     __shared__ uint32_t s_lk[G * 32];
@@ -509,11 +511,14 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
         if (threadIdx.x < G) {
             const int j = threadIdx.x;
             uint32_t b = 0, e = 0;
+            uint64_t o = 0;
             if (j < cnt_members) {
                 const int32_t s = perm[gi.pos0 + j];
                 b = wb[s];
                 e = we[s];
+                if (sink) o = sink_off[s];
             }
+            s_off[j] = o;
             s_wb[j] = b;
             s_we[j] = e;
         }
@@ -635,6 +640,12 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
                 }
             }
             const float sc = reduce_scatter<G>(acc);
+            if (sink) {
+                // every pair's score, at its member's window offset
+                if ((lane & (32 / G - 1)) == 0 && ((cur.act >> my_slot) & 1u))
+                    sink[s_off[my_slot] + (cur.p - s_wb[my_slot])] = sc;
+                continue;
+            }
             const bool want = (lane & (32 / G - 1)) == 0 && ((cur.act >> my_slot) & 1u) &&
                               score_order(sc) >= *(volatile uint32_t *)(thr_u + my_slot);
             slots.offer(want, sc, cur.p, my_slot, K);
@@ -720,8 +731,8 @@ template <typename T, int G, typename E, bool kGlobal>
 static int launch_lists_t(const E *lists, const uint32_t *lstart, uint64_t total10, const uint16_t *list_len,
                           uint32_t num_pep, int64_t stride, const uint32_t *wb, const uint32_t *we,
                           const BatchedWs &ws, void *tiles, int32_t K, int nw,
-                          float *part_s, uint64_t *part_k, unsigned long long *stats, uint32_t *err,
-                          cudaStream_t st) {
+                          float *part_s, uint64_t *part_k, unsigned long long *stats, float *sink,
+                          const uint64_t *sink_off, uint32_t *err, cudaStream_t st) {
     int dev = 0, sms = 0, smem_max = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -739,7 +750,7 @@ static int launch_lists_t(const E *lists, const uint32_t *lstart, uint64_t total
     cudaMemsetAsync(ws.counter, 0, 4, st);
     fn<<<grid, nw * 32, smem, st>>>(lists, lstart, total10, total10 * 10, list_len, num_pep, (const T *)tiles,
                                     stride, wb, we, ws.perm, ws.groups, ws.item_off, ws.ngroups, K,
-                                    ws.counter, part_s, part_k, stats, (uint32_t)qoff, err);
+                                    ws.counter, part_s, part_k, stats, sink, sink_off, (uint32_t)qoff, err);
     return (int)cudaGetLastError();
 }
 
@@ -761,16 +772,17 @@ int hfx_lists_group_fits(int32_t G, int long_rows, int64_t stride, int elem_byte
 int hfx_lists_score(const void *lists, int long_rows, const uint32_t *lstart, uint64_t total10,
                     const uint16_t *list_len, uint32_t num_pep, int elem_kind, int64_t stride, const uint32_t *wb,
                     const uint32_t *we, const BatchedWs &ws, void *tiles, int32_t G, int32_t K, int nw,
-                    float *part_s, uint64_t *part_k, unsigned long long *stats, uint32_t *err, cudaStream_t st) {
+                    float *part_s, uint64_t *part_k, unsigned long long *stats, uint32_t *err, cudaStream_t st,
+                    float *sink, const uint64_t *sink_off) {
 #define HFX_L(T, GG)                                                                                           \
     do {                                                                                                       \
         if (long_rows)                                                                                         \
             return launch_lists_t<T, GG, uint32_t, true>((const uint32_t *)lists, lstart, total10, list_len,   \
                                                          num_pep, stride, wb, we, ws, tiles, K, nw, part_s,    \
-                                                         part_k, stats, err, st);                              \
+                                                         part_k, stats, sink, sink_off, err, st);              \
         return launch_lists_t<T, GG, uint16_t, false>((const uint16_t *)lists, lstart, total10, list_len,      \
                                                       num_pep, stride, wb, we, ws, tiles, K, nw, part_s,       \
-                                                      part_k, stats, err, st);                                 \
+                                                      part_k, stats, sink, sink_off, err, st);                 \
     } while (0)
     if (elem_kind == 0) {
         if (G == 4) HFX_L(float, 4);

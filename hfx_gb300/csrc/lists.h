@@ -23,10 +23,13 @@ int hfx_lists_generate(const hfx::DevDB &db, const int32_t *cover, int64_t npep1
 // Scorer over the lists; long_rows: 32-bit entries and group tiles read
 // from global memory (rows too long for shared memory), else 16-bit entries
 // and tiles staged in shared memory.
+// With a sink, every pair's score is written to sink[sink_off[s] + p - wb[s]]
+// instead of the top-K.
 int hfx_lists_score(const void *lists, int long_rows, const uint32_t *lstart, uint64_t total10,
                     const uint16_t *list_len, uint32_t num_pep, int elem_kind, int64_t stride, const uint32_t *wb,
                     const uint32_t *we, const hfx::BatchedWs &ws, void *tiles, int32_t G, int32_t K, int nw,
-                    float *part_s, uint64_t *part_k, unsigned long long *stats, uint32_t *err, cudaStream_t st);
+                    float *part_s, uint64_t *part_k, unsigned long long *stats, uint32_t *err, cudaStream_t st,
+                    float *sink = nullptr, const uint64_t *sink_off = nullptr);
 // Whether a G-spectrum group tile of rows `stride` bins long (and the
 // scorer's queues) fits in shared memory; always 1 for G <= 8.
 int hfx_lists_group_fits(int32_t G, int long_rows, int64_t stride, int elem_bytes);

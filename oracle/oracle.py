@@ -216,3 +216,61 @@ def search(ions_packed, mt, r, tc, tn, idx, spectra, bw=1.0005079, custom_bw=Fal
     if rc != 0:
         raise RuntimeError(f"oracle search status {rc}")
     return sc, s64, key, pep, nc
+
+
+def evalue_fit(scores, bin_width=350, cutoff_perc=3.0):
+    """Util/Statistics.hs:37-100 for one spectrum's candidate scores (FP32
+    raw XCorrs): (alpha, beta, histogram points) of the least-squares line
+    log10(count / w) = alpha + beta * (bin centre / 10000) over the ranks
+    round(0.3 n) .. round((1 - p/100) n) of the ascending scores shifted by
+    1 - min and kept above 4000.  round halves to even; the cut-off product is
+    single precision (evalueCutOffPerc is a Float), the 30 % one double.
+    linearRegression (statistics-linreg, not in the reference tree) is
+    restated as OLS with sequential sums."""
+    import math
+    sc = np.sort(np.asarray(scores, np.float32)).astype(np.float64)
+    n = len(sc)
+    if n == 0:
+        return float("nan"), float("nan"), 0
+    keep = np.float32(np.float32(1.0) - np.float32(np.float32(cutoff_perc) / np.float32(100.0)))
+    cut_end = int(np.rint(np.float32(keep * np.float32(n))))
+    cut_beg = int(np.rint(0.3 * n))
+    hi = min(max(cut_end, 0), n)
+    lo = min(max(cut_beg, 0), hi)
+    head = float(sc[0])
+    w = float(bin_width)
+    pts = []
+    cur, cnt = None, 0
+    for v in sc[lo:hi]:
+        t = (float(v) + 1.0) + (-head)
+        if not t > 4000.0:
+            continue
+        b = math.ceil(t / w)
+        if b != cur:
+            if cnt:
+                pts.append(((cur * w - w / 2.0) / 10000.0, math.log(cnt / w) / math.log(10.0)))
+            cur, cnt = b, 0
+        cnt += 1
+    if cnt:
+        pts.append(((cur * w - w / 2.0) / 10000.0, math.log(cnt / w) / math.log(10.0)))
+    m = float(len(pts))
+    if not pts:
+        return float("nan"), float("nan"), 0
+    sx = sy = 0.0
+    for x, y in pts:
+        sx += x
+        sy += y
+    mx, my = sx / m, sy / m
+    sxy = sxx = 0.0
+    for x, y in pts:
+        sxy += (x - mx) * (y - my)
+        sxx += (x - mx) * (x - mx)
+    beta = sxy / sxx if sxx != 0.0 else float("nan")
+    return my - beta * mx, beta, len(pts)
+
+
+def evalue(alpha, beta, score):
+    """E-value of a raw score (Statistics.hs:40): 10 ** (alpha + beta * s / 10000)."""
+    import math
+    return math.pow(10.0, alpha + beta * (float(score) / 10000.0))
+
