@@ -1,6 +1,7 @@
 // E-values of the matches (Util/Statistics.hs:37-100, called per spectrum at
 // Search.hs:119-123), computed on the device from every candidate's FP32
-// score instead of copying all scores to the host.
+// score -- the unmodified candidates and, in a modification search, every
+// modified isoform -- instead of copying all scores to the host.
 //
 // Per spectrum, over its n candidate scores sorted ascending:
 //   cut_end = round((1 - p/100) * n)   in single precision (p = evalueCutOffPerc, a Float)
@@ -22,16 +23,24 @@
 
 namespace hfx {
 
-__global__ void k_window_sizes64(const uint32_t *__restrict__ wb, const uint32_t *__restrict__ we, int32_t ns,
-                                 uint64_t *__restrict__ size) {
-    const int32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < ns) size[s] = we[s] > wb[s] ? (uint64_t)(we[s] - wb[s]) : 0ull;
+__device__ __forceinline__ uint64_t plain_count(const uint32_t *wb, const uint32_t *we, int plain, int32_t s) {
+    return plain && we[s] > wb[s] ? (uint64_t)(we[s] - wb[s]) : 0ull;
 }
 
-__global__ void k_segment_ends(const uint64_t *__restrict__ off, const uint64_t *__restrict__ size, int32_t ns,
-                               uint64_t *__restrict__ end) {
+__global__ void k_window_sizes64(const uint32_t *__restrict__ wb, const uint32_t *__restrict__ we, int plain,
+                                 const unsigned long long *__restrict__ isoforms, int32_t ns,
+                                 uint64_t *__restrict__ size) {
     const int32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < ns) end[s] = off[s] + size[s];
+    if (s < ns) size[s] = plain_count(wb, we, plain, s) + (isoforms ? (uint64_t)isoforms[s] : 0ull);
+}
+
+__global__ void k_segment_ends(const uint32_t *__restrict__ wb, const uint32_t *__restrict__ we, int plain,
+                               const uint64_t *__restrict__ off, const uint64_t *__restrict__ size, int32_t ns,
+                               uint64_t *__restrict__ end, unsigned long long *__restrict__ cursor) {
+    const int32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= ns) return;
+    end[s] = off[s] + size[s];
+    if (cursor) cursor[s] = off[s] + plain_count(wb, we, plain, s);
 }
 
 // The histogram points of one spectrum's slice, in ascending bin order;
@@ -113,17 +122,18 @@ __global__ void k_evalue_apply(const float *__restrict__ out_s, const uint64_t *
 
 using namespace hfx;
 
-int hfx_evalue_offsets(const uint32_t *wb, const uint32_t *we, int32_t ns, uint64_t *size, uint64_t *off,
-                       uint64_t *end, cudaStream_t st) {
+int hfx_evalue_offsets(const uint32_t *wb, const uint32_t *we, int plain, const unsigned long long *isoforms,
+                       int32_t ns, uint64_t *size, uint64_t *off, uint64_t *end, unsigned long long *cursor,
+                       cudaStream_t st) {
     if (ns <= 0) return 0;
-    k_window_sizes64<<<(ns + 255) / 256, 256, 0, st>>>(wb, we, ns, size);
+    k_window_sizes64<<<(ns + 255) / 256, 256, 0, st>>>(wb, we, plain, isoforms, ns, size);
     size_t bytes = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, bytes, size, off, ns, st);
     void *tmp = nullptr;
     if (cudaMallocAsync(&tmp, bytes, st) != cudaSuccess) return (int)cudaErrorMemoryAllocation;
     cub::DeviceScan::ExclusiveSum(tmp, bytes, size, off, ns, st);
     cudaFreeAsync(tmp, st);
-    k_segment_ends<<<(ns + 255) / 256, 256, 0, st>>>(off, size, ns, end);
+    k_segment_ends<<<(ns + 255) / 256, 256, 0, st>>>(wb, we, plain, off, size, ns, end, cursor);
     return (int)cudaGetLastError();
 }
 

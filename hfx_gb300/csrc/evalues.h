@@ -3,10 +3,13 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
-// Per spectrum the number of candidates (we - wb), their exclusive scan and
-// the segment ends.
-int hfx_evalue_offsets(const uint32_t *wb, const uint32_t *we, int32_t ns, uint64_t *size, uint64_t *off,
-                       uint64_t *end, cudaStream_t st);
+// Per spectrum the number of candidates -- unmodified (we - wb, when plain)
+// plus modified isoforms (isoforms[s], may be null) -- their exclusive scan,
+// the segment ends and the first entry after the unmodified ones (cursor,
+// may be null).
+int hfx_evalue_offsets(const uint32_t *wb, const uint32_t *we, int plain, const unsigned long long *isoforms,
+                       int32_t ns, uint64_t *size, uint64_t *off, uint64_t *end, unsigned long long *cursor,
+                       cudaStream_t st);
 // Every spectrum's scores sorted ascending (segmented).
 int hfx_evalue_sort(const float *scores, float *sorted, uint64_t total, const uint64_t *off, const uint64_t *end,
                     int32_t ns, cudaStream_t st);

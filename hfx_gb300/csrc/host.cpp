@@ -1112,9 +1112,9 @@ int32_t hfx_search_evalues(hfx_ctx *ctx, const hfx_search_params *p, const float
         return fail(ctx, HFX_ERR_ARG, "bad hfx_search_evalues arguments");
     if (bin_width < 1 || !(cutoff_perc >= 0.0f && cutoff_perc <= 100.0f))
         return fail(ctx, HFX_ERR_ARG, "E-value bin width must be >= 1 and the cut-off 0..100 %");
-    if (p->search_mods && ctx->num_mod > 0)
-        return fail(ctx, HFX_ERR_UNSUPPORTED, "E-values cover unmodified candidates only");
     if (nspec == 0) return HFX_OK;
+    const bool mods_on = p->search_mods != 0 && ctx->num_mod > 0;
+    const bool plain_on = p->search_plain != 0;
     // the search over the step's ion lists, eagerly
     hfx_search_params q = *p;
     q.batch_mode = 1;
@@ -1122,7 +1122,9 @@ int32_t hfx_search_evalues(hfx_ctx *ctx, const hfx_search_params *p, const float
     Batch b{mz, it, pcr, z, tol, off, nspec};
     int32_t rc = search_device(ctx, &q, b, out_s, out_k, out_pep, out_ncand);
     if (rc) return rc;
-    // every candidate's FP32 score, from the step's lists and the FP32 rows
+    // every candidate's FP32 score (Search.hs:116-121: the unmodified
+    // candidates and every modified isoform), from the step's lists, the
+    // modification scorer and the FP32 rows
     cudaError_t e;
     const int32_t ns = nspec;
     const int64_t stride = ctx->last_stride;
@@ -1139,8 +1141,13 @@ int32_t hfx_search_evalues(hfx_ctx *ctx, const hfx_search_params *p, const float
     if (e) return cuda_fail(ctx, e, "alloc");
     uint64_t *send = ctx->buf<uint64_t>("e_end", ns, e);
     if (e) return cuda_fail(ctx, e, "alloc");
+    unsigned long long *cursor = ctx->buf<unsigned long long>("e_cursor", ns, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    // isoforms per spectrum, counted by the search's modification scorer
+    unsigned long long *niso = mods_on ? ctx->buf<unsigned long long>("m_ncand", ns, e) : nullptr;
+    if (e) return cuda_fail(ctx, e, "alloc");
     HFX_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, 4, ctx->stream), "memset err");
-    rc = hfx_evalue_offsets(wb, we, ns, size, soff, send, ctx->stream);
+    rc = hfx_evalue_offsets(wb, we, plain_on ? 1 : 0, niso, ns, size, soff, send, cursor, ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "E-value offsets");
     uint64_t total = 0;
     HFX_CUDA(cudaMemcpyAsync(&total, send + ns - 1, 8, cudaMemcpyDeviceToHost, ctx->stream), "D2H total");
@@ -1177,15 +1184,54 @@ int32_t hfx_search_evalues(hfx_ctx *ctx, const hfx_search_params *p, const float
     if (e) return cuda_fail(ctx, e, "alloc");
     rc = hfx_pack_tiles(rows, 0, stride, meta, ws, tiles, ngroups, G, ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_pack_tiles");
-    const uint64_t total10 = ctx->list_units;
-    const void *lists = long_rows ? (const void *)ctx->buf<uint32_t>("l_lists32", total10 * 10 + 64, e)
-                                  : (const void *)ctx->buf<uint16_t>("l_lists", total10 * 10 + 64, e);
-    const uint16_t *llen = ctx->buf<uint16_t>("l_len", (size_t)kLevels * ctx->num_pep, e);
-    if (e) return cuda_fail(ctx, e, "lists");
-    rc = hfx_lists_score(lists, long_rows, ctx->d_lstart.as<uint32_t>(), total10, llen, (uint32_t)ctx->num_pep, 0,
-                         stride, wb, we, ws, tiles, G, K, 0, ps, pk, nullptr, ctx->d_err.as<uint32_t>(), ctx->stream,
-                         sink, soff);
-    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_lists (all pairs)");
+    if (plain_on) {
+        const uint64_t total10 = ctx->list_units;
+        const void *lists = long_rows ? (const void *)ctx->buf<uint32_t>("l_lists32", total10 * 10 + 64, e)
+                                      : (const void *)ctx->buf<uint16_t>("l_lists", total10 * 10 + 64, e);
+        const uint16_t *llen = ctx->buf<uint16_t>("l_len", (size_t)kLevels * ctx->num_pep, e);
+        if (e) return cuda_fail(ctx, e, "lists");
+        rc = hfx_lists_score(lists, long_rows, ctx->d_lstart.as<uint32_t>(), total10, llen, (uint32_t)ctx->num_pep,
+                             0, stride, wb, we, ws, tiles, G, K, 0, ps, pk, nullptr, ctx->d_err.as<uint32_t>(),
+                             ctx->stream, sink, soff);
+        if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_lists (all pairs)");
+    }
+    if (mods_on) {
+        // the isoforms again, FP32 groups of 4, each score appended to its
+        // spectrum's segment after the unmodified ones
+        const int32_t nm = ctx->num_mod;
+        const int32_t n_gm = (int32_t)ngroups * nm;
+        const uint32_t *mb = ctx->buf<uint32_t>("m_wb", (size_t)ns * nm, e);
+        const uint32_t *me = ctx->buf<uint32_t>("m_we", (size_t)ns * nm, e);
+        uint32_t *mlo = ctx->buf<uint32_t>("m_lo", (size_t)n_gm + 1, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        uint32_t *mhi = ctx->buf<uint32_t>("m_hi", (size_t)n_gm + 1, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        uint32_t *mch = ctx->buf<uint32_t>("m_chunk", (size_t)n_gm + 1, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        int32_t *nch = ctx->buf<int32_t>("m_nchunks", (size_t)n_gm + 1, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        uint32_t *mitem_off = ctx->buf<uint32_t>("m_itemoff", (size_t)n_gm + 2, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        int32_t *partial = ctx->buf<int32_t>("m_partial", hfx_scan_partials_needed(n_gm + 1) + 1, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        rc = hfx_mods_plan(ws, ngroups, mb, me, nm, chunk, mlo, mhi, mch, nch, mitem_off, partial, ctx->stream);
+        if (rc) return cuda_fail(ctx, (cudaError_t)rc, "modification plan (all pairs)");
+        uint32_t mtotal = 0;
+        if (n_gm > 0) {
+            HFX_CUDA(cudaMemcpyAsync(&mtotal, mitem_off + n_gm, 4, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+            HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+        }
+        float *mps = ctx->buf<float>("e_mps", (size_t)mtotal * G * K + 1, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        uint64_t *mpk = ctx->buf<uint64_t>("e_mpk", (size_t)mtotal * G * K + 1, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        if (mtotal > 0) {
+            rc = hfx_mods_score(ctx->devdb(), ctx->devmods(), tiles, 0, stride, mb, me, ws, mlo, mhi, mch, mitem_off,
+                                n_gm, G, K, p->fastdiv, mps, mpk, nullptr, ctx->d_err.as<uint32_t>(), ctx->stream,
+                                sink, cursor, send);
+            if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_mods (all pairs)");
+        }
+    }
     rc = hfx_evalue_sort(sink, sorted, total, soff, send, ns, ctx->stream);
     if (!rc) rc = hfx_evalue_fit(sorted, soff, size, ns, bin_width, cutoff_perc, out_fit, ctx->stream);
     if (!rc) rc = hfx_evalue_apply(out_s, out_k, out_fit, ns, p->top_n, out_ev, ctx->stream);

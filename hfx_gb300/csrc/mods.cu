@@ -91,7 +91,8 @@ k_score_mods(DevDB db, DevMods mods, const T *__restrict__ tiles, int64_t stride
              const GroupInfo *__restrict__ groups, const uint32_t *__restrict__ mlo, const uint32_t *__restrict__ mhi,
              const uint32_t *__restrict__ mchunk, const uint32_t *__restrict__ item_off, int32_t n_gm, int32_t K,
              uint32_t *__restrict__ counter, float *__restrict__ part_s, uint64_t *__restrict__ part_k,
-             unsigned long long *__restrict__ ncand, uint32_t *__restrict__ err) {
+             unsigned long long *__restrict__ ncand, float *__restrict__ sink, unsigned long long *__restrict__ cursor,
+             const uint64_t *__restrict__ sink_end, uint32_t *__restrict__ err) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int32_t words_cap = (int32_t)((stride + 31) / 32);
@@ -190,6 +191,18 @@ k_score_mods(DevDB db, DevMods mods, const T *__restrict__ tiles, int64_t stride
             // candidates counted per member spectrum: one per isoform
             if (ncand && lane < G && ((act >> lane) & 1u) && niso)
                 atomicAdd(ncand + s_spec[lane], (unsigned long long)niso);
+            // score sink (E-values): niso consecutive entries of the member's
+            // segment, claimed at once; the fit reads them as a multiset
+            unsigned long long sbase = ~0ull;
+            if (sink) {
+                if (lane < G && ((act >> lane) & 1u) && niso) {
+                    const int32_t s = s_spec[lane];
+                    const unsigned long long b0 = atomicAdd(cursor + s, (unsigned long long)niso);
+                    if (b0 + niso <= sink_end[s]) sbase = b0;
+                    else atomicOr(err, kErrBounds);
+                }
+                sbase = __shfl_sync(kFullMask, sbase, my_slot);
+            }
             // mion_series.cu:226: residual + delta
             const float residual = __fadd_rn(db.r_sorted[p], delta);
             for (uint32_t rank = 0; rank < niso; ++rank) {
@@ -206,6 +219,7 @@ k_score_mods(DevDB db, DevMods mods, const T *__restrict__ tiles, int64_t stride
                 float acc[G];
                 planes_accumulate<G>(pl, list, wr, dot, acc);
                 const float sc = reduce_scatter<G>(acc);
+                if (sbase != ~0ull && (lane & (32 / G - 1)) == 0 && ((act >> my_slot) & 1u)) sink[sbase + rank] = sc;
                 const bool want = (lane & (32 / G - 1)) == 0 && ((act >> my_slot) & 1u) &&
                                   score_order(sc) >= *(volatile uint32_t *)(thr_u + my_slot);
                 slots.offer(want, sc, mod_key(mu, p, rank), my_slot, K);
@@ -361,8 +375,8 @@ template <bool F, typename T, int G>
 static int launch_mods_t(const DevDB &db, const DevMods &m, const void *tiles, int64_t stride, const uint32_t *mb,
                          const uint32_t *me, const BatchedWs &ws, const uint32_t *mlo, const uint32_t *mhi,
                          const uint32_t *mchunk, const uint32_t *item_off, int32_t n_gm, int32_t K, float *ps,
-                         uint64_t *pk,
-                         unsigned long long *ncand, uint32_t *err, cudaStream_t st) {
+                         uint64_t *pk, unsigned long long *ncand, float *sink, unsigned long long *cursor,
+                         const uint64_t *sink_end, uint32_t *err, cudaStream_t st) {
     int dev = 0, sms = 0, smem_max = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -382,7 +396,7 @@ static int launch_mods_t(const DevDB &db, const DevMods &m, const void *tiles, i
     cudaMemsetAsync(ws.counter, 0, 4, st);
     fn<<<sms * (occ > 0 ? occ : 1), nw * 32, smem, st>>>(db, m, (const T *)tiles, stride, mb, me, ws.perm, ws.groups,
                                                          mlo, mhi, mchunk, item_off, n_gm, K, ws.counter, ps, pk,
-                                                         ncand, err);
+                                                         ncand, sink, cursor, sink_end, err);
     return (int)cudaGetLastError();
 }
 
@@ -390,11 +404,12 @@ int hfx_mods_score(const DevDB &db, const DevMods &m, const void *tiles, int ele
                    const uint32_t *mb, const uint32_t *me, const BatchedWs &ws, const uint32_t *mlo,
                    const uint32_t *mhi, const uint32_t *mchunk, const uint32_t *item_off, int32_t n_gm, int32_t G,
                    int32_t K, int fastdiv, float *ps, uint64_t *pk, unsigned long long *ncand, uint32_t *err,
-                   cudaStream_t st) {
+                   cudaStream_t st, float *sink, unsigned long long *cursor, const uint64_t *sink_end) {
     if (n_gm <= 0) return 0;
+    if (sink && (!cursor || !sink_end)) return (int)cudaErrorInvalidValue;
 #define HFX_M(F, T, GG)                                                                                            \
     return launch_mods_t<F, T, GG>(db, m, tiles, stride, mb, me, ws, mlo, mhi, mchunk, item_off, n_gm, K, ps, pk, \
-                                   ncand, err, st)
+                                   ncand, sink, cursor, sink_end, err, st)
 #define HFX_MG(F, T)              \
     do {                          \
         if (G == 8) HFX_M(F, T, 8); \

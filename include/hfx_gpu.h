@@ -150,16 +150,16 @@ int32_t hfx_search_device(hfx_ctx *ctx, const hfx_search_params *p, const float 
                           int32_t nspec, float *out_score, uint64_t *out_key, uint32_t *out_pep,
                           int64_t *out_ncand);
 /* The device-buffer search plus E-values (Util/Statistics.hs:37-100, applied
- * per spectrum at Search.hs:119-123): every candidate's FP32 score is
- * computed on the device, each spectrum's ascending scores are sliced at
+ * per spectrum at Search.hs:119-123): every candidate's FP32 score -- the
+ * unmodified candidates and, in a modification search, every modified
+ * isoform, as the reference fits over all matches of the spectrum
+ * (Search.hs:116-121) -- is computed on the device, each spectrum's ascending scores are sliced at
  * round(0.3 n) .. round((1 - cutoff_perc/100) n), shifted by 1 - min, kept
  * above 4000 and binned by bin_width; an ordinary least-squares line through
  * (bin centre / 10000, log10(count / bin_width)) gives alpha and beta, and a
  * result of score s gets 10 ** (alpha + beta * s / 10000).  out_ev [nspec]
  * [top_n] (NaN for empty slots), out_fit [nspec][3] = alpha, beta, histogram
- * points.  The reference's defaults are bin_width 350 and cutoff_perc 3.
- * Unmodified candidates only (modification search returns
- * HFX_ERR_UNSUPPORTED). */
+ * points.  The reference's defaults are bin_width 350 and cutoff_perc 3. */
 int32_t hfx_search_evalues(hfx_ctx *ctx, const hfx_search_params *p, const float *mz, const float *it,
                            const int64_t *off, const float *pcr, const float *z, const float *tol, int32_t nspec,
                            int32_t bin_width, float cutoff_perc, float *out_score, uint64_t *out_key,

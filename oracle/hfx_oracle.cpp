@@ -580,14 +580,14 @@ uint32_t hfxo_mod_isoform(const uint8_t *ions, uint32_t tc, uint32_t tn,
     return num;
 }
 
-int32_t hfxo_search(const uint8_t *ions, const float *mt, const float *r,
-                    const uint32_t *tc, const uint32_t *tn,
-                    const uint32_t *idx, int64_t num_pep, const float *mz,
-                    const float *it, const int64_t *off, const float *pcr,
-                    const float *z, const float *tol, int32_t nspec,
-                    const hfxo_params *p, int32_t nthreads, float *out_score,
-                    double *out_score64, uint64_t *out_key, uint32_t *out_pep,
-                    int64_t *out_ncand) {
+int32_t hfxo_search_scores(const uint8_t *ions, const float *mt, const float *r,
+                           const uint32_t *tc, const uint32_t *tn,
+                           const uint32_t *idx, int64_t num_pep, const float *mz,
+                           const float *it, const int64_t *off, const float *pcr,
+                           const float *z, const float *tol, int32_t nspec,
+                           const hfxo_params *p, int32_t nthreads, float *out_score,
+                           double *out_score64, uint64_t *out_key, uint32_t *out_pep,
+                           int64_t *out_ncand, const int64_t *sink_off, float *sink) {
     const int32_t topn = p->topn;
     std::vector<float> rs(num_pep);
     for (int64_t i = 0; i < num_pep; ++i) rs[i] = r[idx[i]];
@@ -653,6 +653,7 @@ int32_t hfxo_search(const uint8_t *ions, const float *mt, const float *r,
                     if (p->prec == 3) e.s = (float)e.s64;
                 };
                 auto push = [&](const Entry &e) {
+                    if (sink) sink[sink_off[s] + ncand] = e.s;
                     if ((int32_t)top.size() < topn) {
                         top.push_back(e);
                         std::push_heap(top.begin(), top.end(), better);
@@ -737,6 +738,19 @@ int32_t hfxo_search(const uint8_t *ions, const float *mt, const float *r,
         }
     }
     return status;
+}
+
+int32_t hfxo_search(const uint8_t *ions, const float *mt, const float *r,
+                    const uint32_t *tc, const uint32_t *tn,
+                    const uint32_t *idx, int64_t num_pep, const float *mz,
+                    const float *it, const int64_t *off, const float *pcr,
+                    const float *z, const float *tol, int32_t nspec,
+                    const hfxo_params *p, int32_t nthreads, float *out_score,
+                    double *out_score64, uint64_t *out_key, uint32_t *out_pep,
+                    int64_t *out_ncand) {
+    return hfxo_search_scores(ions, mt, r, tc, tn, idx, num_pep, mz, it, off, pcr, z, tol, nspec, p,
+                              nthreads, out_score, out_score64, out_key, out_pep, out_ncand, nullptr,
+                              nullptr);
 }
 
 } // extern "C"

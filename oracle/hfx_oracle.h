@@ -144,6 +144,21 @@ int32_t hfxo_search(const uint8_t *ions, const float *mt26, const float *r,
                     float *out_score, double *out_score64, uint64_t *out_key,
                     uint32_t *out_pep, int64_t *out_ncand);
 
+/* As hfxo_search, and also every candidate's score (plain candidates in
+ * mass order, then modified isoforms by combination, position and rank) at
+ * sink[sink_off[s] ...]: the score list the reference hands to its E-value
+ * fit (Search.hs:116-121, every match of the spectrum, modified or not).
+ * sink_off per spectrum: exclusive prefix sum of out_ncand. */
+int32_t hfxo_search_scores(const uint8_t *ions, const float *mt26, const float *r,
+                           const uint32_t *tc, const uint32_t *tn,
+                           const uint32_t *idx_sorted, int64_t num_pep,
+                           const float *mz, const float *it, const int64_t *off,
+                           const float *pcr, const float *z, const float *tol,
+                           int32_t nspec, const hfxo_params *p, int32_t nthreads,
+                           float *out_score, double *out_score64, uint64_t *out_key,
+                           uint32_t *out_pep, int64_t *out_ncand,
+                           const int64_t *sink_off, float *sink);
+
 #ifdef __cplusplus
 }
 #endif

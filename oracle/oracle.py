@@ -59,6 +59,8 @@ def lib():
             "hfxo_mod_isoform": (C.c_uint32, [P, C.c_uint32, C.c_uint32, P, i32, P, C.c_uint32, i32, P, P]),
             "hfxo_search": (i32, [P, P, P, P, P, P, i64, P, P, P, P, P, P, i32, C.POINTER(Params), i32,
                                   P, P, P, P, P]),
+            "hfxo_search_scores": (i32, [P, P, P, P, P, P, i64, P, P, P, P, P, P, i32, C.POINTER(Params), i32,
+                                         P, P, P, P, P, P, P]),
         }
         for k, (res, args) in sig.items():
             f = getattr(L, k)
@@ -193,10 +195,7 @@ def mod_isoform(ions_packed, tc, tn, ma, mod_counts, rank=None, per_type=False):
     return n, un[: int(mc.sum())].copy(), md[: tn - tc].copy()
 
 
-def search(ions_packed, mt, r, tc, tn, idx, spectra, bw=1.0005079, custom_bw=False, remove_pcr=True, ppm=False,
-           topn=10, prec=0, ma=b"", ma_mass=(), max_ma=0, per_type=False, plain=True, nthreads=0, ion_bw=0.0):
-    """Full search (Search.hs:98-124); returns (score, score64, key, pep, ncand)."""
-    mz, it, off, pcr, z, tol = spectra.arrays()
+def _params(bw, custom_bw, remove_pcr, ppm, topn, prec, ma, ma_mass, max_ma, per_type, plain, ion_bw):
     p = Params()
     p.bw, p.custom_bw, p.remove_pcr, p.ppm = bw, int(custom_bw), int(remove_pcr), int(ppm)
     p.topn, p.prec, p.num_ma, p.max_ma, p.per_type, p.plain = topn, prec, len(ma), max_ma, int(per_type), int(plain)
@@ -204,6 +203,17 @@ def search(ions_packed, mt, r, tc, tn, idx, spectra, bw=1.0005079, custom_bw=Fal
     for i, c in enumerate(ma):
         p.ma[i] = c
         p.ma_mass[i] = ma_mass[i]
+    return p
+
+
+def search(ions_packed, mt, r, tc, tn, idx, spectra, bw=1.0005079, custom_bw=False, remove_pcr=True, ppm=False,
+           topn=10, prec=0, ma=b"", ma_mass=(), max_ma=0, per_type=False, plain=True, nthreads=0, ion_bw=0.0,
+           all_scores=False):
+    """Full search (Search.hs:98-124); returns (score, score64, key, pep, ncand),
+    and with all_scores a sixth item: per spectrum every candidate's score
+    (plain, then modified isoforms), the list the E-value fit reads."""
+    mz, it, off, pcr, z, tol = spectra.arrays()
+    p = _params(bw, custom_bw, remove_pcr, ppm, topn, prec, ma, ma_mass, max_ma, per_type, plain, ion_bw)
     ns = len(pcr)
     sc = np.empty((ns, topn), np.float32)
     s64 = np.empty((ns, topn), np.float64)
@@ -215,7 +225,18 @@ def search(ions_packed, mt, r, tc, tn, idx, spectra, bw=1.0005079, custom_bw=Fal
                            nthreads, _p(sc), _p(s64), _p(key), _p(pep), _p(nc))
     if rc != 0:
         raise RuntimeError(f"oracle search status {rc}")
-    return sc, s64, key, pep, nc
+    if not all_scores:
+        return sc, s64, key, pep, nc
+    soff = np.zeros(ns + 1, np.int64)
+    np.cumsum(nc, out=soff[1:])
+    sink = np.empty(max(1, int(soff[-1])), np.float32)
+    rc = lib().hfxo_search_scores(_p(ions_packed), _p(np.ascontiguousarray(mt, np.float32)), _p(r), _p(tc),
+                                  _p(tn), _p(idx), len(r), _p(mz), _p(it), _p(off), _p(pcr), _p(z), _p(tol), ns,
+                                  C.byref(p), nthreads, _p(sc), _p(s64), _p(key), _p(pep), _p(nc), _p(soff),
+                                  _p(sink))
+    if rc != 0:
+        raise RuntimeError(f"oracle search status {rc}")
+    return sc, s64, key, pep, nc, [sink[soff[i]:soff[i + 1]].copy() for i in range(ns)]
 
 
 def evalue_fit(scores, bin_width=350, cutoff_perc=3.0):

@@ -113,21 +113,56 @@ def test_evalues_parameters(eng_tiny, oracle):
             assert math.isclose(fit[i, 1], b, rel_tol=1e-9, abs_tol=1e-9)
 
 
-def test_evalues_refuse_modification_search(gpulib, tiny):
+MA = b"MSTY"
+MA_MASS = [15.995, 79.966, 79.966, 79.966]   # Met oxidation, Ser/Thr/Tyr phosphorylation
+
+
+@pytest.mark.parametrize("precision,plain,per_type", [(0, 1, False), (1, 1, False), (0, 0, True)])
+def test_evalues_with_mods(gpulib, tiny, oracle, precision, plain, per_type):
+    """A modification search fits over every match of the spectrum, modified
+    isoforms included (Search.hs:116-121); the oracle hands back the same
+    score list (plain candidates, then every isoform)."""
     import hfx_gb300
     prot, sp, cfg = tiny
     eng = hfx_gb300.Engine(0)
     try:
         eng.build_db(prot.seq, prot.seg, static_add=synth.static_mods(), **synth.DIGEST)
-        eng.set_mods("MSTY", [15.995, 79.966, 79.966, 79.966], 4, False)
-        sub = sp.subset(np.arange(4))
+        eng.set_mods(MA.decode(), MA_MASS, 4, per_type)
+        sub = sp.subset(np.arange(16))
+        n = len(sub)
         d = torch.device("cuda:0")
-        out = dict(score=torch.empty((4, 10), dtype=torch.float32, device=d),
-                   key=torch.empty((4, 10), dtype=torch.int64, device=d),
-                   pep=torch.empty((4, 10), dtype=torch.int32, device=d),
-                   ev=torch.empty((4, 10), dtype=torch.float64, device=d),
-                   fit=torch.empty((4, 3), dtype=torch.float64, device=d))
-        with pytest.raises(hfx_gb300.HfxError):
-            eng.search_evalues(_dev(sub), hfx_gb300.default_params(top_n=10), out)
+        out = dict(score=torch.empty((n, 10), dtype=torch.float32, device=d),
+                   key=torch.empty((n, 10), dtype=torch.int64, device=d),
+                   pep=torch.empty((n, 10), dtype=torch.int32, device=d),
+                   ncand=torch.empty(n, dtype=torch.int64, device=d),
+                   ev=torch.empty((n, 10), dtype=torch.float64, device=d),
+                   fit=torch.empty((n, 3), dtype=torch.float64, device=d))
+        p = hfx_gb300.default_params(top_n=10, precision=precision, batch_mode=1, search_plain=plain,
+                                     rescore_k=32 if precision else 0)
+        eng.search_evalues(_dev(sub), p, out)
+        r, tc, tn, idx, mt = eng.db_export()
+        sc, _, key, pep, nc, all_sc = oracle.search(oracle.pack_ions(prot.seq, MA), mt, r, tc, tn, idx, sub,
+                                                    topn=10, ma=MA, ma_mass=MA_MASS, max_ma=4, per_type=per_type,
+                                                    plain=bool(plain), all_scores=True)
+        assert np.array_equal(out["ncand"].cpu().numpy(), nc)
+        assert np.array_equal(out["key"].cpu().numpy().view(np.uint64), key)
+        assert np.array_equal(out["score"].cpu().numpy().view(np.uint32), sc.view(np.uint32))
+        assert (key[key != np.iinfo(np.uint64).max] >> np.uint64(63)).any()
+        fit = out["fit"].cpu().numpy()
+        ev = out["ev"].cpu().numpy()
+        fitted = 0
+        for i in range(n):
+            assert len(all_sc[i]) == nc[i]
+            a, b, m = oracle.evalue_fit(all_sc[i])
+            assert int(fit[i, 2]) == m, i
+            if m < 2:
+                continue
+            fitted += 1
+            assert math.isclose(fit[i, 0], a, rel_tol=1e-9, abs_tol=1e-9), (i, fit[i], a, b)
+            assert math.isclose(fit[i, 1], b, rel_tol=1e-9, abs_tol=1e-9), (i, fit[i], a, b)
+            for j in range(10):
+                if key[i, j] != np.iinfo(np.uint64).max:
+                    assert math.isclose(ev[i, j], oracle.evalue(a, b, sc[i, j]), rel_tol=1e-8), (i, j)
+        assert fitted >= n // 2
     finally:
         eng.close()
