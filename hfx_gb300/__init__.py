@@ -29,7 +29,7 @@ BIN_WIDTH_AVG = 1.0011413
 EXPORTED = [
     "hfx_default_params", "hfx_ctx_create", "hfx_ctx_destroy", "hfx_set_stream",
     "hfx_last_error", "hfx_build_db", "hfx_upload_db", "hfx_db_info", "hfx_db_export", "hfx_autotune", "hfx_match_peptide",
-    "hfx_set_protein_segments",
+    "hfx_set_protein_segments", "hfx_match_ions",
     "hfx_set_mods", "hfx_mod_table", "hfx_search_host", "hfx_search_device", "hfx_search_evalues",
     "hfx_preprocess", "hfx_find_windows", "hfx_ion_bins", "hfx_mod_isoforms", "hfx_digest", "hfx_pack_ions",
     "hfx_set_profiling", "hfx_stage_stats", "hfx_search_counters",
@@ -94,6 +94,7 @@ def load_library(path: str = LIB_PATH):
         "hfx_search_device": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, P, i32, P, P, P, P]),
         "hfx_search_evalues": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, P, i32, i32, C.c_float, P, P, P, P,
                                      P, P]),
+        "hfx_match_ions": (i32, [P, C.POINTER(SearchParams), P, i32, P, i32, P, P]),
         "hfx_autotune": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, P, i32, P, P, P, P, i32,
                                C.POINTER(C.c_float)]),
         "hfx_match_peptide": (i32, [P, u64, C.c_uint32, C.c_char_p, i32, C.POINTER(C.c_float),
@@ -302,6 +303,19 @@ class Engine:
             _ptr(dev["z"]), _ptr(dev["tol"]), int(dev["pcr"].numel()), int(bin_width), float(cutoff_perc),
             _ptr(out["score"]), _ptr(out["key"]), _ptr(out["pep"]), _ptr(out.get("ncand")), _ptr(out["ev"]),
             _ptr(out["fit"])))
+
+    def match_ions(self, dev, params: SearchParams, out):
+        """hfx_match_ions: the "Ions" column (matched, total) of every result
+        of the last search on these spectra; out gains "ions_matched" and
+        "ions_total" [nspec, top_n] int32 tensors."""
+        import torch
+        n, k = out["key"].shape
+        if "ions_matched" not in out:
+            out["ions_matched"] = torch.empty((n, k), dtype=torch.int32, device=out["key"].device)
+            out["ions_total"] = torch.empty((n, k), dtype=torch.int32, device=out["key"].device)
+        self._check(self.lib.hfx_match_ions(self.h, C.byref(params), _ptr(dev["z"]), n, _ptr(out["key"]), k,
+                                            _ptr(out["ions_matched"]), _ptr(out["ions_total"])))
+        return out
 
     def match(self, key: int, pep: int):
         """hfx_match_peptide: (peptide text "X.PEPTIDE.Y" with '*' after

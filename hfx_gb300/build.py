@@ -24,7 +24,8 @@ NVCC_FLAGS = [
     "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fno-fast-math",
     "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include"), "-I", CSRC,
 ]
-SOURCES = ["host.cpp", "preprocess.cu", "search.cu", "batched.cu", "lists.cu", "mods.cu", "no_alloc.cu", "legacy.cu", "evalues.cu"]
+SOURCES = ["host.cpp", "preprocess.cu", "search.cu", "batched.cu", "lists.cu", "mods.cu", "no_alloc.cu", "legacy.cu",
+           "evalues.cu", "ions.cu"]
 
 
 def nvcc() -> str:

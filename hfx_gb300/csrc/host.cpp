@@ -12,6 +12,7 @@
 #include "lists.h"
 #include "mods.h"
 #include "evalues.h"
+#include "ions.h"
 #include "../../include/hfx_gpu.h"
 
 #include <algorithm>
@@ -121,6 +122,9 @@ struct hfx_ctx {
     int64_t cap_stride = 0;
     uint32_t cap_groups = 0, cap_items = 0, cap_mitems = 0;
     int64_t last_stride = 0;
+    // the preprocessed rows ("rows32", "meta") of the last search: their stride and spectrum count
+    int64_t rows_stride = 0;
+    int32_t rows_nspec = 0;
     uint32_t last_items = 0, last_mitems = 0;
     bool graph_valid = false;
     cudaGraphExec_t graph_exec = nullptr;
@@ -363,6 +367,8 @@ int32_t run_stage_a(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, in
     }
     rows = ctx->buf<float>("rows32", (size_t)b.nspec * stride, e);
     if (e) return cuda_fail(ctx, e, "alloc rows");
+    ctx->rows_stride = stride;
+    ctx->rows_nspec = b.nspec;
     rows_bf = nullptr;
     rows_h = nullptr;
     if (want_bf) {
@@ -1236,6 +1242,29 @@ int32_t hfx_search_evalues(hfx_ctx *ctx, const hfx_search_params *p, const float
     if (!rc) rc = hfx_evalue_fit(sorted, soff, size, ns, bin_width, cutoff_perc, out_fit, ctx->stream);
     if (!rc) rc = hfx_evalue_apply(out_s, out_k, out_fit, ns, p->top_n, out_ev, ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "E-values");
+    return search_finish(ctx);
+}
+
+int32_t hfx_match_ions(hfx_ctx *ctx, const hfx_search_params *p, const float *z, int32_t nspec,
+                       const uint64_t *keys, int32_t top_n, int32_t *out_matched, int32_t *out_total) {
+    if (!ctx || !p || nspec < 0 || top_n < 1 || !z || !keys || !out_matched || !out_total)
+        return fail(ctx, HFX_ERR_ARG, "bad hfx_match_ions arguments");
+    if (nspec == 0) return HFX_OK;
+    if (nspec != ctx->rows_nspec || ctx->rows_stride <= 0)
+        return fail(ctx, HFX_ERR_ARG, "hfx_match_ions needs the spectra of the last search on this context");
+    HFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaError_t e;
+    const SpecMeta *meta = ctx->buf<SpecMeta>("meta", nspec, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    const float *rows = ctx->buf<float>("rows32", (size_t)nspec * ctx->rows_stride, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    HFX_CUDA(ctx->d_err.ensure(16), "alloc err");
+    HFX_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, 4, ctx->stream), "memset err");
+    // the spectrum bin width (IonSeries.hs:139 binWidth cp)
+    const int rc = hfx_match_ions_launch(ctx->devdb(), ctx->devmods(), ctx->num_ions, meta, rows, ctx->rows_stride,
+                                         z, p->bin_width, keys, nspec, top_n, out_matched, out_total,
+                                         ctx->d_err.as<uint32_t>(), ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_match_ions");
     return search_finish(ctx);
 }
 

@@ -164,6 +164,19 @@ int32_t hfx_search_evalues(hfx_ctx *ctx, const hfx_search_params *p, const float
                            const int64_t *off, const float *pcr, const float *z, const float *tol, int32_t nspec,
                            int32_t bin_width, float cutoff_perc, float *out_score, uint64_t *out_key,
                            uint32_t *out_pep, int64_t *out_ncand, double *out_ev, double *out_fit);
+/* The "Ions" column of the results (Match.hs:36-44 scoreSP over
+ * IonSeries.hs:87-147), device buffers: for each result key of the last
+ * search on this context (hfx_search, hfx_search_device or
+ * hfx_search_evalues over the same nspec spectra; z the same charges and p
+ * the same bin width), out_matched / out_total [nspec][top_n] = matched b
+ * and y ions / (peptide text length - 5) * 2.  The peaks are the 200 largest
+ * values of the spectrum's preprocessed row (ties at the 200th value taken
+ * in index order), binned by index / 3; the ions are the b ladder of the
+ * unmodified peptide for charges 1 .. max(1, z-1) as (m + H*c) / c and
+ * (M+H)+ minus each, binned by round(mz / bin_width / 3) (host masses).
+ * Empty slots get 0 / 0. */
+int32_t hfx_match_ions(hfx_ctx *ctx, const hfx_search_params *p, const float *z, int32_t nspec,
+                       const uint64_t *keys, int32_t top_n, int32_t *out_matched, int32_t *out_total);
 /* Result record of one match (Match.hs:17-27): Location.hs:42-58 lookup --
  * the peptide text "X.PEPTIDE.Y" with its flanking residues ('-' at a
  * protein end) and (M+H)+ = residual + H + H2O (host masses) -- and for a

@@ -740,6 +740,44 @@ int32_t hfxo_search_scores(const uint8_t *ions, const float *mt, const float *r,
     return status;
 }
 
+void hfxo_match_ions(const float *x, int32_t len, float z, float bw,
+                     const uint8_t *pep, int32_t L, const float *mt, float mh,
+                     int32_t nstar, int32_t *matched, int32_t *total) {
+    /* IonSeries.hs:99-109 extractPeaks */
+    std::vector<int32_t> order((size_t)std::max(len, 0));
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return x[a] > x[b]; });
+    const int32_t np = len / 3 + 1;
+    std::vector<float> peaks((size_t)np, 0.0f);
+    for (int32_t k = 0; k < std::min(len, 200); ++k) {
+        const int32_t i = order[k];
+        peaks[i / 3] = std::max(peaks[i / 3], x[i]);
+    }
+    /* IonSeries.hs:87-91 bions: charges [1 .. max 1 (charge-1)] */
+    std::vector<float> ions;
+    const float lim = std::max(1.0f, z - 1.0f);
+    for (float c = 1.0f; c <= lim + 0.5f; c = c + 1.0f) {
+        float m = 0.0f;
+        for (int32_t a = 0; a < L; ++a) {
+            m = m + mt[pep[a] - 'A'];
+            ions.push_back((m + kHostH * c) / c);   /* IonSeries.hs:44 ionMZ */
+        }
+    }
+    /* IonSeries.hs:132-147 matchIonSequence */
+    auto hit = [&](float v) {
+        const float q = (v / bw) / 3.0f;
+        const double rq = (double)std::nearbyint(q);
+        if (!(rq >= 0.0 && rq < (double)np)) return 0;
+        return peaks[(size_t)rq] > 0.0f ? 1 : 0;
+    };
+    int32_t cnt = 0;
+    const size_t n = ions.size();
+    for (size_t k = 0; k + 1 < n; ++k) cnt += hit(ions[k]);      /* init (b) */
+    for (size_t k = 1; k < n; ++k) cnt += hit(mh - ions[k]);     /* tail (y) */
+    *matched = cnt;
+    *total = (L + 4 + nstar - 5) * 2;                            /* Match.hs:41 */
+}
+
 int32_t hfxo_search(const uint8_t *ions, const float *mt, const float *r,
                     const uint32_t *tc, const uint32_t *tn,
                     const uint32_t *idx, int64_t num_pep, const float *mz,

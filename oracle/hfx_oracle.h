@@ -144,6 +144,26 @@ int32_t hfxo_search(const uint8_t *ions, const float *mt26, const float *r,
                     float *out_score, double *out_score64, uint64_t *out_key,
                     uint32_t *out_pep, int64_t *out_ncand);
 
+/* The "Ions" column of one match (Match.hs:36-44 scoreSP over
+ * IonSeries.hs:87-147 extractPeaks / matchIonSequence / bions):
+ *   peaks: the 200 largest values of the spectrum's sequestXCorr vector x
+ *          (ties: lower index first), each max'ed (from 0) into bin i/3 of
+ *          len/3 + 1 bins;
+ *   ions:  for charge c = 1, 2, ... while c <= max(1, z-1) + 1/2 (Float
+ *          enumeration), the ladder of prefix sums of the peptide's residue
+ *          masses (mt26, the last one the whole peptide), each as
+ *          (m + H*c) / c (host H);
+ *   b = every ion but the last of the whole list, y = mh - ion for every
+ *   ion but the first; an ion matches when round((v / bw) / 3) (halves to
+ *   even) is a peak bin with a value above 0;
+ *   matched = matching b + y; total = (text length - 5) * 2 with the text
+ *   "X.PEPTIDE.Y" plus one '*' per modified residue (nstar).
+ * pep[L]: the letters of the unmodified peptide; mh: its (M+H)+
+ * ((res + H) + H2O, host masses). */
+void hfxo_match_ions(const float *x, int32_t len, float z, float bw,
+                     const uint8_t *pep, int32_t L, const float *mt26, float mh,
+                     int32_t nstar, int32_t *matched, int32_t *total);
+
 /* As hfxo_search, and also every candidate's score (plain candidates in
  * mass order, then modified isoforms by combination, position and rank) at
  * sink[sink_off[s] ...]: the score list the reference hands to its E-value

@@ -59,6 +59,7 @@ def lib():
             "hfxo_mod_isoform": (C.c_uint32, [P, C.c_uint32, C.c_uint32, P, i32, P, C.c_uint32, i32, P, P]),
             "hfxo_search": (i32, [P, P, P, P, P, P, i64, P, P, P, P, P, P, i32, C.POINTER(Params), i32,
                                   P, P, P, P, P]),
+            "hfxo_match_ions": (None, [P, i32, f32, f32, P, i32, P, f32, i32, P, P]),
             "hfxo_search_scores": (i32, [P, P, P, P, P, P, i64, P, P, P, P, P, P, i32, C.POINTER(Params), i32,
                                          P, P, P, P, P, P, P]),
         }
@@ -237,6 +238,18 @@ def search(ions_packed, mt, r, tc, tn, idx, spectra, bw=1.0005079, custom_bw=Fal
     if rc != 0:
         raise RuntimeError(f"oracle search status {rc}")
     return sc, s64, key, pep, nc, [sink[soff[i]:soff[i + 1]].copy() for i in range(ns)]
+
+
+def match_ions(x, z, pep, mt, mh, nstar=0, bw=1.0005079):
+    """The "Ions" column (matched, total) of one match (Match.hs:36-44 over
+    IonSeries.hs:87-147); pep: the unmodified peptide's letters (bytes)."""
+    x = np.ascontiguousarray(x, np.float32)
+    pb = np.frombuffer(bytes(pep), np.uint8).copy()
+    m = C.c_int32()
+    t = C.c_int32()
+    lib().hfxo_match_ions(_p(x), len(x), float(z), float(bw), _p(pb), len(pb),
+                          _p(np.ascontiguousarray(mt, np.float32)), float(mh), int(nstar), C.byref(m), C.byref(t))
+    return m.value, t.value
 
 
 def evalue_fit(scores, bin_width=350, cutoff_perc=3.0):
