@@ -29,7 +29,7 @@ BIN_WIDTH_AVG = 1.0011413
 EXPORTED = [
     "hfx_default_params", "hfx_ctx_create", "hfx_ctx_destroy", "hfx_set_stream",
     "hfx_last_error", "hfx_build_db", "hfx_upload_db", "hfx_db_info", "hfx_db_export", "hfx_autotune", "hfx_match_peptide",
-    "hfx_set_protein_segments", "hfx_match_ions",
+    "hfx_set_protein_segments", "hfx_match_ions", "hfx_mass_table",
     "hfx_set_mods", "hfx_mod_table", "hfx_search_host", "hfx_search_device", "hfx_search_evalues",
     "hfx_preprocess", "hfx_find_windows", "hfx_ion_bins", "hfx_mod_isoforms", "hfx_digest", "hfx_pack_ions",
     "hfx_set_profiling", "hfx_stage_stats", "hfx_search_counters",
@@ -95,6 +95,7 @@ def load_library(path: str = LIB_PATH):
         "hfx_search_evalues": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, P, i32, i32, C.c_float, P, P, P, P,
                                      P, P]),
         "hfx_match_ions": (i32, [P, C.POINTER(SearchParams), P, i32, P, i32, P, P]),
+        "hfx_mass_table": (i32, [i32, P, P]),
         "hfx_autotune": (i32, [P, C.POINTER(SearchParams), P, P, P, P, P, P, i32, P, P, P, P, i32,
                                C.POINTER(C.c_float)]),
         "hfx_match_peptide": (i32, [P, u64, C.c_uint32, C.c_char_p, i32, C.POINTER(C.c_float),
@@ -136,6 +137,16 @@ def _ptr(a) -> int | None:
         assert a.flags["C_CONTIGUOUS"]
         return a.ctypes.data
     return a.data_ptr()  # torch tensor on the device
+
+
+def mass_table(mono: bool = True, static_add=None) -> np.ndarray:
+    """hfx_mass_table: residue masses A..Z (Config.hs:266-272) plus static
+    additions."""
+    lib = load_library()
+    add = np.zeros(26, np.float32) if static_add is None else np.ascontiguousarray(static_add, np.float32)
+    out = np.empty(26, np.float32)
+    lib.hfx_mass_table(int(mono), _ptr(add), _ptr(out))
+    return out
 
 
 def digest(seq, seg, mass_table, rule=1, missed=2, min_mass=400.0, max_mass=7200.0, proline_rule=False,

@@ -1008,13 +1008,19 @@ int32_t hfx_pack_ions(const uint8_t *ascii, uint64_t n, const uint8_t *ma, int32
     return HFX_OK;
 }
 
+int32_t hfx_mass_table(int32_t mono, const float *add26, float *out26) {
+    if (!out26) return HFX_ERR_ARG;
+    // Config.hs:266-272 initializeAAMasses: static add + residue mass
+    for (int i = 0; i < 26; ++i) out26[i] = (add26 ? add26[i] : 0.0f) + (mono ? kMonoMass[i] : kAvgMass[i]);
+    return HFX_OK;
+}
+
 int32_t hfx_build_db(hfx_ctx *ctx, const uint8_t *seq, const uint32_t *seg, int32_t nprot, const float *add26,
                      int32_t mono, int32_t rule, int32_t missed, float min_mass, float max_mass,
                      int32_t proline_rule, int32_t min_len, int32_t max_len) {
     if (!ctx || !seq || !seg || nprot < 0 || missed < 0 || rule < 0 || rule > 13)
         return fail(ctx, HFX_ERR_ARG, "bad hfx_build_db arguments");
-    // Config.hs:266-272: table = static add + residue mass
-    for (int i = 0; i < 26; ++i) ctx->mt[i] = (add26 ? add26[i] : 0.0f) + (mono ? kMonoMass[i] : kAvgMass[i]);
+    hfx_mass_table(mono, add26, ctx->mt);
     const uint32_t nion = seg[nprot];
     for (uint32_t i = 0; i < nion; ++i)
         if (seq[i] < 'A' || seq[i] > 'Z') return fail(ctx, HFX_ERR_ARG, "residue outside A-Z");

@@ -61,6 +61,7 @@ class Spectra:
     z: np.ndarray
     tol: np.ndarray
     source: list = field(default_factory=list)   # generating peptide of each spectrum
+    title: list = field(default_factory=list)    # ms2info (MGF TITLE) of each spectrum, when read from a file
 
     def arrays(self):
         return self.mz, self.it, self.off, self.pcr, self.z, self.tol
@@ -78,7 +79,8 @@ class Spectra:
             off.append(off[-1] + (b - a))
         return Spectra(np.concatenate(mz).astype(np.float32), np.concatenate(it).astype(np.float32),
                        np.array(off, np.int64), self.pcr[idx].copy(), self.z[idx].copy(),
-                       self.tol[idx].copy(), [self.source[i] for i in idx] if self.source else [])
+                       self.tol[idx].copy(), [self.source[i] for i in idx] if self.source else [],
+                       [self.title[i] for i in idx] if self.title else [])
 
 
 def proteins(n: int, seed: int, len_lo: int = 100, len_hi: int = 800) -> Proteins:

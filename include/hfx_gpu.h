@@ -110,13 +110,17 @@ int64_t hfx_digest(const uint8_t *seq, const uint32_t *seg, int32_t nprot, const
                    int32_t rule, int32_t missed, float min_mass, float max_mass, int32_t proline_rule,
                    int32_t min_len, int32_t max_len, float *r, uint32_t *tc, uint32_t *tn, int64_t cap);
 int32_t hfx_pack_ions(const uint8_t *ascii, uint64_t n, const uint8_t *ma, int32_t num_ma, uint8_t *out);
+/* Host-only: the residue mass table of Config.hs:266-272 (initializeAAMasses):
+ * out26[c] = static_add26[c] (nullable: 0) + the mono or average mass of c. */
+int32_t hfx_mass_table(int32_t mono, const float *static_add26, float *out26);
 
 /* Upload a prebuilt database (r, tc, tn per fragment, ASCII residues) --
  * the SequenceDB fields of Fragment.hs:151-158. */
 int32_t hfx_upload_db(hfx_ctx *ctx, const uint8_t *ions_ascii, uint64_t num_ions, const float *r,
                       const uint32_t *tc, const uint32_t *tn, uint64_t num_pep,
                       const float *mass_table26);
-/* Database sizes and host copies in residual-mass order. */
+/* Database sizes and host copies: r, tc, tn per fragment in digest order,
+ * idx_sorted[q] = the fragment at residual-mass position q. */
 int32_t hfx_db_info(const hfx_ctx *ctx, uint64_t *num_ions, uint64_t *num_pep);
 int32_t hfx_db_export(const hfx_ctx *ctx, float *r, uint32_t *tc, uint32_t *tn, uint32_t *idx_sorted,
                       float *mass_table26);

@@ -1,0 +1,100 @@
+"""End to end through the file readers: a FASTA (and .gz) database and MGF
+spectra written from the seeded workload, read back by libhfx_gpu.so and
+searched, give the same results as the in-memory arrays; so does a database
+written to a .index file and uploaded from it (readIndex + withDeviceDB)."""
+import gzip
+
+import numpy as np
+import pytest
+
+from hfx_gb300 import io as hio
+from hfx_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _fasta(prot):
+    out = []
+    for i in range(len(prot.seg) - 1):
+        s = bytes(prot.seq[prot.seg[i]:prot.seg[i + 1]])
+        out.append(b">sp|P%05d|PROT%d Protein %d" % (i, i, i))
+        out += [s[k:k + 60] for k in range(0, len(s), 60)]
+    return b"\n".join(out) + b"\n"
+
+
+def _f(x):
+    return np.format_float_positional(np.float32(x), unique=True, trim="0")
+
+
+def _mgf(sp):
+    out = []
+    for i in range(len(sp)):
+        out += ["BEGIN IONS", f"TITLE=spectrum {i}", f"PEPMASS={_f(sp.pcr[i])}", f"CHARGE={int(sp.z[i])}+"]
+        a, b = sp.off[i], sp.off[i + 1]
+        out += [f"{_f(m)} {_f(v)}" for m, v in zip(sp.mz[a:b], sp.it[a:b])]
+        out.append("END IONS")
+    return ("\n".join(out) + "\n").encode()
+
+
+def _same(a, b):
+    assert np.array_equal(a.key, b.key) and np.array_equal(a.pep, b.pep) and np.array_equal(a.ncand, b.ncand)
+    assert np.array_equal(a.score.view(np.uint32), b.score.view(np.uint32))
+
+
+@pytest.fixture(scope="module")
+def direct(gpulib, tiny):
+    import hfx_gb300
+    prot, sp, cfg = tiny
+    sub = sp.subset(np.arange(48))
+    eng = hfx_gb300.Engine(0)
+    eng.build_db(prot.seq, prot.seg, static_add=synth.static_mods(), **synth.DIGEST)
+    res = eng.search(sub, hfx_gb300.default_params(top_n=10, batch_mode=1))
+    yield eng, prot, sub, res
+    eng.close()
+
+
+@pytest.mark.parametrize("gz", [False, True])
+def test_fasta_and_mgf_files(direct, tmp_path, gz):
+    import hfx_gb300
+    eng0, prot, sub, ref = direct
+    data = _fasta(prot)
+    db = tmp_path / ("db.fasta.gz" if gz else "db.fasta")
+    db.write_bytes(gzip.compress(data) if gz else data)
+    (tmp_path / "run.mgf").write_bytes(_mgf(sub))
+    pf = hio.read_fasta(str(db))
+    assert pf.seq.tobytes() == prot.seq.tobytes() and np.array_equal(pf.seg, prot.seg)
+    spx = hio.read_spectra(str(tmp_path / "run.mgf"), tol=float(sub.tol[0]))
+    spx.tol = sub.tol.copy()
+    assert spx.title[3] == b"spectrum 3"
+    assert np.array_equal(spx.mz.view(np.uint32), sub.mz.view(np.uint32))
+    eng = hfx_gb300.Engine(0)
+    try:
+        eng.build_db(pf.seq, pf.seg, static_add=synth.static_mods(), **synth.DIGEST)
+        _same(eng.search(spx, hfx_gb300.default_params(top_n=10, batch_mode=1)), ref)
+    finally:
+        eng.close()
+
+
+def test_index_file(direct, tmp_path):
+    import hfx_gb300
+    eng0, prot, sub, ref = direct
+    r, tc, tn, idx, mt = eng0.db_export()      # fragments in digest order
+    nf = len(idx)
+    frag_seg = np.concatenate([np.searchsorted(tc, prot.seg[:-1]), [nf]]).astype(np.uint32)
+    adds = {chr(ord("A") + i): float(v) for i, v in enumerate(synth.static_mods()) if v != 0}
+    opts = "\n" + "".join(f"{k} = {v}\n" for k, v in [("database", "db.fasta"), ("missed-cleavages", 1),
+                                                       ("digestion-rule", 1), ("aa-mass-type", "Mono")])
+    opts += "".join(f"add_{k} = {_f(v)}\n" for k, v in adds.items())
+    headers = [b"sp|P%05d" % i for i in range(len(prot.seg) - 1)]
+    path = str(tmp_path / "db.index")
+    hio.write_index(path, hio.IndexFile(opts, headers, prot.seq, prot.seg, r, tc, tn, frag_seg))
+    x = hio.read_index(path)
+    assert np.array_equal(x.mass_table().view(np.uint32), mt.view(np.uint32))
+    eng = hfx_gb300.Engine(0)
+    try:
+        eng.upload_db(x.ions, x.r, x.c, x.n, x.mass_table())
+        _same(eng.search(sub, hfx_gb300.default_params(top_n=10, batch_mode=1)), ref)
+    finally:
+        eng.close()
