@@ -218,3 +218,89 @@ def decode_index(data: bytes):
     c, n, frag_seg = words(), words(), words()
     return dict(options=options, headers=headers, ions=ions, ion_seg=ion_seg, r=np.array(r, np.float32), c=c, n=n,
                 frag_seg=frag_seg)
+
+
+# ------------------------------------------------------------------ text output
+# GHC Numeric (base < 4.6) restated over numpy's Dragon4 shortest digits:
+# floatToDigits, roundTo (halves up on the first dropped digit) and the
+# formatRealFloat layouts; Util/PrettyPrint.hs:99-211 for the tables.
+
+def float_digits(x, f32):
+    if x == 0:
+        return [0], 0
+    s = np.format_float_scientific(np.float32(x) if f32 else np.float64(x), unique=True, trim="-")
+    mant, ex = s.split("e")
+    ds = [int(c) for c in mant if c.isdigit()]
+    while len(ds) > 1 and ds[-1] == 0:
+        ds.pop()
+    return ds, int(ex) + 1
+
+
+def round_to(d, ds):
+    c = 1 if d < len(ds) and ds[d] >= 5 else 0
+    out = []
+    for k in range(d - 1, -1, -1):
+        v = (ds[k] if k < len(ds) else 0) + c
+        out.append(0 if v == 10 else v)
+        c = 1 if v == 10 else 0
+    out.reverse()
+    return (1, [1] + out) if c else (0, out)
+
+
+def show_ffloat(x, dec=4, f32=False):
+    x = float(np.float32(x)) if f32 else float(x)
+    if math.isnan(x):
+        return "NaN"
+    if math.isinf(x):
+        return "-Infinity" if x < 0 else "Infinity"
+    if x < 0 or (x == 0 and math.copysign(1, x) < 0):
+        return "-" + show_ffloat(-x, dec, f32)
+    ds, e = float_digits(x, f32)
+    if e >= 0:
+        ei, r = round_to(dec + e, ds)
+        s = "".join(map(str, r))
+        ls, rs = s[:e + ei] or "0", s[e + ei:]
+        return ls + ("." + rs if rs else "")
+    ei, r = round_to(dec, [0] * (-e) + ds)
+    r = r if ei else [0] + r
+    s = "".join(map(str, r))
+    return s[0] + ("." + s[1:] if len(s) > 1 else "")
+
+
+def show_efloat(x, dec=4):
+    x = float(x)
+    if math.isnan(x):
+        return "NaN"
+    if math.isinf(x):
+        return "-Infinity" if x < 0 else "Infinity"
+    if x < 0 or (x == 0 and math.copysign(1, x) < 0):
+        return "-" + show_efloat(-x, dec)
+    d = max(dec, 1)
+    ds, e = float_digits(x, False)
+    if ds == [0]:
+        return "0." + "0" * d + "e0"
+    ei, r = round_to(d + 1, ds)
+    if ei:
+        r = r[:-1]
+    s = "".join(map(str, r))
+    return s[0] + "." + s[1:] + "e" + str(e - 1 + ei)
+
+
+def show_float32(x):
+    x = float(np.float32(x))
+    if math.isnan(x):
+        return "NaN"
+    if x < 0 or (x == 0 and math.copysign(1, x) < 0):
+        return "-" + show_float32(-x)
+    ds, e = float_digits(x, True)
+    s = "".join(map(str, ds))
+    if e < 0 or e > 7:
+        return "0.0e0" if s == "0" else s[0] + "." + (s[1:] or "0") + "e" + str(e - 1)
+    if e == 0:
+        return "0." + s
+    return s[:e].ljust(e, "0") + "." + (s[e:] or "0")
+
+
+def pp_as_rows(rows, q):
+    w = [max(len(r[c]) for r in rows) for c in range(len(rows[0]))]
+    return "\n".join(" ".join(cell + " " * (w[c] - len(cell) + q) for c, cell in enumerate(r)) for r in rows)

@@ -161,3 +161,37 @@ def test_ions_ties_at_the_200th_peak(eng_tiny, oracle):
         free = np.nonzero(key[k + a] == pos)[0]
         assert len(tied) == 1 and len(free) == 1, (a, key[a], pos)
         assert got_m[a, tied[0]] < got_m[k + a, free[0]], (a, got_m[a], got_m[k + a])
+
+
+def test_scan_report(eng_tiny):
+    """printScanResults text of searched spectra: the header, the results
+    table with the search's own XCorr / Ions / E-value and the details."""
+    import hfx_gb300
+    from hfx_gb300 import report
+    eng, prot, sp = eng_tiny
+    sub = sp.subset(np.arange(6))
+    headers = [b"sp|P%05d|PROT%d Protein %d - Homo sapiens" % (i, i, i) for i in range(len(prot.seg) - 1)]
+    dev = _dev(sub)
+    out = _out(len(sub), 10)
+    out["ev"] = torch.empty((len(sub), 10), dtype=torch.float64, device="cuda:0")
+    out["fit"] = torch.empty((len(sub), 3), dtype=torch.float64, device="cuda:0")
+    p = hfx_gb300.default_params(top_n=10, batch_mode=1)
+    eng.search_evalues(dev, p, out)
+    eng.match_ions(dev, p, out)
+    res = hfx_gb300.SearchResult(score=out["score"].cpu().numpy(), key=out["key"].cpu().numpy().view(np.uint64),
+                                 pep=out["pep"].cpu().numpy().view(np.uint32), ncand=out["ncand"].cpu().numpy())
+    ions = (out["ions_matched"].cpu().numpy(), out["ions_total"].cpu().numpy())
+    ev = out["ev"].cpu().numpy()
+    for i in range(len(sub)):
+        txt = report.scan_report(eng, headers, sub, i, res, ions, ev, "run.mgf", "db.fasta", "Trypsin KR P")
+        blocks = txt.split("\n\n")
+        assert len(blocks) == 4 and blocks[-1] == ""
+        rows = blocks[1].split("\n")
+        assert rows[0].split() == ["#", "(M+H)+", "deltCn", "XCorr", "Ions", "Reference", "Peptide", "E-value"]
+        top = rows[2].split()
+        text, mh, prot_i = eng.match(int(res.key[i, 0]), int(res.pep[i, 0]))
+        assert top[0] == "1." and top[2] == "0.0000" and top[6] == text
+        assert top[4] == f"{ions[0][i, 0]}/{ions[1][i, 0]}" and top[5] == headers[prot_i].split()[0].decode()
+        assert top[3] == report.format_number(float(np.float32(res.score[i, 0] / np.float32(10000))), 2)
+        assert top[7] == report.format_number(float(ev[i, 0]), 3)
+        assert blocks[2].split("\n")[0].startswith(" 1.  " + headers[prot_i].decode())
