@@ -571,6 +571,37 @@ __device__ __forceinline__ float reduce_scatter(float (&acc)[G]) {
     return s;
 }
 
+// reduce_scatter<G> within each half-warp (lanes 0-15 and 16-31 reduce
+// separately): member j's sum ends in lanes j * (16 / G) .. of each half.
+template <int G>
+__device__ __forceinline__ float reduce_scatter16(float (&acc)[G]) {
+    const int lane = threadIdx.x & 31;
+    float v[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) v[g] = acc[g];
+    int n = G;
+    int off = 8;
+#pragma unroll
+    for (int step = 0; step < 4; ++step) {
+        if (n == 1) break;
+        const int half = n / 2;
+        const bool hi = (lane & off) != 0;
+#pragma unroll
+        for (int k = 0; k < G / 2; ++k) {
+            if (k < half) {
+                const float send = hi ? v[k] : v[half + k];
+                const float keep = hi ? v[half + k] : v[k];
+                v[k] = __fadd_rn(keep, __shfl_xor_sync(kFullMask, send, off));
+            }
+        }
+        n = half;
+        off >>= 1;
+    }
+    float s = v[0];
+    for (; off >= 1; off >>= 1) s = __fadd_rn(s, __shfl_xor_sync(kFullMask, s, off));
+    return s;
+}
+
 // Compact the planes (clearing them) into the sorted distinct-bin list and
 // accumulate the gather-dot for every active spectrum; every lane ends with
 // the canonical sums.

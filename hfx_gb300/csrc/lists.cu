@@ -20,6 +20,7 @@
 #include "batched.h"
 #include "lists.h"
 #include <algorithm>
+#include <type_traits>
 #include "batched_common.cuh"
 
 namespace hfx {
@@ -463,7 +464,13 @@ __global__ void __launch_bounds__(256) k_rescore_lists(const E *__restrict__ lis
 // E = list entry type (uint16_t up to 16,383 bins, uint32_t for long rows);
 // kGlobal: the group tile is read from global memory (L2) instead of being
 // staged in shared memory (rows too long for shared memory).
-template <typename T, int G, typename E, bool kGlobal>
+// kPair: two candidates per warp, one per half-warp (entry i of a list by
+// lane i % 16 of its half).  The per-candidate work around the list --
+// the claim, the reduction, the admission -- is then shared by two
+// candidates.  It changes the order of the sums, so it serves the BF16/FP16
+// pass only, whose scores pick the candidates that FP32 rescoring orders;
+// FP32 scoring keeps the canonical order (kPair false).
+template <typename T, int G, typename E, bool kGlobal, bool kPair>
 __global__ void __launch_bounds__(1024, 1)
 k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, uint64_t total10,
               uint64_t list_total, const uint16_t *__restrict__ list_len, uint32_t num_pep,
@@ -474,8 +481,11 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
               float *__restrict__ part_s, uint64_t *__restrict__ part_k, unsigned long long *__restrict__ stats,
               float *__restrict__ sink, const uint64_t *__restrict__ sink_off, uint32_t qoff,
               uint32_t *__restrict__ err) {
+    static_assert(!kPair || G <= 8, "half-warp candidates take up to 8 spectra per group");
+    constexpr int kW = kPair ? 16 : 32;  // lanes per candidate
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int hl = lane & (kW - 1), half = kPair ? lane >> 4 : 0;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     T *stile = reinterpret_cast<T *>(smem + 128);
     const T *tile = stile;
@@ -545,19 +555,24 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
             }
             phase ^= 1u;
         }
-        const uint32_t my_b = lane < G ? s_wb[lane] : 0u, my_e = lane < G ? s_we[lane] : 0u;
+        // member hl's window, in each half
+        const uint32_t my_b = hl < G ? s_wb[hl] : 0u, my_e = hl < G ? s_we[hl] : 0u;
         const int z = (int)gi.charges;
         const uint16_t *llen = list_len + (size_t)(z >= 1 ? z - 1 : 0) * num_pep;
         // Three-stage software pipeline over the warp's candidates: while
-        // candidate i is scored, candidate i+1's first 128 list entries are
-        // in flight and candidate i+2 is claimed with its list length and
+        // candidate i is scored, candidate i+1's first list entries are in
+        // flight and candidate i+2 is claimed with its list length and
         // offset loads in flight, so no stage waits on a dependent load.
+        // Per lane: its half's candidate; `live` (warp-uniform) while any
+        // candidate was claimed.
         struct Meta {
             uint32_t p, act, n, ls;
+            bool live;
         };
         struct Cand {
             uint32_t p, act;
             int n;
+            bool live;
             const E *lp;
             uint32_t e[4];
         };
@@ -568,13 +583,17 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
             m.ls = 0u;
             while (true) {
                 uint32_t q = 0;
-                if (lane == 0) q = atomicAdd(&s_next, 1u);
-                m.p = __shfl_sync(kFullMask, q, 0);
-                if (m.p >= p1) break;
-                m.act = __ballot_sync(kFullMask, lane < G && my_b <= m.p && m.p < my_e) & ((1u << G) - 1u);
-                if (m.act) break;
+                if (lane == 0) q = atomicAdd(&s_next, kPair ? 2u : 1u);
+                const uint32_t base = __shfl_sync(kFullMask, q, 0);
+                m.live = base < p1;
+                m.p = base + (uint32_t)half;
+                if (!m.live) break;
+                const uint32_t bal =
+                    __ballot_sync(kFullMask, hl < G && m.p < p1 && my_b <= m.p && m.p < my_e);
+                m.act = (bal >> (16 * half)) & ((1u << G) - 1u);
+                if (bal) break;
             }
-            if (m.p < p1 && z >= 1 && m.p < num_pep) {
+            if (m.act && z >= 1 && m.p < num_pep) {
                 m.n = llen[m.p];
                 m.ls = lstart[m.p];
             }
@@ -585,11 +604,12 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
             c.p = m.p;
             c.act = m.act;
             c.n = (int)m.n;
+            c.live = m.live;
             c.lp = lists;
-            if (m.p < p1 && z >= 1) {
+            if (m.act && z >= 1) {
                 const uint64_t off = total10 * (uint64_t)(z * (z - 1) / 2) + (uint64_t)z * m.ls;
                 if (m.p >= num_pep || off + (uint64_t)c.n > list_total) {
-                    if (lane == 0) atomicOr(err, kErrBounds);
+                    if (hl == 0) atomicOr(err, kErrBounds);
                     c.n = 0;
                 } else {
                     c.lp = lists + off;
@@ -597,58 +617,81 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
             }
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const int i = 32 * k + lane;
+                const int i = kW * k + hl;
                 c.e[k] = i < c.n ? (uint32_t)__ldg(c.lp + i) : 0xFFFFFFFFu;
             }
             return c;
         };
         Meta ahead = claim();
         Cand nxt = issue(ahead);
-        if (nxt.p < p1) ahead = claim();
-        while (nxt.p < p1) {
+        if (nxt.live) ahead = claim();
+        while (nxt.live) {
             const Cand cur = nxt;
             nxt = issue(ahead);
-            if (nxt.p < p1) ahead = claim();
+            if (nxt.live) ahead = claim();
             float acc[G];
 #pragma unroll
             for (int j = 0; j < G; ++j) acc[j] = 0.0f;
             const int n = cur.n;
-            my_cand += 1u;
-            my_entries += (uint32_t)n;
-            my_psm += (uint32_t)__popc(cur.act);
-            // entries [i0, i0+128) in e, the next 128 already in flight in f
+            const int nmax = kPair ? max(n, __shfl_xor_sync(kFullMask, n, 16)) : n;
+            // entries [i0, i0 + 4 kW) in e, the next 4 kW already in flight in f
             uint32_t e[4], f[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 e[k] = cur.e[k];
-                const int i = 128 + 32 * k + lane;
+                const int i = 4 * kW + kW * k + hl;
                 f[k] = i < n ? (uint32_t)__ldg(cur.lp + i) : 0xFFFFFFFFu;
             }
-            for (int i0 = 0; i0 < n; i0 += 128) {
+            for (int i0 = 0; i0 < nmax; i0 += 4 * kW) {
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const uint32_t bin = e[k] >> 2;
                     if ((int32_t)bin < nb) TileFma<T, G>::fma(tile, bin, e[k] & 3u, acc);
                 }
                 // lists ascend: once an entry lies beyond the tile, so do the rest
-                if ((__shfl_sync(kFullMask, e[3], 31) >> 2) >= (uint32_t)nb) break;
+                const uint32_t last = __shfl_sync(kFullMask, e[3], (lane & ~(kW - 1)) | (kW - 1));
+                if (__all_sync(kFullMask, (last >> 2) >= (uint32_t)nb)) break;
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     e[k] = f[k];
-                    const int i = i0 + 256 + 32 * k + lane;
+                    const int i = i0 + 8 * kW + kW * k + hl;
                     f[k] = i < n ? (uint32_t)__ldg(cur.lp + i) : 0xFFFFFFFFu;
                 }
             }
-            const float sc = reduce_scatter<G>(acc);
-            if (sink) {
-                // every pair's score, at its member's window offset
-                if ((lane & (32 / G - 1)) == 0 && ((cur.act >> my_slot) & 1u))
-                    sink[s_off[my_slot] + (cur.p - s_wb[my_slot])] = sc;
-                continue;
+            if constexpr (kPair) {
+                const float sc = reduce_scatter16<G>(acc);
+                const uint32_t act_a = __shfl_sync(kFullMask, cur.act, 0), act_b = __shfl_sync(kFullMask, cur.act, 16);
+                const uint32_t p_a = __shfl_sync(kFullMask, cur.p, 0), p_b = __shfl_sync(kFullMask, cur.p, 16);
+                const int n_a = __shfl_sync(kFullMask, n, 0), n_b = __shfl_sync(kFullMask, n, 16);
+                my_cand += (act_a != 0u) + (act_b != 0u);
+                my_entries += (uint32_t)(n_a + n_b);
+                my_psm += (uint32_t)(__popc(act_a) + __popc(act_b));
+                // member j's sums sit in lanes j * 16 / G of each half; its
+                // admission lane is j * 32 / G
+                const float sc_a = __shfl_sync(kFullMask, sc, lane >> 1);
+                const float sc_b = __shfl_sync(kFullMask, sc, 16 + (lane >> 1));
+                const bool owner = (lane & (32 / G - 1)) == 0;
+                const bool want_a = owner && ((act_a >> my_slot) & 1u) &&
+                                    score_order(sc_a) >= *(volatile uint32_t *)(thr_u + my_slot);
+                slots.offer(want_a, sc_a, p_a, my_slot, K);
+                const bool want_b = owner && ((act_b >> my_slot) & 1u) &&
+                                    score_order(sc_b) >= *(volatile uint32_t *)(thr_u + my_slot);
+                slots.offer(want_b, sc_b, p_b, my_slot, K);
+            } else {
+                my_cand += 1u;
+                my_entries += (uint32_t)n;
+                my_psm += (uint32_t)__popc(cur.act);
+                const float sc = reduce_scatter<G>(acc);
+                if (sink) {
+                    // every pair's score, at its member's window offset
+                    if ((lane & (32 / G - 1)) == 0 && ((cur.act >> my_slot) & 1u))
+                        sink[s_off[my_slot] + (cur.p - s_wb[my_slot])] = sc;
+                    continue;
+                }
+                const bool want = (lane & (32 / G - 1)) == 0 && ((cur.act >> my_slot) & 1u) &&
+                                  score_order(sc) >= *(volatile uint32_t *)(thr_u + my_slot);
+                slots.offer(want, sc, cur.p, my_slot, K);
             }
-            const bool want = (lane & (32 / G - 1)) == 0 && ((cur.act >> my_slot) & 1u) &&
-                              score_order(sc) >= *(volatile uint32_t *)(thr_u + my_slot);
-            slots.offer(want, sc, cur.p, my_slot, K);
         }
         slots.drain(K);
         __syncthreads();  // every warp has merged its queues
@@ -727,7 +770,7 @@ static size_t lists_queue_offset(bool global_tile, int64_t stride, int G, size_t
     return 128 + (global_tile ? 0 : (((size_t)stride * G * elem_bytes + 15) & ~(size_t)15));
 }
 
-template <typename T, int G, typename E, bool kGlobal>
+template <typename T, int G, typename E, bool kGlobal, bool kPair>
 static int launch_lists_t(const E *lists, const uint32_t *lstart, uint64_t total10, const uint16_t *list_len,
                           uint32_t num_pep, int64_t stride, const uint32_t *wb, const uint32_t *we,
                           const BatchedWs &ws, void *tiles, int32_t K, int nw,
@@ -741,7 +784,7 @@ static int launch_lists_t(const E *lists, const uint32_t *lstart, uint64_t total
     const size_t qoff = lists_queue_offset(kGlobal, stride, G, sizeof(T));
     const size_t smem = qoff + (size_t)nw * CtaSlots<G>::warp_bytes();
     if (smem > (size_t)smem_max) return (int)cudaErrorInvalidValue;
-    auto fn = k_score_lists<T, G, E, kGlobal>;
+    auto fn = k_score_lists<T, G, E, kGlobal, kPair>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
     int per = 0;
@@ -761,8 +804,8 @@ int hfx_lists_group_fits(int32_t G, int long_rows, int64_t stride, int elem_byte
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaFuncAttributes fa{};
     const cudaError_t e =
-        long_rows ? cudaFuncGetAttributes(&fa, k_score_lists<__nv_bfloat16, 16, uint32_t, true>)
-                  : cudaFuncGetAttributes(&fa, k_score_lists<__nv_bfloat16, 16, uint16_t, false>);
+        long_rows ? cudaFuncGetAttributes(&fa, k_score_lists<__nv_bfloat16, 16, uint32_t, true, false>)
+                  : cudaFuncGetAttributes(&fa, k_score_lists<__nv_bfloat16, 16, uint16_t, false, false>);
     if (e != cudaSuccess) return 0;
     const size_t smem = lists_queue_offset(long_rows != 0, stride, 16, (size_t)elem_bytes) +
                         (size_t)list_warps(16) * CtaSlots<16>::warp_bytes();
@@ -774,15 +817,21 @@ int hfx_lists_score(const void *lists, int long_rows, const uint32_t *lstart, ui
                     const uint32_t *we, const BatchedWs &ws, void *tiles, int32_t G, int32_t K, int nw,
                     float *part_s, uint64_t *part_k, unsigned long long *stats, uint32_t *err, cudaStream_t st,
                     float *sink, const uint64_t *sink_off) {
+    // BF16/FP16 groups of up to 8 spectra score two candidates per warp
+    // (their scores only choose what FP32 rescoring orders); FP32 scoring,
+    // with or without a sink, keeps the canonical order
+    if (elem_kind != 0 && sink) return (int)cudaErrorInvalidValue;
 #define HFX_L(T, GG)                                                                                           \
     do {                                                                                                       \
+        constexpr bool kP = !std::is_same<T, float>::value && GG <= 8;                                         \
         if (long_rows)                                                                                         \
-            return launch_lists_t<T, GG, uint32_t, true>((const uint32_t *)lists, lstart, total10, list_len,   \
-                                                         num_pep, stride, wb, we, ws, tiles, K, nw, part_s,    \
-                                                         part_k, stats, sink, sink_off, err, st);              \
-        return launch_lists_t<T, GG, uint16_t, false>((const uint16_t *)lists, lstart, total10, list_len,      \
-                                                      num_pep, stride, wb, we, ws, tiles, K, nw, part_s,       \
-                                                      part_k, stats, sink, sink_off, err, st);                 \
+            return launch_lists_t<T, GG, uint32_t, true, kP>((const uint32_t *)lists, lstart, total10,         \
+                                                             list_len, num_pep, stride, wb, we, ws, tiles, K,  \
+                                                             nw, part_s, part_k, stats, sink, sink_off, err,   \
+                                                             st);                                              \
+        return launch_lists_t<T, GG, uint16_t, false, kP>((const uint16_t *)lists, lstart, total10, list_len,  \
+                                                          num_pep, stride, wb, we, ws, tiles, K, nw, part_s,   \
+                                                          part_k, stats, sink, sink_off, err, st);             \
     } while (0)
     if (elem_kind == 0) {
         if (G == 4) HFX_L(float, 4);
