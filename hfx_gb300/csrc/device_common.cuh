@@ -244,9 +244,16 @@ template <> __device__ __forceinline__ float load_x<__half>(const __half *row, u
     return __half2float(row[i]);
 }
 
-__device__ __forceinline__ float level_weight(uint32_t lvl) {
-    return lvl == 3u ? 50.0f : (lvl == 2u ? 25.0f : 10.0f);
+// Weight of a list entry's level: 10, 25, 50 for levels 1, 2, 3 (0 for
+// level 0).  The three values share their low 16 bits (zero) and differ in
+// two bytes, which one byte permute picks by level: bytes 1..3 of `lo` and
+// 5..7 of `hi` are the third and fourth bytes of 10.0f, 25.0f, 50.0f.
+__device__ __forceinline__ uint32_t level_weight_hi16(uint32_t lvl) {
+    uint32_t r;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(0x48C82000u), "r"(0x42414100u), "r"(lvl * 0x11u + 0x40u));
+    return r & 0xFFFFu;  // the bf16 (upper half) bits of the weight
 }
+__device__ __forceinline__ float level_weight(uint32_t lvl) { return __uint_as_float(level_weight_hi16(lvl) << 16); }
 
 // A set of spectra scored against the same candidate list.
 template <typename T, int G>
@@ -349,10 +356,13 @@ template <> struct TileLoad<float, 8> {
 // fmaf(weight, float(x), acc): bit-identical to the FP32 path, without the
 // conversions.
 __device__ __forceinline__ uint16_t level_weight_bf16(uint32_t lvl) {
-    return lvl == 3u ? (uint16_t)0x4248u : (lvl == 2u ? (uint16_t)0x41C8u : (uint16_t)0x4120u);  // 50, 25, 10
+    return (uint16_t)level_weight_hi16(lvl);  // 0x4120, 0x41C8, 0x4248 = 10, 25, 50
 }
 __device__ __forceinline__ uint16_t level_weight_f16(uint32_t lvl) {
-    return lvl == 3u ? (uint16_t)0x5240u : (lvl == 2u ? (uint16_t)0x4E40u : (uint16_t)0x4900u);  // 50, 25, 10
+    // 0x4900, 0x4E40, 0x5240 = 10, 25, 50 in FP16, by the same byte permute
+    uint32_t r;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(0x40400000u), "r"(0x524E4900u), "r"(lvl * 0x11u + 0x40u));
+    return (uint16_t)(r & 0xFFFFu);
 }
 
 template <typename T, int G>

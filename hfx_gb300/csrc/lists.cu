@@ -548,6 +548,15 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
                 mbar_arrive_expect_tx(bar, bytes);
                 bulk_g2s(stile, tiles + (size_t)g * stride * G, bytes, bar);
             }
+            // bins [nb, stride + 8) of the shared tile read as zero: every
+            // list bin (< stride) and the pad entry (bin = stride) may be
+            // gathered without a bounds test
+            {
+                uint4 *z = reinterpret_cast<uint4 *>(stile);
+                const size_t z0 = (size_t)nb * G * sizeof(T) / 16, z1 = (size_t)(stride + 8) * G * sizeof(T) / 16;
+                for (size_t i = z0 + threadIdx.x; i < z1; i += blockDim.x) z[i] = make_uint4(0u, 0u, 0u, 0u);
+                fence_proxy_async();  // before a later item's bulk copy overwrites these bytes
+            }
             __syncthreads();
             if (!mbar_wait(bar, phase, kWaitLimit)) {
                 if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
@@ -557,6 +566,10 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
         }
         // member hl's window, in each half
         const uint32_t my_b = hl < G ? s_wb[hl] : 0u, my_e = hl < G ? s_we[hl] : 0u;
+        // entry past a list's end: the zero bin `stride` of the shared tile
+        // (beyond every group's bins, so it also ends the scan), or an
+        // out-of-range bin for tiles in global memory
+        const uint32_t pad = kGlobal ? 0xFFFFFFFFu : ((uint32_t)stride << 2);
         const int z = (int)gi.charges;
         const uint16_t *llen = list_len + (size_t)(z >= 1 ? z - 1 : 0) * num_pep;
         // Three-stage software pipeline over the warp's candidates: while
@@ -618,7 +631,7 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const int i = kW * k + hl;
-                c.e[k] = i < c.n ? (uint32_t)__ldg(c.lp + i) : 0xFFFFFFFFu;
+                c.e[k] = i < c.n ? (uint32_t)__ldg(c.lp + i) : pad;
             }
             return c;
         };
@@ -640,13 +653,17 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
             for (int k = 0; k < 4; ++k) {
                 e[k] = cur.e[k];
                 const int i = 4 * kW + kW * k + hl;
-                f[k] = i < n ? (uint32_t)__ldg(cur.lp + i) : 0xFFFFFFFFu;
+                f[k] = i < n ? (uint32_t)__ldg(cur.lp + i) : pad;
             }
             for (int i0 = 0; i0 < nmax; i0 += 4 * kW) {
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const uint32_t bin = e[k] >> 2;
-                    if ((int32_t)bin < nb) TileFma<T, G>::fma(tile, bin, e[k] & 3u, acc);
+                    if constexpr (kGlobal) {
+                        if ((int32_t)bin < nb) TileFma<T, G>::fma(tile, bin, e[k] & 3u, acc);
+                    } else {
+                        TileFma<T, G>::fma(tile, bin, e[k] & 3u, acc);  // zero beyond nb
+                    }
                 }
                 // lists ascend: once an entry lies beyond the tile, so do the rest
                 const uint32_t last = __shfl_sync(kFullMask, e[3], (lane & ~(kW - 1)) | (kW - 1));
@@ -655,7 +672,7 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
                 for (int k = 0; k < 4; ++k) {
                     e[k] = f[k];
                     const int i = i0 + 8 * kW + kW * k + hl;
-                    f[k] = i < n ? (uint32_t)__ldg(cur.lp + i) : 0xFFFFFFFFu;
+                    f[k] = i < n ? (uint32_t)__ldg(cur.lp + i) : pad;
                 }
             }
             if constexpr (kPair) {
@@ -767,7 +784,9 @@ constexpr int list_warps(int G) { return G >= 16 ? 32 : 16; }
 // Dynamic shared memory of the list scorer: an mbarrier, the group tile
 // (none when it is read from global memory), then the warps' queues.
 static size_t lists_queue_offset(bool global_tile, int64_t stride, int G, size_t elem_bytes) {
-    return 128 + (global_tile ? 0 : (((size_t)stride * G * elem_bytes + 15) & ~(size_t)15));
+    // the shared tile holds stride + 8 bins: the zero bins after the group's
+    // rows and the pad entry's bin
+    return 128 + (global_tile ? 0 : (((size_t)(stride + 8) * G * elem_bytes + 15) & ~(size_t)15));
 }
 
 template <typename T, int G, typename E, bool kGlobal, bool kPair>
