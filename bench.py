@@ -46,7 +46,7 @@ KERNELS = {0: "k_score_spectrum", 1: "k_score_lists", 2: "k_score_batched"}
 # DRAM bytes (read + write) per launch of the scorer, from one ncu capture
 # of the default workload (profiles/k_score_lists_full_bf16.md), keyed by
 # (kernel, workload, precision, spectra).
-TRAFFIC = {("k_score_lists", "full", 1, 10000): 2.711e9 + 13.1e6}
+TRAFFIC = {("k_score_lists", "full", 1, 10000): 2.699e9 + 13.1e6}
 
 
 def _args():
