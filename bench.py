@@ -321,11 +321,13 @@ def main():
     cpu_n, agree_n, plain_n = _samples(a)
     a.cpu_sample, a.agree_sample = cpu_n, agree_n
     graph = int(mode != 0 and not a.no_graph)
-    p = hfx_gb300.default_params(top_n=cfg["top_n"], precision=prec, batch_mode=mode, rescore_k=32 if prec else 0,
+    # candidates rescored in FP32: the top-50 at 0.02 Da (its configuration asks for them), 32 elsewhere
+    rk = (50 if a.workload == "highres" else 32) if prec else 0
+    p = hfx_gb300.default_params(top_n=cfg["top_n"], precision=prec, batch_mode=mode, rescore_k=rk,
                                  group_size=a.group_size, chunk=a.chunk, use_graph=graph, **_pkw(cfg))
     # stage events and work counters need the eager launches
     p_prof = hfx_gb300.default_params(top_n=cfg["top_n"], precision=prec, batch_mode=mode,
-                                      rescore_k=32 if prec else 0, group_size=a.group_size, chunk=a.chunk,
+                                      rescore_k=rk, group_size=a.group_size, chunk=a.chunk,
                                       **_pkw(cfg))
     d = torch.device("cuda", local)
     dev = dict(mz=torch.from_numpy(sp.mz).to(d), it=torch.from_numpy(sp.it).to(d),
@@ -474,7 +476,8 @@ def main():
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"{a.workload}: " + DESCRIBE.get(a.workload, "{n} spectra").format(n=ns),
                    "psm_per_step": psm_step,
-                   "precision": ["fp32", "bf16 store + fp32 rescore", "fp16 store + fp32 rescore"][prec],
+                   "precision": ["fp32", "bf16 store + fp32 rescore", "fp16 store + fp32 rescore"][prec]
+                   + (f" of the top {rk}" if prec else ""),
                    "batch_mode": ["per-spectrum launches", "batched over ion lists", "batched fused"][mode],
                    "launch": "one CUDA-graph replay per step" if graph else "eager launches",
                    "autotuned": tuned,

@@ -22,6 +22,7 @@
 #include "batched.h"
 #include "batched_common.cuh"
 #include "mods_device.cuh"
+#include <type_traits>
 
 namespace hfx {
 
@@ -267,6 +268,8 @@ k_score_batched(DevDB db, const T *__restrict__ tiles, int64_t stride, const uin
 }
 
 // Per spectrum: merge its slot of every item of its group.
+// R = 1: up to 32 kept per spectrum (WarpTopK), R = 2: up to 64 (WarpTopK64).
+template <int R>
 __global__ void k_merge_items(const float *__restrict__ part_s, const uint64_t *__restrict__ part_k,
                               const uint32_t *__restrict__ item_off, const int32_t *__restrict__ group_of,
                               const int32_t *__restrict__ slot_of, const SpecMeta *__restrict__ meta, int32_t nspec,
@@ -275,25 +278,43 @@ __global__ void k_merge_items(const float *__restrict__ part_s, const uint64_t *
     const int lane = threadIdx.x & 31;
     const int32_t s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (s >= nspec) return;
-    WarpTopK tk;
+    typename std::conditional<R == 1, WarpTopK, WarpTopK64>::type tk;
     tk.init();
     if (meta[s].status == 0) {
         const int32_t g = group_of[s], j = slot_of[s];
         for (uint32_t it = item_off[g]; it < item_off[g + 1]; ++it) {
             const size_t o = ((size_t)it * G + j) * K;
-            const float sc = lane < K ? part_s[o + lane] : -INFINITY;
-            const uint64_t kk = lane < K ? part_k[o + lane] : ~0ull;
-            for (int t = 0; t < K; ++t) {
-                const float ts = __shfl_sync(kFullMask, sc, t);
-                const uint64_t tk2 = __shfl_sync(kFullMask, kk, t);
-                if (tk2 == ~0ull) break;
-                tk.insert(ts, tk2, kout);
+            bool done = false;
+            for (int r = 0; r < R && !done; ++r) {
+                const int i = 32 * r + lane;
+                const float sc = i < K ? part_s[o + i] : -INFINITY;
+                const uint64_t kk = i < K ? part_k[o + i] : ~0ull;
+                for (int t = 0; t < 32 && 32 * r + t < K; ++t) {
+                    const float ts = __shfl_sync(kFullMask, sc, t);
+                    const uint64_t tk2 = __shfl_sync(kFullMask, kk, t);
+                    if (tk2 == ~0ull) {
+                        done = true;  // the item's list ends here
+                        break;
+                    }
+                    tk.insert(ts, tk2, kout);
+                }
             }
         }
     }
-    if (lane < kout) {
-        out_s[(size_t)s * kout + lane] = tk.s;
-        out_k[(size_t)s * kout + lane] = tk.k;
+    if constexpr (R == 1) {
+        if (lane < kout) {
+            out_s[(size_t)s * kout + lane] = tk.s;
+            out_k[(size_t)s * kout + lane] = tk.k;
+        }
+    } else {
+        if (lane < kout) {
+            out_s[(size_t)s * kout + lane] = tk.s0;
+            out_k[(size_t)s * kout + lane] = tk.k0;
+        }
+        if (32 + lane < kout) {
+            out_s[(size_t)s * kout + 32 + lane] = tk.s1;
+            out_k[(size_t)s * kout + 32 + lane] = tk.k1;
+        }
     }
 }
 
@@ -527,8 +548,13 @@ int hfx_clamp_items(uint32_t *off, int64_t n1, uint32_t cap, uint32_t *err, cuda
 int hfx_batched_merge(const float *part_s, const uint64_t *part_k, const BatchedWs &ws, const SpecMeta *meta,
                       int32_t nspec, int32_t G, int32_t K, int32_t kout, float *out_s, uint64_t *out_k,
                       cudaStream_t st) {
-    k_merge_items<<<(nspec + 3) / 4, 128, 0, st>>>(part_s, part_k, ws.item_off, ws.group_of, ws.slot_of, meta, nspec,
-                                                   G, K, kout, out_s, out_k);
+    if (kout > kMaxKept || K > kMaxKept) return (int)cudaErrorInvalidValue;
+    if (kout > 32 || K > 32)
+        k_merge_items<2><<<(nspec + 3) / 4, 128, 0, st>>>(part_s, part_k, ws.item_off, ws.group_of, ws.slot_of, meta,
+                                                          nspec, G, K, kout, out_s, out_k);
+    else
+        k_merge_items<1><<<(nspec + 3) / 4, 128, 0, st>>>(part_s, part_k, ws.item_off, ws.group_of, ws.slot_of, meta,
+                                                          nspec, G, K, kout, out_s, out_k);
     return (int)cudaGetLastError();
 }
 

@@ -112,12 +112,15 @@ __host__ __device__ constexpr size_t cta_queue_bytes(int G, int key_bytes) {
     return (size_t)G * cta_queue_len(G) * (4 + key_bytes);
 }
 
-template <int G, typename Key = uint32_t, int Q = cta_queue_len(G)>
+// L: entries per member list (32, or 64 to keep up to 64 candidates: each
+// lane then holds list entries lane and 32 + lane).
+template <int G, typename Key = uint32_t, int Q = cta_queue_len(G), int L = 32>
 struct CtaSlots {
+    static_assert(L == 32 || L == 64, "member lists hold 32 or 64 entries");
     static constexpr int kQ = Q;
     static constexpr Key kNone = ~Key(0);
-    float *ls;       // [G][32] scores of the CTA's lists
-    Key *lk;         // [G][32] keys
+    float *ls;       // [G][L] scores of the CTA's lists
+    Key *lk;         // [G][L] keys
     uint32_t *lock;  // [G]
     uint32_t *thr;   // [G] score_order of each list's K-th (0 = none yet)
     float *qs;       // this warp's queues: [G][kQ] scores, then [G][kQ] keys
@@ -139,9 +142,9 @@ struct CtaSlots {
         qn = 0u;
         err = err_;
     }
-    // Item start, by threads [0, 32 G) of the CTA (a barrier must follow).
+    // Item start, by threads [0, L G) of the CTA (a barrier must follow).
     __device__ __forceinline__ void reset_shared() {
-        for (int t = threadIdx.x; t < G * 32; t += blockDim.x) {
+        for (int t = threadIdx.x; t < G * L; t += blockDim.x) {
             ls[t] = -INFINITY;
             lk[t] = kNone;
         }
@@ -198,18 +201,51 @@ struct CtaSlots {
             return;
         }
         __threadfence_block();
-        float ws = *(volatile float *)(ls + j * 32 + lane);
-        Key wk = *(volatile Key *)(lk + j * 32 + lane);
-        // the top 32 of both lists as a bitonic sequence, then sorted best first
-        if (better(rs, rk, ws, wk)) {
-            ws = rs;
-            wk = rk;
-        }
+        float kth;
+        if constexpr (L == 32) {
+            float ws = *(volatile float *)(ls + j * 32 + lane);
+            Key wk = *(volatile Key *)(lk + j * 32 + lane);
+            // the top 32 of both lists as a bitonic sequence, then sorted best first
+            if (better(rs, rk, ws, wk)) {
+                ws = rs;
+                wk = rk;
+            }
 #pragma unroll
-        for (int d = 16; d > 0; d >>= 1) cx(ws, wk, d, true);
-        *(volatile float *)(ls + j * 32 + lane) = ws;
-        *(volatile Key *)(lk + j * 32 + lane) = wk;
-        const float kth = __shfl_sync(kFullMask, ws, K - 1);
+            for (int d = 16; d > 0; d >>= 1) cx(ws, wk, d, true);
+            *(volatile float *)(ls + j * 32 + lane) = ws;
+            *(volatile Key *)(lk + j * 32 + lane) = wk;
+            kth = __shfl_sync(kFullMask, ws, K - 1);
+        } else {
+            // entries lane (w0) and 32 + lane (w1); the queue, ascending, fills
+            // the last 16 of 64 positions (w1 of lanes 16..31, which rs holds)
+            float w0 = *(volatile float *)(ls + j * 64 + lane), w1 = *(volatile float *)(ls + j * 64 + 32 + lane);
+            Key k0 = *(volatile Key *)(lk + j * 64 + lane), k1 = *(volatile Key *)(lk + j * 64 + 32 + lane);
+            if (better(rs, rk, w1, k1)) {
+                w1 = rs;
+                k1 = rk;
+            }
+            // bitonic merge of the 64: positions i and i + 32 in the lane,
+            // then each half across lanes
+            if (better(w1, k1, w0, k0)) {
+                const float ts = w0;
+                const Key tk = k0;
+                w0 = w1;
+                k0 = k1;
+                w1 = ts;
+                k1 = tk;
+            }
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) {
+                cx(w0, k0, d, true);
+                cx(w1, k1, d, true);
+            }
+            *(volatile float *)(ls + j * 64 + lane) = w0;
+            *(volatile float *)(ls + j * 64 + 32 + lane) = w1;
+            *(volatile Key *)(lk + j * 64 + lane) = k0;
+            *(volatile Key *)(lk + j * 64 + 32 + lane) = k1;
+            const float a = __shfl_sync(kFullMask, w0, (K - 1) & 31), b = __shfl_sync(kFullMask, w1, (K - 1) & 31);
+            kth = K > 32 ? b : a;
+        }
         if (lane == 0 && kth != -INFINITY) *(volatile uint32_t *)(thr + j) = score_order(kth);
         __threadfence_block();
         __syncwarp();
@@ -249,13 +285,17 @@ struct CtaSlots {
         qn = 0u;
     }
 
-    // After a barrier: slot j's top-K (lanes < K; warp-wide).
+    // After a barrier: slot j's top-K (entries < K; warp-wide).
     __device__ __forceinline__ void result(int j, int K, float *out_s, uint64_t *out_k) const {
         const int lane = threadIdx.x & 31;
-        if (lane < K) {
-            const Key k = lk[j * 32 + lane];
-            out_s[lane] = ls[j * 32 + lane];
-            out_k[lane] = k == kNone ? ~0ull : (uint64_t)k;
+#pragma unroll
+        for (int r = 0; r < L / 32; ++r) {
+            const int i = 32 * r + lane;
+            if (i < K) {
+                const Key k = lk[j * L + i];
+                out_s[i] = ls[j * L + i];
+                out_k[i] = k == kNone ? ~0ull : (uint64_t)k;
+            }
         }
     }
 };

@@ -654,6 +654,38 @@ struct WarpTopK {
     }
 };
 
+// The same for up to 64 entries: lane l holds entries l (s0, k0) and
+// 32 + l (s1, k1).
+struct WarpTopK64 {
+    float s0, s1;
+    uint64_t k0, k1;
+    __device__ __forceinline__ void init() {
+        s0 = s1 = -INFINITY;
+        k0 = k1 = ~0ull;
+    }
+    __device__ __forceinline__ void insert(float ns, uint64_t nk, int K) {
+        const int lane = threadIdx.x & 31;
+        const int i0 = lane, i1 = 32 + lane;
+        const uint32_t b0 = __ballot_sync(kFullMask, i0 < K && better(s0, k0, ns, nk));
+        const uint32_t b1 = __ballot_sync(kFullMask, i1 < K && better(s1, k1, ns, nk));
+        const int pos = __popc(b0) + __popc(b1);
+        // entry i moves to i + 1 for pos <= i < K - 1
+        const float u0 = __shfl_up_sync(kFullMask, s0, 1), u1 = __shfl_up_sync(kFullMask, s1, 1);
+        const uint64_t v0 = __shfl_up_sync(kFullMask, k0, 1), v1 = __shfl_up_sync(kFullMask, k1, 1);
+        const float c = __shfl_sync(kFullMask, s0, 31);  // entry 31 becomes entry 32
+        const uint64_t ck = __shfl_sync(kFullMask, k0, 31);
+        if (pos < K) {
+            if (i0 == pos) { s0 = ns; k0 = nk; }
+            else if (i0 > pos && i0 < K) { s0 = u0; k0 = v0; }
+            if (i1 == pos) { s1 = ns; k1 = nk; }
+            else if (i1 > pos && i1 < K) {
+                s1 = lane == 0 ? c : u1;
+                k1 = lane == 0 ? ck : v1;
+            }
+        }
+    }
+};
+
 // Bounded spin on an mbarrier phase: returns false after max_iter tries.
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);

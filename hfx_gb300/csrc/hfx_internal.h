@@ -10,6 +10,7 @@ namespace hfx {
 constexpr int kListCap = 1056;   // u16 distinct-bin list entries per warp (1024 + 32)
 constexpr int kMaxWords = 256;   // bit-plane words per plane (8192 bins)
 constexpr int kMaxTopK = 32;     // per-warp top-K kept in registers
+constexpr int kMaxKept = 64;     // candidates kept per spectrum for FP32 rescoring (list scoring)
 
 struct LayoutParams {
     float bw;           // spectrum bin width (Correlation.hs:29-30)

@@ -464,12 +464,17 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     const int32_t chunk = p->chunk > 0 ? p->chunk : 4096;
     if (G != 1 && G != 2 && G != 4 && G != 8 && G != 16)
         return fail(ctx, HFX_ERR_ARG, "group_size must be 1, 2, 4, 8 or 16");
-    const int32_t K = elem_kind == 0 ? p->top_n : std::max(p->top_n, std::min(p->rescore_k > 0 ? p->rescore_k : 32,
-                                                                               kMaxTopK));
     // rows longer than the shared-memory bit planes: 32-bit sorted lists,
     // tiles read from global memory, list-based rescoring; no fused or
     // modification scoring
     const bool long_rows = stride > (int64_t)kMaxWords * 32;
+    // candidates kept for FP32 rescoring: up to 64 when unmodified candidates
+    // alone are list-scored in groups of up to 8, else up to 32
+    const bool lists_only = (p->batch_mode == 1 || long_rows) && !(p->search_mods != 0 && ctx->num_mod > 0);
+    const int32_t K = elem_kind == 0 ? p->top_n
+                                     : std::max(p->top_n, std::min(p->rescore_k > 0 ? p->rescore_k : 32,
+                                                                   lists_only ? kMaxKept : kMaxTopK));
+    if (K > 32 && G == 16) G = 8;
     if (G == 16) {
         // two 16-byte loads per bin: list scoring of BF16/FP16 rows only
         if (elem_kind == 0 || (p->batch_mode != 1 && !long_rows) || (p->search_mods != 0 && ctx->num_mod > 0))

@@ -410,8 +410,8 @@ __global__ void __launch_bounds__(256) k_rescore_lists(const E *__restrict__ lis
                                                        const uint64_t *__restrict__ kept_k, int32_t K, int32_t topn,
                                                        float *__restrict__ out_s, uint64_t *__restrict__ out_k,
                                                        uint32_t *__restrict__ out_pep, uint32_t *__restrict__ err) {
-    __shared__ float res_s[kMaxTopK];
-    __shared__ uint64_t res_k[kMaxTopK];
+    __shared__ float res_s[kMaxKept];
+    __shared__ uint64_t res_k[kMaxKept];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int32_t s = blockIdx.x;
     const SpecMeta m = meta[s];
@@ -470,7 +470,7 @@ __global__ void __launch_bounds__(256) k_rescore_lists(const E *__restrict__ lis
 // candidates.  It changes the order of the sums, so it serves the BF16/FP16
 // pass only, whose scores pick the candidates that FP32 rescoring orders;
 // FP32 scoring keeps the canonical order (kPair false).
-template <typename T, int G, typename E, bool kGlobal, bool kPair>
+template <typename T, int G, typename E, bool kGlobal, bool kPair, int L>
 __global__ void __launch_bounds__(1024, 1)
 k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, uint64_t total10,
               uint64_t list_total, const uint16_t *__restrict__ list_len, uint32_t num_pep,
@@ -494,8 +494,8 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
     __shared__ uint32_t s_wb[G], s_we[G];
     __shared__ uint64_t s_off[G];  // with a sink: where each member's window starts in it
     __shared__ uint32_t thr_u[G], s_lock[G];
-    __shared__ float s_ls[G * 32];
-    __shared__ uint32_t s_lk[G * 32];
+    __shared__ float s_ls[G * L];
+    __shared__ uint32_t s_lk[G * L];
     __shared__ unsigned long long s_stats[4];
 
     const int32_t ngroups = (int32_t)*ngroups_p;
@@ -506,7 +506,7 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
     const int my_slot = reduce_slot_of_lane<G>(lane);
     uint32_t my_cand = 0, my_entries = 0, my_psm = 0, my_claims = 0;
     uint32_t phase = 0;
-    CtaSlots<G> slots;
+    CtaSlots<G, uint32_t, cta_queue_len(G), L> slots;
     slots.bind(s_ls, s_lk, s_lock, thr_u, smem + qoff + (size_t)warp * CtaSlots<G>::warp_bytes(), err);
     while (true) {
         if (threadIdx.x == 0) s_item = (int32_t)atomicAdd(counter, 1u);
@@ -789,7 +789,7 @@ static size_t lists_queue_offset(bool global_tile, int64_t stride, int G, size_t
     return 128 + (global_tile ? 0 : (((size_t)(stride + 8) * G * elem_bytes + 15) & ~(size_t)15));
 }
 
-template <typename T, int G, typename E, bool kGlobal, bool kPair>
+template <typename T, int G, typename E, bool kGlobal, bool kPair, int L>
 static int launch_lists_t(const E *lists, const uint32_t *lstart, uint64_t total10, const uint16_t *list_len,
                           uint32_t num_pep, int64_t stride, const uint32_t *wb, const uint32_t *we,
                           const BatchedWs &ws, void *tiles, int32_t K, int nw,
@@ -803,7 +803,7 @@ static int launch_lists_t(const E *lists, const uint32_t *lstart, uint64_t total
     const size_t qoff = lists_queue_offset(kGlobal, stride, G, sizeof(T));
     const size_t smem = qoff + (size_t)nw * CtaSlots<G>::warp_bytes();
     if (smem > (size_t)smem_max) return (int)cudaErrorInvalidValue;
-    auto fn = k_score_lists<T, G, E, kGlobal, kPair>;
+    auto fn = k_score_lists<T, G, E, kGlobal, kPair, L>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
     int per = 0;
@@ -823,8 +823,8 @@ int hfx_lists_group_fits(int32_t G, int long_rows, int64_t stride, int elem_byte
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaFuncAttributes fa{};
     const cudaError_t e =
-        long_rows ? cudaFuncGetAttributes(&fa, k_score_lists<__nv_bfloat16, 16, uint32_t, true, false>)
-                  : cudaFuncGetAttributes(&fa, k_score_lists<__nv_bfloat16, 16, uint16_t, false, false>);
+        long_rows ? cudaFuncGetAttributes(&fa, k_score_lists<__nv_bfloat16, 16, uint32_t, true, false, 32>)
+                  : cudaFuncGetAttributes(&fa, k_score_lists<__nv_bfloat16, 16, uint16_t, false, false, 32>);
     if (e != cudaSuccess) return 0;
     const size_t smem = lists_queue_offset(long_rows != 0, stride, 16, (size_t)elem_bytes) +
                         (size_t)list_warps(16) * CtaSlots<16>::warp_bytes();
@@ -840,17 +840,26 @@ int hfx_lists_score(const void *lists, int long_rows, const uint32_t *lstart, ui
     // (their scores only choose what FP32 rescoring orders); FP32 scoring,
     // with or without a sink, keeps the canonical order
     if (elem_kind != 0 && sink) return (int)cudaErrorInvalidValue;
-#define HFX_L(T, GG)                                                                                           \
+    // up to 64 kept candidates per member in the BF16/FP16 two-per-warp pass
+    if (K > kMaxKept || (K > 32 && (elem_kind == 0 || G > 8))) return (int)cudaErrorInvalidValue;
+#define HFX_LL(T, GG, LL)                                                                                      \
     do {                                                                                                       \
         constexpr bool kP = !std::is_same<T, float>::value && GG <= 8;                                         \
         if (long_rows)                                                                                         \
-            return launch_lists_t<T, GG, uint32_t, true, kP>((const uint32_t *)lists, lstart, total10,         \
-                                                             list_len, num_pep, stride, wb, we, ws, tiles, K,  \
-                                                             nw, part_s, part_k, stats, sink, sink_off, err,   \
-                                                             st);                                              \
-        return launch_lists_t<T, GG, uint16_t, false, kP>((const uint16_t *)lists, lstart, total10, list_len,  \
-                                                          num_pep, stride, wb, we, ws, tiles, K, nw, part_s,   \
-                                                          part_k, stats, sink, sink_off, err, st);             \
+            return launch_lists_t<T, GG, uint32_t, true, kP, LL>((const uint32_t *)lists, lstart, total10,     \
+                                                                 list_len, num_pep, stride, wb, we, ws, tiles, \
+                                                                 K, nw, part_s, part_k, stats, sink, sink_off, \
+                                                                 err, st);                                     \
+        return launch_lists_t<T, GG, uint16_t, false, kP, LL>((const uint16_t *)lists, lstart, total10,        \
+                                                              list_len, num_pep, stride, wb, we, ws, tiles, K, \
+                                                              nw, part_s, part_k, stats, sink, sink_off, err,  \
+                                                              st);                                             \
+    } while (0)
+#define HFX_L(T, GG) HFX_LL(T, GG, 32)
+#define HFX_L64(T, GG)                 \
+    do {                               \
+        if (K > 32) HFX_LL(T, GG, 64); \
+        HFX_LL(T, GG, 32);             \
     } while (0)
     if (elem_kind == 0) {
         if (G == 4) HFX_L(float, 4);
@@ -858,18 +867,20 @@ int hfx_lists_score(const void *lists, int long_rows, const uint32_t *lstart, ui
         if (G == 2) HFX_L(float, 2);
         if (G == 1) HFX_L(float, 1);
     } else if (elem_kind == 1) {
-        if (G == 8) HFX_L(__nv_bfloat16, 8);
+        if (G == 8) HFX_L64(__nv_bfloat16, 8);
         if (G == 16) HFX_L(__nv_bfloat16, 16);
-        if (G == 4) HFX_L(__nv_bfloat16, 4);
-        if (G == 2) HFX_L(__nv_bfloat16, 2);
-        if (G == 1) HFX_L(__nv_bfloat16, 1);
+        if (G == 4) HFX_L64(__nv_bfloat16, 4);
+        if (G == 2) HFX_L64(__nv_bfloat16, 2);
+        if (G == 1) HFX_L64(__nv_bfloat16, 1);
     } else {
-        if (G == 8) HFX_L(__half, 8);
+        if (G == 8) HFX_L64(__half, 8);
         if (G == 16) HFX_L(__half, 16);
-        if (G == 4) HFX_L(__half, 4);
-        if (G == 2) HFX_L(__half, 2);
-        if (G == 1) HFX_L(__half, 1);
+        if (G == 4) HFX_L64(__half, 4);
+        if (G == 2) HFX_L64(__half, 2);
+        if (G == 1) HFX_L64(__half, 1);
     }
+#undef HFX_L64
+#undef HFX_LL
 #undef HFX_L
     return (int)cudaErrorInvalidValue;
 }

@@ -39,7 +39,8 @@ typedef struct hfx_search_params {
                                       spectrum, tol < 0 is |tol| ppm, tol >= 0 is Da           */
     int32_t top_n;                 /* matches kept per spectrum, 1..32                         */
     int32_t precision;             /* 0 FP32 rows; 1 BF16 rows + FP32 rescore; 2 FP16 + rescore */
-    int32_t rescore_k;             /* candidates rescored in FP32 (>= top_n, <= 32)            */
+    int32_t rescore_k;             /* candidates rescored in FP32 (>= top_n; <= 64 when only   */
+                                   /* unmodified candidates are list-scored, else <= 32)       */
     int32_t batch_mode;            /* 0 one launch per spectrum; 1 batched over per-step ion
                                       lists; 2 batched with ion lists rebuilt per work item    */
     int32_t fastdiv;               /* 1: __fdividef in ion m/z, as ion_series.cu:59-69         */

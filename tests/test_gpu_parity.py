@@ -410,3 +410,50 @@ def test_autotune_picks_a_valid_shape(full_engine):
     res = eng.search(sub, p)
     assert np.array_equal(res.key, ref.key)
     assert np.array_equal(res.score.view(np.uint32), ref.score.view(np.uint32))
+
+
+@pytest.mark.parametrize("G", [4, 8])
+def test_keep_64_candidates(full_engine, oracle, G):
+    """Up to 64 candidates kept per spectrum for FP32 rescoring (two member
+    lists of 32 per lane pair, 64-entry item merges): the top-32 after
+    rescoring equals the oracle's, and so does the top-10 with 50 kept."""
+    import hfx_gb300
+    eng, prot, sp = full_engine
+    sub = sp.subset(np.arange(96))
+    for top_n, keep in ((32, 64), (10, 50)):
+        ref = oracle.search(*_oracle_db(oracle, eng, prot), sub, topn=top_n)
+        p = hfx_gb300.default_params(top_n=top_n, batch_mode=1, precision=1, rescore_k=keep, group_size=G,
+                                     chunk=512)
+        _compare(eng.search(sub, p), ref, f"keep {keep} top {top_n} G={G}")
+
+
+def test_keep_50_at_002_da(tiny_engine, oracle):
+    """The 0.02 Da configuration's top-50 rescoring (long rows, 32-bit
+    lists, tiles read from L2)."""
+    import hfx_gb300
+    eng, prot, sp = tiny_engine
+    sub = _highres_subset(sp, 16)
+    ref = oracle.search(*_oracle_db(oracle, eng, prot), sub, topn=10, bw=HIGHRES, custom_bw=True, ion_bw=HIGHRES)
+    for prec in (1, 2):
+        p = hfx_gb300.default_params(top_n=10, bin_width=HIGHRES, custom_bin_width=1, batch_mode=1,
+                                     precision=prec, rescore_k=50, ion_bins_custom=1)
+        _compare(eng.search(sub, p), ref, f"0.02 Da keep 50 precision {prec}")
+
+
+def test_keep_more_than_32_capped_with_mods(gpulib, tiny, oracle):
+    """With modification search the kept candidates stay at most 32 (the
+    modified scorer's lists hold 32): a larger rescore_k is capped, and the
+    results still equal the oracle's."""
+    import hfx_gb300
+    prot, sp, cfg = tiny
+    eng = hfx_gb300.Engine(0)
+    try:
+        eng.build_db(prot.seq, prot.seg, static_add=synth.static_mods(), **synth.DIGEST)
+        eng.set_mods("MSTY", [15.995, 79.966, 79.966, 79.966], 4, False)
+        sub = sp.subset(np.arange(16))
+        db = _oracle_db(oracle, eng, prot, b"MSTY")
+        ref = oracle.search(*db, sub, topn=10, ma=b"MSTY", ma_mass=[15.995, 79.966, 79.966, 79.966], max_ma=4)
+        p = hfx_gb300.default_params(top_n=10, batch_mode=1, precision=1, rescore_k=64)
+        _compare(eng.search(sub, p), ref, "mods keep capped")
+    finally:
+        eng.close()
