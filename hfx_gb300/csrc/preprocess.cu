@@ -78,12 +78,39 @@ __global__ void k_layout(const float *__restrict__ mz, const int64_t *__restrict
 }
 
 // One CTA per spectrum; the whole row sits in shared memory.
+// Block-wide exclusive scan of one value per thread (blockDim.x <= 1024).
+__device__ __forceinline__ int32_t block_excl_scan(int32_t v, int32_t *warp_tot, int32_t &total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int32_t x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int32_t t = __shfl_up_sync(0xFFFFFFFFu, x, d);
+        if (lane >= d) x += t;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int32_t w = lane < nw ? warp_tot[lane] : 0;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int32_t t = __shfl_up_sync(0xFFFFFFFFu, w, d);
+            if (lane >= d) w += t;
+        }
+        warp_tot[lane] = w;
+    }
+    __syncthreads();
+    total = warp_tot[nw - 1];
+    const int32_t before = (warp ? warp_tot[warp - 1] : 0) + x - v;
+    __syncthreads();
+    return before;
+}
+
 __global__ void __launch_bounds__(256) k_preprocess(const float *__restrict__ mz, const float *__restrict__ it,
                                                     const int64_t *__restrict__ off,
                                                     const float *__restrict__ pcr, LayoutParams lp,
                                                     const SpecMeta *__restrict__ meta, int64_t stride,
                                                     float *__restrict__ out32, __nv_bfloat16 *__restrict__ outbf,
-                                                    __half *__restrict__ outh) {
+                                                    __half *__restrict__ outh, int fold_nonzero) {
     extern __shared__ float sh[];
     const int32_t s = blockIdx.x;
     const SpecMeta m = meta[s];
@@ -131,7 +158,28 @@ __global__ void __launch_bounds__(256) k_preprocess(const float *__restrict__ mz
         e[i] = (mx > 1e-6f && i < sel * 10) ? __fmul_rn(50.0f, __fdiv_rn(e[i], mx)) : 0.0f;
     }
     __syncthreads();
-    // crossCorrolation, Correlation.hs:105-109
+    // crossCorrolation, Correlation.hs:105-109.  Every e is >= 0, so the
+    // left fold over a window equals the left fold over its nonzero bins
+    // (adding +0 is exact and the sum never is -0); with fold_nonzero the
+    // nonzero bins are listed once in bin order (nz_val) with, per bin, how
+    // many precede it (nz_before), and each window folds only those.
+    float *nz_val = e + stride;
+    int32_t *nz_before = reinterpret_cast<int32_t *>(e + 2 * stride);
+    if (fold_nonzero) {
+        __shared__ int32_t warp_tot[32];
+        const int32_t per = (len + (int32_t)blockDim.x - 1) / (int32_t)blockDim.x;
+        const int32_t j0 = min(len, tid * per), j1 = min(len, j0 + per);
+        int32_t c = 0;
+        for (int32_t j = j0; j < j1; ++j) c += e[j] > 0.0f ? 1 : 0;
+        int32_t total = 0;
+        int32_t pos = block_excl_scan(c, warp_tot, total);
+        for (int32_t j = j0; j < j1; ++j) {
+            nz_before[j] = pos;
+            if (e[j] > 0.0f) nz_val[pos++] = e[j];
+        }
+        if (tid == 0) nz_before[len] = total;
+        __syncthreads();
+    }
     __nv_bfloat16 *obf = outbf ? outbf + (int64_t)s * stride : nullptr;
     __half *oh = outh ? outh + (int64_t)s * stride : nullptr;
     for (int64_t i = tid; i < stride; i += blockDim.x) {
@@ -140,7 +188,11 @@ __global__ void __launch_bounds__(256) k_preprocess(const float *__restrict__ mz
             const int32_t lo = max(0, (int32_t)i - 75);
             const int32_t hi = min(len, lo + 151);
             float acc = 0.0f;
-            for (int32_t j = lo; j < hi; ++j) acc = __fadd_rn(acc, e[j]);
+            if (fold_nonzero) {
+                for (int32_t t = nz_before[lo]; t < nz_before[hi]; ++t) acc = __fadd_rn(acc, nz_val[t]);
+            } else {
+                for (int32_t j = lo; j < hi; ++j) acc = __fadd_rn(acc, e[j]);
+            }
             x = __fsub_rn(e[i], __fdiv_rn(acc, 150.0f));
         }
         o32[i] = x;
@@ -162,32 +214,6 @@ __global__ void __launch_bounds__(256) k_preprocess(const float *__restrict__ mz
 constexpr int kSparsePeaks = 4096;
 constexpr size_t kDenseRowBytes = 200 * 1024;  // rows up to 51,200 bins are built densely in shared memory
 
-// Block-wide exclusive scan of one value per thread (blockDim.x <= 1024).
-__device__ __forceinline__ int32_t block_excl_scan(int32_t v, int32_t *warp_tot, int32_t &total) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    int32_t x = v;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const int32_t t = __shfl_up_sync(0xFFFFFFFFu, x, d);
-        if (lane >= d) x += t;
-    }
-    if (lane == 31) warp_tot[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-        int32_t w = lane < nw ? warp_tot[lane] : 0;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const int32_t t = __shfl_up_sync(0xFFFFFFFFu, w, d);
-            if (lane >= d) w += t;
-        }
-        warp_tot[lane] = w;
-    }
-    __syncthreads();
-    total = warp_tot[nw - 1];
-    const int32_t before = (warp ? warp_tot[warp - 1] : 0) + x - v;
-    __syncthreads();
-    return before;
-}
 
 __global__ void __launch_bounds__(256) k_preprocess_sparse(const float *__restrict__ mz, const float *__restrict__ it,
                                                            const int64_t *__restrict__ off,
@@ -362,7 +388,7 @@ int hfx_launch_preprocess(const float *mz, const float *it, const int64_t *off, 
                           const LayoutParams &lp, const SpecMeta *meta, int32_t nspec, int64_t stride,
                           float *out32, __nv_bfloat16 *outbf, __half *outh, uint32_t *err, cudaStream_t st) {
     if (nspec <= 0) return 0;
-    const size_t smem = (size_t)stride * sizeof(float);
+    size_t smem = (size_t)stride * sizeof(float);
     if (smem > kDenseRowBytes) {
         // long rows: the sparse form (needs the error word for its peak limit)
         if (!err) return (int)cudaErrorInvalidValue;
@@ -376,6 +402,11 @@ int hfx_launch_preprocess(const float *mz, const float *it, const int64_t *off, 
         cudaFuncSetAttribute(k_preprocess, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDenseRowBytes);
         attr_set = true;
     }
-    k_preprocess<<<nspec, 256, smem, st>>>(mz, it, off, pcr, lp, meta, stride, out32, outbf, outh);
+    // the row, its nonzero values and their running count (stride + 1 ints)
+    // when they fit; otherwise every window folds all its bins
+    const size_t smem3 = (size_t)stride * 8 + ((size_t)stride + 1) * 4;
+    const int fold_nonzero = smem3 <= kDenseRowBytes ? 1 : 0;
+    if (fold_nonzero) smem = smem3;
+    k_preprocess<<<nspec, 256, smem, st>>>(mz, it, off, pcr, lp, meta, stride, out32, outbf, outh, fold_nonzero);
     return (int)cudaGetLastError();
 }
