@@ -324,14 +324,17 @@ __global__ void __launch_bounds__(256) k_gen_lists_long(DevDB db, const int32_t 
         const uint32_t tc = db.tc_sorted[p], tn = db.tn_sorted[p];
         const float r = db.r_sorted[p];
         const uint32_t nchunk = (tn - tc + 31u) / 32u;
-        if (tn < tc || nchunk * 32u * (uint32_t)zmax * 10u > (uint32_t)kLongKeys) {
+        // keys of (prefix k, charge c) at 10 (k z + c - 1), padded to a power of two
+        uint32_t nmax = 32u;
+        while (tn >= tc && nmax < (tn - tc) * (uint32_t)zmax * 10u) nmax <<= 1;
+        if (tn < tc || nmax > (uint32_t)kLongKeys) {
             if (lane == 0) atomicOr(err, kErrTooLong);
             if (lane < kLevels && ((need >> lane) & 1u)) list_len[(size_t)lane * db.num_pep + p] = 0;
             continue;
         }
         for (int z = 1; z <= zmax; ++z) {
             if (!((need >> (z - 1)) & 1u)) continue;
-            const int32_t nslot = (int32_t)nchunk * 32 * z * 10;
+            const int32_t nslot = (int32_t)(tn - tc) * z * 10;
             int32_t n2 = 32;
             while (n2 < nslot) n2 <<= 1;
             for (int32_t i = lane; i < n2; i += 32) kb[i] = 0xFFFFFFFFu;
@@ -354,9 +357,10 @@ __global__ void __launch_bounds__(256) k_gen_lists_long(DevDB db, const int32_t 
                 carry = __shfl_sync(kFullMask, v, cnt - 1);
                 if (lane < cnt) {
                     const float y = __fsub_rn(r, v);
+                    const uint32_t k = 32u * ci + (uint32_t)lane;
                     for (int c = 1; c <= z; ++c)
                         emit_keys<FastDiv>(v, y, charge_const<FastDiv>(c), nbins, ibw,
-                                           kb + ((size_t)(ci * z + (c - 1)) * 32 + lane) * 10);
+                                           kb + ((size_t)k * z + (c - 1)) * 10);
                 }
             }
             __syncwarp();
