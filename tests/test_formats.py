@@ -215,3 +215,22 @@ def test_file_suffixes(tmp_path):
         hio.read_spectra(str(tmp_path / "c.txt"))
     with pytest.raises(hio.FormatError):
         hio.read_spectra(str(tmp_path / "missing.mgf"))
+
+
+def test_gzip_members_and_fasta_corners(F):
+    """Concatenated gzip members read as one stream; empty and letterless
+    sequence lines."""
+    a = b">p1 one\nACDE\n"
+    b = b">p2 two\n\n\nKKR\n>p3 empty\n>p4\nMM\n"
+    data = gzip.compress(a) + gzip.compress(b)
+    got = hio.parse_fasta(data, gz=True)
+    ref = F.read_fasta(data, gz=True)
+    assert got.headers == [h for h, _ in ref] == [b"p1 one", b"p2 two", b"p3 empty", b"p4"]
+    assert got.seq.tobytes() == b"ACDEKKRMM" and got.seg.tolist() == [0, 4, 7, 7, 9]
+
+
+def test_mgf_sample_without_peaks(F):
+    text = b"BEGIN IONS\nPEPMASS=712.5\nCHARGE=2+\nEND IONS\n"
+    got = hio.parse_spectra(text, "mgf")
+    assert len(got) == 1 and got.off.tolist() == [0, 0] and got.pcr[0] == np.float32(712.5)
+    assert F.read_mgf(text)[0][3] == []

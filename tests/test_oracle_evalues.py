@@ -1,9 +1,11 @@
 """CPU checks of the oracle's E-value restatement (Util/Statistics.hs:37-100):
 the slice ranks, the shift and the 4000 floor, the histogram points and the
-least-squares line, on hand-built score sets."""
+least-squares line, on hand-built score sets; and the full score list the
+fit reads (every unmodified candidate and modified isoform)."""
 import math
 
 import numpy as np
+import pytest
 
 
 def test_fit_recovers_a_known_line(oracle):
@@ -57,3 +59,25 @@ def test_empty_and_degenerate(oracle):
     a, b, m = oracle.evalue_fit(np.full(100, 5.0, np.float32))   # nothing clears 4000
     assert m == 0 and math.isnan(a)
     assert math.isclose(oracle.evalue(1.0, -2.0, 10000.0), 0.1, rel_tol=1e-15)
+
+
+@pytest.mark.parametrize("plain", [True, False])
+def test_all_scores_list_matches_top(oracle, plain):
+    """hfxo_search_scores hands back every candidate's score (unmodified,
+    then every modified isoform): as many as the candidate count, and its
+    best ten are the search's top-10 scores."""
+    from hfx_gb300 import synth
+    prot, sp, cfg = synth.workload("tiny")
+    ma, ma_mass = b"MSTY", [15.995, 79.966, 79.966, 79.966]
+    mt = oracle.mass_table(True, synth.static_mods())
+    dg = {k: v for k, v in synth.DIGEST.items() if k != "mono"}
+    r, tc, tn = oracle.digest(prot.seq, prot.seg, mt, **dg)
+    idx = oracle.sort_idx(r)
+    sub = sp.subset(np.arange(8))
+    sc, _, key, _, nc, all_sc = oracle.search(oracle.pack_ions(prot.seq, ma), mt, r, tc, tn, idx, sub, topn=10,
+                                              ma=ma, ma_mass=ma_mass, max_ma=4, plain=plain, all_scores=True)
+    for i in range(len(sub)):
+        assert len(all_sc[i]) == nc[i]
+        top = np.sort(all_sc[i])[::-1][:10]
+        v = sc[i][key[i] != np.iinfo(np.uint64).max]
+        assert np.array_equal(top[:len(v)].view(np.uint32), v.view(np.uint32)), i

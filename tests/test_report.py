@@ -129,3 +129,37 @@ def test_config_and_wrapping(F):
     d = R.format_detail([long, "short"]).split("\n")
     assert all(len(l) == len(d[0]) for l in d[:-2]) and d[-2:] == ["", ""]
     assert d[0].startswith(" 1.  word00 ") and d[1].startswith("     word") and len(d[0]) <= 3 + 2 + 95
+
+
+def test_scan_report_glue(F):
+    """scan_report assembles printScanResults from a search result, Ions and
+    E-values (the engine's record lookup stood in for by a table)."""
+    import types
+    from hfx_gb300 import synth
+
+    class Records:
+        def match(self, key, pep):
+            return (f"K.PEP{pep}TIDE.R", np.float32(1000.5 + pep), pep % 3)
+
+    headers = [b"sp|P0|A protein zero", b"sp|P1|B protein one", b"sp|P2|C protein two"]
+    sp = synth.Spectra(np.zeros(0, np.float32), np.zeros(0, np.float32), np.zeros(3, np.int64),
+                       np.array([500.25, 600.5], np.float32), np.array([2.0, 3.0], np.float32),
+                       np.array([3.0, 3.0], np.float32), [], [b"scan A", b"scan B"])
+    none = np.iinfo(np.uint64).max
+    res = types.SimpleNamespace(score=np.array([[52000.0, 31000.0, 0.0], [40000.0, 0.0, 0.0]], np.float32),
+                                key=np.array([[7, 9, none], [4, none, none]], np.uint64),
+                                pep=np.array([[3, 5, 0], [1, 0, 0]], np.uint32))
+    ions = (np.array([[12, 5, 0], [8, 0, 0]], np.int32), np.array([[26, 26, 0], [20, 0, 0]], np.int32))
+    ev = np.array([[1.5e-6, 0.25, np.nan], [3e-3, np.nan, np.nan]])
+    txt = R.scan_report(Records(), headers, sp, 0, res, ions, ev, "run.mgf", "db.fasta", "Trypsin KR P", tol=3.0)
+    blocks = txt.split("\n\n")
+    assert len(blocks) == 4 and blocks[-1] == ""
+    assert blocks[0].split("\n")[0].startswith("Title       :: scan A")
+    rows = [l.split() for l in blocks[1].split("\n")[2:]]
+    assert len(rows) == 2
+    assert rows[0] == ["1.", F.show_ffloat(1003.5, 4, f32=True), "0.0000", "5.2000", "12/26", "sp|P0|A",
+                       "K.PEP3TIDE.R", F.show_efloat(1.5e-6, 4)]
+    assert rows[1][2] == F.show_ffloat(float(np.float32((np.float32(5.2) - np.float32(3.1)) / np.float32(5.2))), 4)
+    assert rows[1][5] == "sp|P2|C" and rows[1][7] == F.show_efloat(0.25, 4)
+    det = blocks[2].split("\n")
+    assert det[0].startswith(" 1.  sp|P0|A protein zero") and det[1].startswith(" 2.  sp|P2|C protein two")
