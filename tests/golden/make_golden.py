@@ -1,6 +1,6 @@
 """Generate the golden fixtures of tests/golden from the REFERENCE's own code.
 
-Run here (not on the GPU machine): it needs the reference checkout and
+Run where the reference checkout is (not on a GPU machine): it needs it and
 oracle/_ref/libhfx_ref.so, which `make -C oracle ref` compiles from the
 reference's unmodified Thrust sources (filter.cu, filter_by_mod.cu,
 calc_mod_cands.cu, prepare_gen_mod.cu, gen_mod_pep.cu, prepare_scoring.cu,
