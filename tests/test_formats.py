@@ -234,3 +234,18 @@ def test_mgf_sample_without_peaks(F):
     got = hio.parse_spectra(text, "mgf")
     assert len(got) == 1 and got.off.tolist() == [0, 0] and got.pcr[0] == np.float32(712.5)
     assert F.read_mgf(text)[0][3] == []
+
+
+def test_index_options_mass_table(F):
+    """readIndex's readConfig over the options text: aa-mass-type and the
+    add_X lines give the residue table (Config.hs:197-216, 266-272)."""
+    import hfx_gb300
+    for mono in (True, False):
+        opts = F.index_options("db.fasta", 1, 1, 400.0, 7200.0, mono, {"C": 57.021, "M": 15.9949})
+        x = hio.IndexFile(opts, [], np.zeros(0, np.uint8), np.zeros(1, np.uint32), np.zeros(0, np.float32),
+                          np.zeros(0, np.uint32), np.zeros(0, np.uint32), np.zeros(1, np.uint32))
+        add = np.zeros(26, np.float32)
+        add[ord("C") - 65], add[ord("M") - 65] = np.float32(57.021), np.float32(15.9949)
+        want = hfx_gb300.mass_table(mono, add)
+        assert np.array_equal(x.mass_table().view(np.uint32), want.view(np.uint32))
+        assert x.option("missed-cleavages") == "1" and x.option("aa-mass-type") == ("Mono" if mono else "Average")
