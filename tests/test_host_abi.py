@@ -6,6 +6,7 @@ import re
 import subprocess
 
 import numpy as np
+import pytest
 
 from hfx_gb300 import synth
 
@@ -92,3 +93,47 @@ def test_no_cpu_fallback_without_library(tmp_path):
             pass
     finally:
         hfx_gb300._lib = hfx_gb300._lib_saved
+
+
+def test_headers_are_plain_c(tmp_path):
+    """Every public header compiles as C99, and a C program that links
+    libhfx_gpu.so calls the host-only readers and formatters (no GPU)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    inc = os.path.join(ROOT, "include")
+    for h in sorted(os.listdir(inc)):
+        if h.endswith(".h"):
+            r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only", "-x", "c",
+                                os.path.join(inc, h)], capture_output=True, text=True)
+            assert r.returncode == 0, r.stderr
+    src = tmp_path / "io_check.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include <string.h>
+#include "hfx_io.h"
+#include "hfx_report.h"
+int main(void) {
+    const char mgf[] = "BEGIN IONS\nTITLE=t\nCHARGE=2+\nPEPMASS=500.25\n100 1\n200 2\nEND IONS\n";
+    hfx_spectra *s = 0;
+    char err[128];
+    if (hfx_parse_spectra(mgf, (int64_t)strlen(mgf), 1, &s, err, sizeof err) != 0) return 1;
+    const float *mz, *it, *pcr, *z;
+    const int64_t *off;
+    hfx_spectra_arrays(s, &mz, &it, &off, &pcr, &z);
+    char num[64];
+    hfx_format_number((double)pcr[0], 0, num, sizeof num);
+    printf("%lld %lld %s %g\n", (long long)hfx_spectra_count(s), (long long)off[1], num, (double)mz[1]);
+    hfx_spectra_free(s);
+    return 0;
+}
+''')
+    lib_dir = os.path.join(ROOT, "hfx_gb300")
+    exe = tmp_path / "io_check"
+    r = subprocess.run([cc, "-std=c99", "-I", inc, str(src), "-L", lib_dir, "-lhfx_gpu", "-Wl,-rpath," + lib_dir,
+                        "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.split() == ["1", "2", "500.25", "200"], (r.stdout, r.stderr)
