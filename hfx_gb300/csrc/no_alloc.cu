@@ -13,7 +13,7 @@
 // The kernels are variants of the per-spectrum scorer and merge of search.cu
 // (same device routines, same canonical FP32 order), so the results equal
 // the regular per-spectrum path's bit for bit.
-#include <mutex>
+#include <algorithm>
 
 #include "hfx_internal.h"
 #include "device_common.cuh"
@@ -110,33 +110,38 @@ __global__ void k_merge_na(const uint8_t *__restrict__ scratch, int32_t nblocks,
     }
 }
 
-// Per-device set-up: the scratch array's device address (a host-side name of
-// a __device__ array is not a device address) and the kernels' shared-memory
-// limit.  Done once per device, with that device current.
-struct DeviceSetup {
-    bool ready = false;
-    uint8_t *scratch = nullptr;
-};
-std::mutex g_setup_mu;
-DeviceSetup g_setup[64];
+// Dynamic shared memory of one launch: the row, then the larger of the
+// warps' bit planes with their staging lists and the block's merge buffer.
+size_t smem_bytes(int32_t len, int32_t top_n) {
+    const size_t words = (size_t)(len + 31) / 32;
+    return (size_t)((len + 3) & ~3) * 4 +
+           std::max((size_t)kNaWarps * 3 * words * 4 + (size_t)kNaWarps * kListCap * 2,
+                    (size_t)kNaWarps * top_n * 16);
+}
 
-int32_t setup_device(int dev, uint8_t **scratch) {
-    if (dev < 0 || dev >= 64) return HFX_ERR_UNSUPPORTED;
-    std::lock_guard<std::mutex> lock(g_setup_mu);
-    DeviceSetup &s = g_setup[dev];
-    if (!s.ready) {
-        void *p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return HFX_ERR_CUDA;
-        const int smem_max = 200 * 1024;
-        if (cudaFuncSetAttribute(k_score_spectrum_na<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 smem_max) != cudaSuccess ||
-            cudaFuncSetAttribute(k_score_spectrum_na<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 smem_max) != cudaSuccess)
-            return HFX_ERR_CUDA;
-        s.scratch = static_cast<uint8_t *>(p);
-        s.ready = true;
-    }
-    *scratch = s.scratch;
+// Set-up, with the device current: the scratch array's device address (the
+// host-side name of a __device__ array is not a device address) and the
+// kernels' shared-memory limit, sized for the largest launch this entry
+// point makes.  It runs on every call: both are host calls that allocate
+// nothing, and redoing them keeps a call correct after a device reset or
+// under another context on the same device, where the module is loaded
+// anew.
+int32_t setup_device(uint8_t **scratch, int *smem_limit) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return HFX_ERR_CUDA;
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return HFX_ERR_CUDA;
+    int optin = 0;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+        return HFX_ERR_CUDA;
+    const int want = (int)std::min<size_t>(smem_bytes(kMaxWords * 32, kNaMaxK), (size_t)optin);
+    if (cudaFuncSetAttribute(k_score_spectrum_na<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, want) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k_score_spectrum_na<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, want) !=
+            cudaSuccess)
+        return HFX_ERR_CUDA;
+    *scratch = static_cast<uint8_t *>(p);
+    *smem_limit = want;
     return HFX_OK;
 }
 
@@ -158,10 +163,12 @@ extern "C" int32_t hfx_score_spectrum_noalloc(const uint8_t *ions, const float *
     if (len < 1 || len > kMaxWords * 32) return HFX_ERR_ARG;           // rows of at most 8192 bins
     if (charges < 0 || charges > 4) return HFX_ERR_ARG;
     if (end < begin || end > num_pep) return HFX_ERR_ARG;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return HFX_ERR_CUDA;
+    // an error left pending by the caller's own work is not taken for this
+    // call's: it stays pending and nothing is launched
+    if (cudaPeekAtLastError() != cudaSuccess) return HFX_ERR_CUDA;
     uint8_t *scratch = nullptr;
-    int32_t rc = setup_device(dev, &scratch);
+    int smem_limit = 0;
+    int32_t rc = setup_device(&scratch, &smem_limit);
     if (rc != HFX_OK) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     DevDB db;
@@ -175,9 +182,8 @@ extern "C" int32_t hfx_score_spectrum_noalloc(const uint8_t *ions, const float *
     const uint32_t ncand = end - begin;
     const int32_t nblocks = ncand == 0 ? 1 : (int32_t)min((ncand + 31u) / 32u, (uint32_t)kNaMaxBlocks);
     const int32_t words = (len + 31) / 32;
-    const size_t smem = (size_t)((len + 3) & ~3) * 4 +
-                        max((size_t)kNaWarps * 3 * words * 4 + (size_t)kNaWarps * kListCap * 2,
-                            (size_t)kNaWarps * top_n * 16);
+    const size_t smem = smem_bytes(len, top_n);
+    if (smem > (size_t)smem_limit) return HFX_ERR_UNSUPPORTED;  // a device with less shared memory
     if (fastdiv)
         k_score_spectrum_na<true><<<nblocks, kNaWarps * 32, smem, st>>>(db, row, len, charges, begin, end, words,
                                                                        top_n, scratch);

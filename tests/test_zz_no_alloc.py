@@ -86,6 +86,27 @@ def test_noalloc_matches_regular_path(gpulib):
             checked += 1
         assert checked >= 2
 
+        # the __fdividef variant, and a window of every candidate (more than
+        # HFX_NOALLOC_MAX_BLOCKS x 32, so each block strides over several
+        # chunks), both against the regular path on the same settings
+        s0 = int(np.nonzero(lens_h > 0)[0][0])
+        wide = sp.subset(np.array([s0, s0]))
+        wide.tol[:] = 20000.0  # a Da window covering the whole database
+        for fastdiv, spec in ((1, sp.subset(np.array([s0]))), (0, wide), (1, wide)):
+            ref = eng.search(spec, hfx_gb300.default_params(top_n=topn, batch_mode=0, fastdiv=fastdiv))
+            b, e = (int(wb_h[s0]), int(we_h[s0])) if len(spec) == 1 else (0, len(r))
+            assert int(ref.ncand[0]) == e - b
+            for _ in range(2):
+                rc = f(ions.data_ptr(), r_s.data_ptr(), tc_s.data_ptr(), tn_s.data_ptr(), idx_d.data_ptr(), len(r),
+                       mt_h.ctypes.data, rows[s0].data_ptr(), int(lens_h[s0]), _charges(sp.z[s0]), b, e, topn,
+                       fastdiv, stream.cuda_stream, out_s.data_ptr(), out_k.data_ptr(), out_p.data_ptr())
+                assert rc == 0
+                torch.cuda.synchronize()
+                assert np.array_equal(out_k.cpu().numpy().view(np.uint64), ref.key[0]), (fastdiv, e - b)
+                assert np.array_equal(out_s.cpu().numpy().view(np.uint32), ref.score[0].view(np.uint32))
+                assert np.array_equal(out_p.cpu().numpy().view(np.uint32), ref.pep[0])
+        assert len(r) > 304 * 32
+
         # sizes beyond the fixed scratch are rejected, nothing is launched
         rc = f(ions.data_ptr(), r_s.data_ptr(), tc_s.data_ptr(), tn_s.data_ptr(), idx_d.data_ptr(), len(r),
                mt_h.ctypes.data, rows[0].data_ptr(), int(lens_h[0]), 1, 0, 10, 33, 0, stream.cuda_stream,
