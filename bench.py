@@ -11,17 +11,22 @@ with pinned host buffers, copies included.  Between timed steps the L2 is
 flushed by writing a 512 MB buffer (outside the timed events).
 
 Beside the headline the line carries the plain FP32 path (one launch per
-spectrum) timed on the same spectra, the top-10 agreement of the headline
-search with it and with the FP64 oracle on a sample, and the oracle timed
-on the host cores (cpu_baseline).
+spectrum) timed on the same spectra and its top-10 agreement; `parity`: the
+timed search's top-10 keys, FP32 scores and candidate counts compared bit
+for bit with the oracle's FP32 search of every spectrum (the +-3 Da
+workloads; a sample of the open-window ones) and its agreement with the
+FP64 oracle; the oracle timed on the host cores (cpu_baseline); and the
+rooflines of the step and of each kernel.
 
 --impl reference times the reference's search restated on the CPU (the
 oracle port: the reference's Haskell host and CUDA kernels cannot run on
-this machine) on the same workload, with every host thread.
+this machine) on the same spectra, with every host thread, plus a one-thread
+figure on a sample.
 
 Multi-GPU: spectra are independent, so each rank searches its own batch
 (weak scaling, no collective on the data path); value = all ranks' pairs /
-max over ranks of the elapsed time.
+max over ranks of the elapsed time.  `--gpus N` without torchrun re-runs the
+command under torchrun.
 """
 from __future__ import annotations
 
@@ -43,10 +48,13 @@ METRIC = "peptide-spectrum XCorrs/s"
 UNIT = "PSM/s"
 KERNELS = {0: "k_score_spectrum", 1: "k_score_lists", 2: "k_score_batched"}
 
-# DRAM bytes (read + write) per launch of the scorer, from one ncu capture
-# of the default workload (profiles/k_score_lists_full_bf16.md), keyed by
-# (kernel, workload, precision, spectra).
-TRAFFIC = {("k_score_lists", "full", 1, 10000): 2.699e9 + 13.1e6}
+# DRAM bytes (read + write) per launch, from one-pass ncu captures of the
+# default workload (summaries under profiles/), keyed by (kernel, workload,
+# precision, spectra).  Each figure carries the hash of the kernel's source
+# files at capture time; when the source has changed since, the figure is
+# not reported (traffic null, marked stale).
+KERNEL_SRC = ["hfx_gb300/csrc/lists.cu", "hfx_gb300/csrc/device_common.cuh", "hfx_gb300/csrc/batched_common.cuh"]
+TRAFFIC = {}
 
 
 def _args():
@@ -73,9 +81,38 @@ def _args():
     ap.add_argument("--group-size", type=int, default=0, help="spectra per batched work item (0 = default)")
     ap.add_argument("--chunk", type=int, default=0, help="candidates per batched work item (0 = default)")
     ap.add_argument("--no-graph", action="store_true", help="eager launches instead of CUDA-graph replays")
+    ap.add_argument("--shard", action="store_true",
+                    help="N > 1: split ONE batch across the ranks by candidate counts (strong scaling) instead of "
+                         "one batch per rank (weak scaling)")
     ap.add_argument("--tune", default="auto", choices=["auto", "on", "off"],
                     help="hfx_autotune of group size and work-item size before the warm-up (auto: 'full' only)")
     return ap.parse_args()
+
+
+def _src_hash(files=KERNEL_SRC):
+    import hashlib
+    h = hashlib.sha1()
+    for f in files:
+        with open(os.path.join(ROOT, f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:12]
+
+
+def _traffic(kern, workload, prec, ns):
+    """(bytes per launch, note) of a captured kernel, None when absent or stale."""
+    t = TRAFFIC.get((kern, workload, prec, ns))
+    if t is None:
+        return None, "no capture for this kernel and workload"
+    if t["src"] != _src_hash():
+        return None, "stale: kernel source changed since the capture"
+    return t["bytes"], t["profile"]
+
+
+def _relaunch(a):
+    """--gpus N > 1 without a launcher: re-run this command under torchrun."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={a.gpus}",
+           "--master-addr", "127.0.0.1", "--master-port", os.environ.get("MASTER_PORT", "29517")] + sys.argv
+    os.execvp(cmd[0], cmd)
 
 
 def _dist():
@@ -95,10 +132,12 @@ DESCRIBE = {
 
 
 def _samples(a):
-    """Workload-dependent default sample sizes of the CPU-side arms."""
+    """Workload-dependent default sample sizes of the CPU-side arms: every
+    spectrum of the +-3 Da workloads (the oracle searches 10,000 of them in
+    seconds on the host cores), samples of the open-window ones."""
     full = a.workload in ("full", "tiny")
-    cpu = a.cpu_sample if a.cpu_sample >= 0 else (10000 if full else 300)
-    agree = a.agree_sample if a.agree_sample >= 0 else (1000 if full else 200)
+    cpu = a.cpu_sample if a.cpu_sample >= 0 else (1 << 30 if full else 300)
+    agree = a.agree_sample if a.agree_sample >= 0 else (1 << 30 if full else 200)
     plain = a.plain_sample if a.plain_sample >= 0 else (1 << 30 if full else 2000)
     return cpu, agree, plain
 
@@ -226,50 +265,81 @@ def _oracle_inputs(prot, cfg):
 
 
 def run_reference(a, rank, world):
-    """CPU arm: the oracle port of the reference search, all host threads."""
+    """CPU arm: the oracle port of the reference search on the same spectra as
+    the GPU arm, all host threads; rank 0 only.  Beside it, the same search on
+    one thread over a bounded sample."""
     if rank != 0:
         return
     prot, sp, cfg = _workload(a.workload, a.spectra, 0)
     O, db, mods = _oracle_inputs(prot, cfg)
     cpu_n, _, _ = _samples(a)
-    sample = sp.subset(np.arange(min(len(sp), max(50, cpu_n // 4))))
+    sample = sp if cpu_n >= len(sp) else sp.subset(np.arange(cpu_n))
     threads = os.cpu_count() or 1
-    for _ in range(max(1, min(a.warmup, 1))):
-        O.search(*db, sample.subset(np.arange(min(20, len(sample)))), topn=cfg["top_n"], nthreads=threads, **_okw(cfg), **mods)
+    kw = dict(topn=cfg["top_n"], **_okw(cfg), **mods)
+    warm = sample.subset(np.arange(min(50, len(sample))))
+    for _ in range(max(1, a.warmup)):
+        O.search(*db, warm, nthreads=threads, **kw)
     t0 = time.perf_counter()
     psm = 0
     for _ in range(a.steps):
-        res = O.search(*db, sample, topn=cfg["top_n"], nthreads=threads, **_okw(cfg), **mods)
+        res = O.search(*db, sample, nthreads=threads, **kw)
         psm += int(res[4].sum())
     dt = time.perf_counter() - t0
     v = psm / dt
+    # one thread, a bounded sample (about a second of work)
+    one = sample.subset(np.arange(min(len(sample), 200)))
+    t1 = time.perf_counter()
+    r1 = O.search(*db, one, nthreads=1, **kw)
+    dt1 = time.perf_counter() - t1
+    whole = len(sample) == len(sp)
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": 1000 * dt / a.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": a.workload + f" ({len(sample)} of {len(sp)} spectra per step)"},
+            "config": {"workload": f"{a.workload}: " + DESCRIBE.get(a.workload, "{n} spectra").format(n=len(sp))
+                       + ("" if whole else f" ({len(sample)} of {len(sp)} spectra per step)"),
+                       "psm_per_step": psm // a.steps},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{len(sample)} spectra of the {a.workload} workload per step"},
+                             "sample": (f"all {len(sp)} spectra" if whole else f"{len(sample)} of {len(sp)} spectra")
+                             + f" of the {a.workload} workload per step"},
+            "cpu_1thread": {"value": float(r1[4].sum()) / dt1, "unit": UNIT, "cores": 1, "kind": "port",
+                            "sample": f"first {len(one)} spectra, {int(r1[4].sum())} pairs, {dt1:.2f} s"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
 def _cpu_baseline(a, O, db, mods, sp, cfg):
-    sample = sp.subset(np.arange(min(len(sp), a.cpu_sample)))
+    """The oracle (ref32, the reference's FP32 operation order) timed on the
+    host cores; returns the baseline figure and the oracle's result."""
+    n = min(len(sp), a.cpu_sample)
+    sample = sp if n == len(sp) else sp.subset(np.arange(n))
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
     res = O.search(*db, sample, topn=cfg["top_n"], nthreads=threads, **_okw(cfg), **mods)
     dt = time.perf_counter() - t0
     return {"value": float(res[4].sum()) / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"first {len(sample)} of {len(sp)} spectra, {int(res[4].sum())} pairs, {dt:.1f} s"}
+            "sample": f"first {len(sample)} of {len(sp)} spectra, {int(res[4].sum())} pairs, {dt:.1f} s"}, res
+
+
+def _parity(res32, key, score, ncand):
+    """Bitwise comparison of the GPU result with the oracle's FP32 result on
+    the spectra the oracle searched: per spectrum, the top-N keys (candidate
+    set and order), the FP32 scores and the candidate counts."""
+    s32, k32, n32 = res32[0], res32[2], res32[4]
+    n = len(k32)
+    keys = np.all(k32 == key[:n], axis=1)
+    scores = np.all(s32.view(np.uint32) == score[:n].view(np.uint32), axis=1)
+    counts = n32.astype(np.int64) == ncand[:n].astype(np.int64)
+    return {"spectra": int(n), "keys_bitexact": float(keys.mean()), "scores_bitexact": float(scores.mean()),
+            "candidate_counts_equal": float(counts.mean())}
 
 
 def _agreement(a, O, db, mods, sp, cfg, key, score):
-    """Top-10 agreement of the GPU result with the FP64 oracle on a sample:
-    the fraction of spectra whose top-N candidates (keys, in order) match,
-    and the largest relative XCorr difference of the matched entries."""
+    """Top-N agreement of the GPU result with the FP64 oracle: the fraction
+    of spectra whose top-N candidates (keys, in order) match, and the
+    largest relative XCorr difference of the matched entries."""
     n = min(len(sp), a.agree_sample)
-    sample = sp.subset(np.arange(n))
+    sample = sp if n == len(sp) else sp.subset(np.arange(n))
     threads = os.cpu_count() or 1
     _, s64, k64, _, _ = O.search(*db, sample, topn=cfg["top_n"], prec=3, nthreads=threads, **_okw(cfg), **mods)
     same_order = np.all(k64 == key[:n], axis=1)
@@ -300,6 +370,10 @@ def _timed(eng, dev, p, out, steps, flush, stream):
 def main():
     a = _args()
     rank, world, local = _dist()
+    if a.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return _relaunch(a)
+    if world != a.gpus:
+        print(f"bench: --gpus {a.gpus} but WORLD_SIZE {world}; using {world}", file=sys.stderr)
     if a.impl == "reference":
         return run_reference(a, rank, world)
     import torch
@@ -308,7 +382,8 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    prot, sp, cfg = _workload(a.workload, a.spectra, rank)
+    strong = a.shard and world > 1
+    prot, sp, cfg = _workload(a.workload, a.spectra, 0 if strong else rank)
     from hfx_gb300 import synth
     eng = hfx_gb300.Engine(local)
     eng.build_db(prot.seq, prot.seg, static_add=synth.static_mods(), **synth.DIGEST)
@@ -318,6 +393,18 @@ def main():
     stream = torch.cuda.current_stream()
     eng.set_stream(stream.cuda_stream)
     prec, mode = a.precision, a.batch_mode
+    shard_range = None
+    if strong:
+        # this rank's run of the batch, balanced by the windows' candidate counts
+        from hfx_gb300 import shard
+        d0 = torch.device("cuda", local)
+        dv = {k: torch.from_numpy(v).to(d0) for k, v in zip(("mz", "it", "off", "pcr", "z", "tol"), sp.arrays())}
+        b0 = torch.empty(len(sp), dtype=torch.int32, device=d0)
+        e0 = torch.empty(len(sp), dtype=torch.int32, device=d0)
+        eng.find_windows(dv, hfx_gb300.default_params(top_n=cfg["top_n"], **_pkw(cfg)), b0, e0)
+        nc = np.maximum((e0 - b0).cpu().numpy().astype(np.int64), 0)
+        shard_range = shard.partition(nc, world)[rank]
+        sp = sp.subset(np.arange(*shard_range))
     cpu_n, agree_n, plain_n = _samples(a)
     a.cpu_sample, a.agree_sample = cpu_n, agree_n
     graph = int(mode != 0 and not a.no_graph)
@@ -359,12 +446,20 @@ def main():
     total_ms = _timed(eng, dev, p, out, a.steps, flush, stream)
     torch.cuda.synchronize()
     clocks = clk.stop()
+    # the timed searches' own result (the stage-event pass below overwrites `out`)
+    key = out["key"].cpu().numpy().view(np.uint64)
+    score = out["score"].cpu().numpy()
+    ncand = out["ncand"].cpu().numpy()
+    psm_all = psm_step
     if world > 1:
         t = torch.tensor([total_ms], device=d)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
+        c = torch.tensor([psm_step], dtype=torch.int64, device=d)
+        torch.distributed.all_reduce(c, op=torch.distributed.ReduceOp.SUM)
+        psm_all = int(c.item())
     ms_step = total_ms / a.steps
-    value = psm_step * world / (ms_step / 1000.0)
+    value = psm_all / (ms_step / 1000.0)
     # per-stage device times and work counters: the same steps again, with stage events
     eng.set_profiling(True)
     eng.stage_stats(reset=True)
@@ -373,8 +468,7 @@ def main():
     stats = eng.stage_stats(reset=True)
     work = {k: v // a.steps for k, v in eng.counters(reset=True).items()}
     eng.set_profiling(False)
-    key = out["key"].cpu().numpy().view(np.uint64)
-    score = out["score"].cpu().numpy()
+    eager_same = bool(np.array_equal(out["key"].cpu().numpy().view(np.uint64), key))
     # e2e through the host-buffer C ABI (pinned buffers, copies in the timed region)
     pin = {k: torch.from_numpy(v).pin_memory() for k, v in
            dict(mz=sp.mz, it=sp.it, off=sp.off, pcr=sp.pcr, z=sp.z, tol=sp.tol).items()}
@@ -384,8 +478,10 @@ def main():
             return tuple(pin[k].numpy() for k in ("mz", "it", "off", "pcr", "z", "tol"))
     h2d = sum(int(v.numel() * v.element_size()) for v in pin.values())
     d2h = ns * tn_ * (4 + 8 + 4) + ns * 8
-    eng.search(Pinned(), p)
+    r_e2e = eng.search(Pinned(), p)
     torch.cuda.synchronize()
+    e2e_same = bool(np.array_equal(r_e2e.key, key) and np.array_equal(r_e2e.score.view(np.uint32),
+                                                                       score.view(np.uint32)))
     e2e_tot = 0.0
     for _ in range(a.e2e_steps):
         flush.zero_()
@@ -393,7 +489,7 @@ def main():
         t1 = time.perf_counter()
         eng.search(Pinned(), p)
         e2e_tot += time.perf_counter() - t1
-    e2e_value = psm_step * world / (e2e_tot / a.e2e_steps)
+    e2e_value = psm_all / (e2e_tot / a.e2e_steps)
     # the plain FP32 path (one launch per spectrum) on the same spectra
     plain = None
     if not a.no_plain and not has_mods:
@@ -426,7 +522,6 @@ def main():
     kern = "k_score_mods" if stage == "mods" else KERNELS[mode if mode in KERNELS else 1]
     if has_mods and mode == 0:
         kern = "k_score_mods" if stage == "mods" else "k_score_batched"
-    sc_ms, sc_launch, _ = stats[stage]
     rng = np.random.Generator(np.random.PCG64(7))
     r, tc, tn, idx, mt = eng.db_export()
     bsz = 2 if prec else 4
@@ -457,26 +552,59 @@ def main():
         meanL = float(np.mean((tn[idx] - tc[idx])[pos]))
         bpp = meanU * bsz + meanL + 16
         u_basis = "list entries streamed per candidate (run counters)"
-    # pairs scored by the dominant kernel per launch (all of the step's pairs
-    # go through it, or its modified share when it is the modification scorer)
+    # pairs scored by the modification scorer or the plain scorer
     psm_kernel = psm_step
     if stage == "mods":
         psm_kernel = psm_step - int(np.sum(np.where(lens > 0, we - wb, 0)))
     elif has_mods:
         psm_kernel = int(np.sum(np.where(lens > 0, we - wb, 0)))
-    per_launch_ms = sc_ms / max(1, sc_launch)
-    per_launch_psm = psm_kernel * a.steps / max(1, sc_launch)
-    achieved = bpp * per_launch_psm / (per_launch_ms / 1000.0) / 1e9
     peak, peak_kind = _peaks()
-    traffic = TRAFFIC.get((kern, a.workload, prec, ns))
     launches_per_step = sum(v[1] for v in stats.values()) / a.steps
+    # Per-kernel rooflines.  "moved" bytes are what each kernel reads and
+    # writes by design, from the run's own work counters: the generator
+    # reads each needed peptide's residues and metadata and writes its lists;
+    # the list scorer streams list entries, list metadata and the spectrum
+    # tiles it stages.  The per-pair figure U*s + L + 16 of the search as a
+    # whole is reported for the step (`step`), where the benchmark spec's target is
+    # defined.
+    es = 4 if long_rows else 2
+    kern_rows = {}
+    stage_of = {"lists": "k_gen_lists" + ("_long" if long_rows else ""), "score": kern, "mods": "k_score_mods"}
+    step_ms_all = sum(v[0] for v in stats.values()) / a.steps
+    for st, kname in stage_of.items():
+        ms_st, nl_st, _ = stats.get(st, (0.0, 0, 0))
+        if not nl_st or ms_st <= 0:
+            continue
+        ms_st /= a.steps
+        if st == "lists":
+            moved = work["list_entries"] * es + work["residues_read"] + 16 * work["lists"]
+            basis = "list entries written + residues read + 16 B per list"
+        elif st == "score" and mode == 1:
+            moved = work["entries_streamed"] * es + work["tile_bytes"] + 8 * work["candidates"]
+            basis = "list entries streamed + spectrum tiles staged + 8 B per candidate"
+        else:
+            moved = bpp * (psm_kernel if st == stage else psm_step)
+            basis = "U*s + L + 16 per pair (ions rebuilt from residues per pair)"
+        tr, tr_note = _traffic(kname, a.workload, prec, ns)
+        ach = moved / (ms_st / 1000.0) / 1e9
+        kern_rows[kname] = {"stage_ms_per_step": ms_st, "share": ms_st / max(1e-9, step_ms_all),
+                            "moved_bytes": moved, "bytes_basis": basis, "achieved": ach, "frac": ach / peak,
+                            "traffic": tr, "traffic_note": tr_note}
+    dom = max(kern_rows, key=lambda k: kern_rows[k]["stage_ms_per_step"]) if kern_rows else kern
+    drow = kern_rows.get(dom, {})
+    step_ach = bpp * psm_step / (ms_step / 1000.0) / 1e9
+    psm_ach = None
+    if dom in (kern,):
+        psm_ach = bpp * psm_kernel / (drow.get("stage_ms_per_step", ms_step) / 1000.0) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
-        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic",
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "strong" if strong else "weak",
+        "vs_baseline": None,
+        "dtype": ["f32", "bf16", "f16"][prec], "data": "synthetic",
         "config": {"workload": f"{a.workload}: " + DESCRIBE.get(a.workload, "{n} spectra").format(n=ns),
                    "psm_per_step": psm_step,
-                   "precision": ["fp32", "bf16 store + fp32 rescore", "fp16 store + fp32 rescore"][prec]
+                   "precision": ["fp32", "bf16 store, fp32 accumulate, fp32 rescore",
+                                 "fp16 store, fp32 accumulate, fp32 rescore"][prec]
                    + (f" of the top {rk}" if prec else ""),
                    "batch_mode": ["per-spectrum launches", "batched over ion lists", "batched fused"][mode],
                    "launch": "one CUDA-graph replay per step" if graph else "eager launches",
@@ -484,20 +612,37 @@ def main():
                    "l2": "flushed between timed steps (512 MB write)",
                    "stage_ms_per_step": {k: v[0] / a.steps for k, v in stats.items() if v[1]},
                    "work_per_step": work},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "result_equals_device_run": e2e_same},
         "gpu_launches": int(launches_per_step * a.steps),
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "kernel": kern,
-                     "bytes_per_psm": bpp, "mean_distinct_bins": meanU, "u_basis": u_basis, "peak_kind": peak_kind,
-                     "step_achieved": bpp * psm_step / (ms_step / 1000.0) / 1e9},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": drow.get("achieved"), "peak": peak, "unit": "GB/s",
+                     "frac": drow.get("frac"), "traffic": drow.get("traffic"),
+                     "traffic_note": drow.get("traffic_note"), "bytes_basis": drow.get("bytes_basis"),
+                     "peak_kind": peak_kind,
+                     "binding": "SM instruction issue and shared-memory wavefronts, not DRAM "
+                                "(ncu summaries under profiles/)",
+                     "kernels": kern_rows,
+                     "step": {"achieved": step_ach, "frac": step_ach / peak, "bytes_per_psm": bpp,
+                              "mean_distinct_bins": meanU, "u_basis": u_basis,
+                              "basis": "U*s + L + 16 bytes per pair x pairs per step / ms_per_step"},
+                     "psm_basis_achieved": psm_ach},
         "clocks": clocks,
+        "graph_equals_eager": eager_same,
     }
+    if strong:
+        line["config"]["shard"] = f"one batch split by candidate counts; rank 0 spectra {shard_range}"
     if plain is not None:
         line["plain_fp32"] = plain
     if rank == 0 and not a.no_cpu:
         O, db, mods = _oracle_inputs(prot, cfg)
+        line["cpu_baseline"], res32 = _cpu_baseline(a, O, db, mods, sp, cfg)
+        # rescored FP32 scores and keys against the oracle's FP32 search
+        if prec == 0 or rk >= cfg["top_n"]:
+            line["parity"] = _parity(res32, key, score, ncand)
         line["fp64_agreement"] = _agreement(a, O, db, mods, sp, cfg, key, score)
-        line["cpu_baseline"] = _cpu_baseline(a, O, db, mods, sp, cfg)
+        if "parity" in line:
+            line["parity"].update({"fp64_top_order": line["fp64_agreement"]["top_order"],
+                                   "fp64_max_rel_err": line["fp64_agreement"]["max_rel_err"]})
     if rank == 0:
         s = json.dumps(line)
         print(s, flush=True)

@@ -32,7 +32,7 @@ EXPORTED = [
     "hfx_set_protein_segments", "hfx_match_ions", "hfx_mass_table",
     "hfx_set_mods", "hfx_mod_table", "hfx_search_host", "hfx_search_device", "hfx_search_evalues",
     "hfx_preprocess", "hfx_find_windows", "hfx_ion_bins", "hfx_mod_isoforms", "hfx_digest", "hfx_pack_ions",
-    "hfx_set_profiling", "hfx_stage_stats", "hfx_search_counters",
+    "hfx_set_profiling", "hfx_stage_stats", "hfx_search_counters", "hfx_set_workspace_limit",
 ]
 STAGES = ["layout", "preprocess", "windows", "score", "topn", "rescore", "mods", "lists", "pack"]
 
@@ -110,6 +110,7 @@ def load_library(path: str = LIB_PATH):
         "hfx_set_profiling": (i32, [P, i32]),
         "hfx_stage_stats": (i32, [P, P, P, P, i32]),
         "hfx_search_counters": (i32, [P, P, i32]),
+        "hfx_set_workspace_limit": (i32, [P, u64, C.POINTER(u64)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -187,6 +188,25 @@ class SearchResult:
     ncand: np.ndarray   # [nspec]
 
 
+class SearchCancelled(RuntimeError):
+    """Raised by Engine.search_batches when cancelled between batches;
+    `partial` holds the rows of the spectra searched before, `done` their
+    count."""
+
+    def __init__(self, partial: "SearchResult", done: int):
+        super().__init__(f"search cancelled after {done} spectra")
+        self.partial = partial
+        self.done = done
+
+
+def _concat(parts, params) -> "SearchResult":
+    tn = (params or default_params()).top_n
+    if not parts:
+        return SearchResult(np.zeros((0, tn), np.float32), np.zeros((0, tn), np.uint64),
+                            np.zeros((0, tn), np.uint32), np.zeros(0, np.int64))
+    return SearchResult(*(np.concatenate([getattr(r, f) for r in parts]) for f in ("score", "key", "pep", "ncand")))
+
+
 class Engine:
     """One CUDA context with a search database (Fragment.hs DeviceSeqDB)."""
 
@@ -229,8 +249,37 @@ class Engine:
         """Work counters of the batched list path (see hfx_search_counters)."""
         c = np.zeros(8, np.uint64)
         self._check(self.lib.hfx_search_counters(self.h, _ptr(c), int(reset)))
-        names = ["lists", "list_entries", "candidates", "entries_streamed", "pairs", "positions_claimed"]
+        names = ["lists", "list_entries", "candidates", "entries_streamed", "pairs", "positions_claimed",
+                 "residues_read", "tile_bytes"]
         return {n: int(c[i]) for i, n in enumerate(names)}
+
+    def set_workspace_limit(self, nbytes: int) -> int:
+        """hfx_set_workspace_limit: cap the context's workspace bytes (0 = no
+        cap); returns the bytes held now.  A search that would need more
+        raises HfxError with code HFX_ERR_OOM."""
+        used = C.c_uint64()
+        self._check(self.lib.hfx_set_workspace_limit(self.h, int(nbytes), C.byref(used)))
+        return used.value
+
+    def search_batches(self, spectra, params: SearchParams | None = None, batch: int = 4096, cancel=None,
+                       on_batch=None) -> SearchResult:
+        """Search `spectra` in batches of `batch` spectra (one hfx_search_host
+        call each, as the reference searches its scans in groups,
+        Main.hs:122-151).  `cancel` (a threading.Event or anything with
+        is_set()) is checked between batches: once set, no further batch is
+        started and SearchCancelled is raised carrying the rows of the batches
+        already searched.  on_batch(i, lo, hi) runs after batch i."""
+        import numpy as np
+        n = len(spectra)
+        parts = []
+        for i, lo in enumerate(range(0, n, batch)):
+            if cancel is not None and cancel.is_set():
+                raise SearchCancelled(_concat(parts, params), lo)
+            hi = min(n, lo + batch)
+            parts.append(self.search(spectra.subset(np.arange(lo, hi)), params))
+            if on_batch is not None:
+                on_batch(i, lo, hi)
+        return _concat(parts, params)
 
     def set_stream(self, stream_ptr: int):
         self._check(self.lib.hfx_set_stream(self.h, stream_ptr))

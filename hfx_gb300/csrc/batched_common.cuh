@@ -127,6 +127,9 @@ struct CtaSlots {
     Key *qk;
     uint32_t qn;     // slot lanes: entries queued for the lane's slot
     uint32_t *err;
+    // lock hold test (the word after the error word; 0 = off): member 0's
+    // lock starts held and a merge gives up after this many attempts
+    uint32_t test_hold;
 
     __host__ __device__ static constexpr size_t warp_bytes() { return cta_queue_bytes(G, (int)sizeof(Key)); }
     static_assert(Q == cta_queue_len(G), "queue length and cta_queue_bytes disagree");
@@ -141,6 +144,7 @@ struct CtaSlots {
         qk = reinterpret_cast<Key *>(queue + (size_t)G * kQ * 4);
         qn = 0u;
         err = err_;
+        test_hold = err_[1] & 0xFFu;
     }
     // Item start, by threads [0, L G) of the CTA (a barrier must follow).
     __device__ __forceinline__ void reset_shared() {
@@ -149,7 +153,7 @@ struct CtaSlots {
             lk[t] = kNone;
         }
         if (threadIdx.x < G) {
-            lock[threadIdx.x] = 0u;
+            lock[threadIdx.x] = (test_hold != 0u && threadIdx.x == 0) ? 2u : 0u;
             thr[threadIdx.x] = 0u;
         }
     }
@@ -189,7 +193,8 @@ struct CtaSlots {
         const Key rk = __shfl_sync(kFullMask, nk, 31 - lane);
         uint32_t got = 0u;
         if (lane == 0) {
-            for (uint32_t i = 0; i < kLockLimit; ++i)
+            const uint32_t limit = test_hold != 0u ? test_hold : kLockLimit;
+            for (uint32_t i = 0; i < limit; ++i)
                 if (atomicCAS(lock + j, 0u, 1u) == 0u) {
                     got = 1u;
                     break;

@@ -15,6 +15,8 @@
 #include "ions.h"
 #include "../../include/hfx_gpu.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -73,6 +75,11 @@ struct DBuf {
 
 }  // namespace
 
+namespace {
+const char *const kStageNames[HFX_NSTAGES] = {"layout", "preprocess", "windows", "score", "topn",
+                                              "rescore", "mods", "lists", "pack"};
+}  // namespace
+
 struct hfx_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -110,7 +117,11 @@ struct hfx_ctx {
     int64_t stage_launches[HFX_NSTAGES] = {0};
     int64_t stage_units[HFX_NSTAGES] = {0};
 
+    // NVTX ranges, one per stage, for timeline tools (no-ops without one)
+    int nvtx_depth = 0;
     void stage_begin(int s) {
+        nvtxRangePushA(kStageNames[s]);
+        ++nvtx_depth;
         if (!profile || gmode == 2) return;
         if (!ev[s][0]) { cudaEventCreate(&ev[s][0]); cudaEventCreate(&ev[s][1]); }
         cudaEventRecord(ev[s][0], stream);
@@ -143,19 +154,24 @@ struct hfx_ctx {
     bool debug_sync = false;
     std::string fault_stage;
     std::string err_stage;  // with debug_sync: the first stage after which the device error word was set
+    void nvtx_close() {
+        for (; nvtx_depth > 0; --nvtx_depth) nvtxRangePop();
+    }
     void stage_end(int s, int64_t launches, int64_t units = 0) {
+        if (nvtx_depth > 0) {
+            nvtxRangePop();
+            --nvtx_depth;
+        }
         if (gmode == 2) return;
         stage_launches[s] += launches;
         stage_units[s] += units;
         if (debug_sync && fault_stage.empty()) {
-            static const char *names[HFX_NSTAGES] = {"layout", "preprocess", "windows", "score", "topn",
-                                                     "rescore", "mods", "lists", "pack"};
             const cudaError_t e = cudaStreamSynchronize(stream);
-            if (e != cudaSuccess) fault_stage = names[s];
+            if (e != cudaSuccess) fault_stage = kStageNames[s];
             uint32_t w = 0;
             if (e == cudaSuccess && err_stage.empty() && d_err.p &&
                 cudaMemcpy(&w, d_err.p, 4, cudaMemcpyDeviceToHost) == cudaSuccess && w)
-                err_stage = std::string(names[s]) + " (word " + std::to_string(w) + ")";
+                err_stage = std::string(kStageNames[s]) + " (word " + std::to_string(w) + ")";
         }
         if (!profile) return;
         cudaEventRecord(ev[s][1], stream);
@@ -172,9 +188,23 @@ struct hfx_ctx {
         }
     }
 
+    // Workspace byte cap (hfx_set_workspace_limit; 0 = none): a workspace
+    // that would take the context's total beyond it is not allocated and the
+    // call reports HFX_ERR_OOM, as when cudaMalloc itself fails.
+    size_t ws_limit = 0;
+    size_t ws_total() const {
+        size_t t = 0;
+        for (const auto &kv : ws) t += kv.second.n;
+        return t;
+    }
     template <typename T> T *buf(const char *name, size_t count, cudaError_t &e) {
         DBuf &b = ws[name];
-        e = b.ensure(count * sizeof(T) + 16);
+        const size_t want = count * sizeof(T) + 16;
+        if (ws_limit && want > b.n && ws_total() - b.n + std::max<size_t>(want, 256) > ws_limit) {
+            e = cudaErrorMemoryAllocation;
+            return nullptr;
+        }
+        e = b.ensure(want);
         return b.as<T>();
     }
     DevDB devdb() const {
@@ -709,12 +739,35 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     return HFX_OK;
 }
 
+// Failure-detection test: HFX_TEST_HOLD_LOCK=n (1..255) makes every scorer
+// CTA start with member 0's admission lock held by nobody and give up on it
+// after n attempts, so the bounded wait runs out, the CTA records a timeout
+// in the error word and goes on, and the search returns HFX_ERR_TIMEOUT.
+// Read at each search (eager searches; a captured graph keeps the value of
+// its capture).  Off (0) by default.
+int test_lock_attempts() {
+    const char *v = std::getenv("HFX_TEST_HOLD_LOCK");
+    if (!v || !*v) return 0;
+    const int n = std::atoi(v);
+    return n < 0 ? 0 : (n > 255 ? 255 : n);
+}
+
+// Clears the device error word and sets the word after it, which the
+// scorers read as the lock hold test (0 = off).
+cudaError_t clear_err(hfx_ctx *ctx) {
+    cudaError_t e = cudaMemsetAsync(ctx->d_err.p, 0, 4, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(static_cast<uint8_t *>(ctx->d_err.p) + 4, test_lock_attempts(), 4, ctx->stream);
+    return e;
+}
+
 // Everything a search enqueues, from clearing the error word to the last
 // kernel; in gmode 2 this is what the CUDA graph captures.
 int32_t search_enqueue(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, float *out_s, uint64_t *out_k,
                        uint32_t *out_pep, int64_t *out_ncand) {
     int32_t rc = 0;
-    HFX_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, 4, ctx->stream), "memset err");
+    ctx->nvtx_close();
+    HFX_CUDA(clear_err(ctx), "memset err");
     int64_t stride = 0;
     SpecMeta *meta = nullptr;
     float *rows = nullptr;
@@ -925,6 +978,13 @@ const char *hfx_last_error(const hfx_ctx *ctx) { return ctx ? ctx->err.c_str() :
 int32_t hfx_set_profiling(hfx_ctx *ctx, int32_t on) {
     if (!ctx) return HFX_ERR_ARG;
     ctx->profile = on != 0;
+    return HFX_OK;
+}
+
+int32_t hfx_set_workspace_limit(hfx_ctx *ctx, uint64_t bytes, uint64_t *in_use) {
+    if (!ctx) return HFX_ERR_ARG;
+    ctx->ws_limit = (size_t)bytes;
+    if (in_use) *in_use = ctx->ws_total();
     return HFX_OK;
 }
 
@@ -1163,7 +1223,7 @@ int32_t hfx_search_evalues(hfx_ctx *ctx, const hfx_search_params *p, const float
     // isoforms per spectrum, counted by the search's modification scorer
     unsigned long long *niso = mods_on ? ctx->buf<unsigned long long>("m_ncand", ns, e) : nullptr;
     if (e) return cuda_fail(ctx, e, "alloc");
-    HFX_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, 4, ctx->stream), "memset err");
+    HFX_CUDA(clear_err(ctx), "memset err");
     rc = hfx_evalue_offsets(wb, we, plain_on ? 1 : 0, niso, ns, size, soff, send, cursor, ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "E-value offsets");
     uint64_t total = 0;
@@ -1270,7 +1330,7 @@ int32_t hfx_match_ions(hfx_ctx *ctx, const hfx_search_params *p, const float *z,
     const float *rows = ctx->buf<float>("rows32", (size_t)nspec * ctx->rows_stride, e);
     if (e) return cuda_fail(ctx, e, "alloc");
     HFX_CUDA(ctx->d_err.ensure(16), "alloc err");
-    HFX_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, 4, ctx->stream), "memset err");
+    HFX_CUDA(clear_err(ctx), "memset err");
     // the spectrum bin width (IonSeries.hs:139 binWidth cp)
     const int rc = hfx_match_ions_launch(ctx->devdb(), ctx->devmods(), ctx->num_ions, meta, rows, ctx->rows_stride,
                                          z, p->bin_width, keys, nspec, top_n, out_matched, out_total,
@@ -1360,6 +1420,54 @@ int32_t hfx_match_peptide(hfx_ctx *ctx, uint64_t key, uint32_t pep, char *text, 
     return HFX_OK;
 }
 
+namespace {
+
+// The persisted choices of hfx_autotune: a text file of lines
+// "<batch shape key>\t<group size>\t<chunk>\t<ms>", named by the
+// HFX_AUTOTUNE_FILE environment variable.  The key holds what the choice
+// depends on: the device, the database and batch sizes and the search
+// settings that select the kernels.
+std::string autotune_key(const hfx_ctx *ctx, const hfx_search_params *p, int32_t nspec, int64_t npeaks) {
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, ctx->device) != cudaSuccess) return std::string();
+    char buf[512];
+    std::snprintf(buf, sizeof buf,
+                  "%s/sm%d%d/%d SMs|pep %llu|spectra %d|peaks %lld|prec %d|mode %d|mods %d|bw %.7g/%d/%d|"
+                  "tol %d|top %d|rescore %d|fastdiv %d|maxlen %d",
+                  prop.name, prop.major, prop.minor, prop.multiProcessorCount, (unsigned long long)ctx->num_pep,
+                  nspec, (long long)npeaks, p->precision, p->batch_mode,
+                  (p->search_mods != 0 && ctx->num_mod > 0) ? ctx->num_mod : 0, (double)p->bin_width,
+                  p->custom_bin_width, p->ion_bins_custom, p->tol_ppm, p->top_n, p->rescore_k, p->fastdiv,
+                  p->max_len);
+    std::string k(buf);
+    for (char &c : k)
+        if (c == '\t' || c == '\n') c = ' ';
+    return k;
+}
+
+bool autotune_lookup(const char *path, const std::string &key, int32_t *g, int32_t *c, float *ms) {
+    FILE *f = std::fopen(path, "r");
+    if (!f) return false;
+    char line[1024];
+    bool found = false;
+    while (std::fgets(line, sizeof line, f)) {
+        char *t1 = std::strchr(line, '\t');
+        if (!t1 || (size_t)(t1 - line) != key.size() || std::strncmp(line, key.c_str(), key.size()) != 0) continue;
+        int gg = 0, cc = 0;
+        float mm = 0.0f;
+        if (std::sscanf(t1 + 1, "%d\t%d\t%f", &gg, &cc, &mm) == 3 && gg > 0 && cc > 0) {
+            *g = gg;  // the last matching line wins
+            *c = cc;
+            *ms = mm;
+            found = true;
+        }
+    }
+    std::fclose(f);
+    return found;
+}
+
+}  // namespace
+
 int32_t hfx_autotune(hfx_ctx *ctx, hfx_search_params *p, const float *mz, const float *it, const int64_t *off,
                      const float *pcr, const float *z, const float *tol, int32_t nspec, float *out_s,
                      uint64_t *out_k, uint32_t *out_pep, int64_t *out_ncand, int32_t reps, float *ms_out) {
@@ -1367,6 +1475,22 @@ int32_t hfx_autotune(hfx_ctx *ctx, hfx_search_params *p, const float *mz, const 
     if (p->batch_mode == 0) return fail(ctx, HFX_ERR_ARG, "hfx_autotune tunes the batched modes");
     HFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     Batch b{mz, it, pcr, z, tol, off, nspec};
+    // a choice persisted for this batch shape is reused without timing
+    const char *cache = std::getenv("HFX_AUTOTUNE_FILE");
+    std::string key;
+    if (cache && *cache) {
+        int64_t npk = 0;
+        HFX_CUDA(cudaMemcpy(&npk, off + nspec, 8, cudaMemcpyDeviceToHost), "D2H peak count");
+        key = autotune_key(ctx, p, nspec, npk);
+        int32_t g = 0, c = 0;
+        float ms = 0.0f;
+        if (!key.empty() && autotune_lookup(cache, key, &g, &c, &ms)) {
+            p->group_size = g;
+            p->chunk = c;
+            if (ms_out) *ms_out = ms;
+            return search_device(ctx, p, b, out_s, out_k, out_pep, out_ncand);
+        }
+    }
     hfx_search_params q = *p;
     q.use_graph = 0;
     // one 16-byte shared-memory load per bin: 8 BF16/FP16 or 4 FP32 spectra
@@ -1411,6 +1535,13 @@ int32_t hfx_autotune(hfx_ctx *ctx, hfx_search_params *p, const float *mz, const 
     p->group_size = best_g;
     p->chunk = best_c;
     if (ms_out) *ms_out = best;
+    if (!key.empty()) {
+        FILE *f = std::fopen(cache, "a");
+        if (f) {
+            std::fprintf(f, "%s\t%d\t%d\t%.4f\n", key.c_str(), best_g, best_c, (double)best);
+            std::fclose(f);
+        }
+    }
     return HFX_OK;
 }
 
@@ -1476,7 +1607,7 @@ int32_t hfx_preprocess(hfx_ctx *ctx, const hfx_search_params *p, const float *mz
     int rc = hfx_launch_layout(mz, off, pcr, z, tol, nspec, lp, meta, d_max, nullptr, ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_layout");
     HFX_CUDA(ctx->d_err.ensure(16), "alloc err");
-    HFX_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, 4, ctx->stream), "memset err");
+    HFX_CUDA(clear_err(ctx), "memset err");
     rc = hfx_launch_preprocess(mz, it, off, pcr, lp, meta, nspec, stride, rows, (__nv_bfloat16 *)rows_bf16,
                                (__half *)rows_fp16, ctx->d_err.as<uint32_t>(), ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_preprocess");

@@ -179,13 +179,13 @@ __global__ void __launch_bounds__(256) k_gen_lists(DevDB db, const int32_t *__re
     uint32_t *planes = reinterpret_cast<uint32_t *>(smem) + (size_t)warp * 3 * words;
     uint16_t *list = reinterpret_cast<uint16_t *>(reinterpret_cast<uint32_t *>(smem) + (size_t)nw * 3 * words) +
                      (size_t)warp * list_cap;
-    __shared__ unsigned long long s_stats[2];
-    if (threadIdx.x < 2) s_stats[threadIdx.x] = 0ull;
+    __shared__ unsigned long long s_stats[3];
+    if (threadIdx.x < 3) s_stats[threadIdx.x] = 0ull;
     for (int32_t i = lane; i < 3 * words; i += 32) planes[i] = 0u;
     __syncthreads();
     const Planes pl{planes, planes + words, planes + 2 * words};
     const float mt_lane = db.mt[lane];
-    unsigned long long my_lists = 0, my_entries = 0;
+    unsigned long long my_lists = 0, my_entries = 0, my_res = 0;
     for (int64_t t = (int64_t)blockIdx.x * nw + warp; t < (int64_t)db.num_pep; t += (int64_t)gridDim.x * nw) {
         const uint32_t p = (uint32_t)t;
         uint32_t need = 0;
@@ -196,6 +196,7 @@ __global__ void __launch_bounds__(256) k_gen_lists(DevDB db, const int32_t *__re
         const int zmax = 32 - __clz(need);
         const uint32_t tc = db.tc_sorted[p], tn = db.tn_sorted[p];
         const float r = db.r_sorted[p];
+        my_res += tn > tc ? tn - tc : 0u;
         WordRange all{0x7FFFFFFF, 0};
         for (int z = 1; z <= zmax; ++z) {
             const WordRange wr = build_planes_range<FastDiv>(pl, db.ions, tc, tn, r, z, z, nbins, mt_lane, NoMods{});
@@ -226,11 +227,13 @@ __global__ void __launch_bounds__(256) k_gen_lists(DevDB db, const int32_t *__re
         if (lane == 0) {
             atomicAdd(&s_stats[0], my_lists);
             atomicAdd(&s_stats[1], my_entries);
+            atomicAdd(&s_stats[2], my_res);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
             atomicAdd(&stats[0], s_stats[0]);
             atomicAdd(&stats[1], s_stats[1]);
+            atomicAdd(&stats[6], s_stats[2]);
         }
     }
 }
@@ -500,12 +503,12 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
     __shared__ uint32_t thr_u[G], s_lock[G];
     __shared__ float s_ls[G * L];
     __shared__ uint32_t s_lk[G * L];
-    __shared__ unsigned long long s_stats[4];
+    __shared__ unsigned long long s_stats[5];
 
     const int32_t ngroups = (int32_t)*ngroups_p;
     const uint32_t total = item_off[ngroups];
     if (threadIdx.x == 0) mbar_init(bar, 1);
-    if (threadIdx.x < 4) s_stats[threadIdx.x] = 0ull;
+    if (threadIdx.x < 5) s_stats[threadIdx.x] = 0ull;
     __syncthreads();
     const int my_slot = reduce_slot_of_lane<G>(lane);
     uint32_t my_cand = 0, my_entries = 0, my_psm = 0, my_claims = 0;
@@ -537,11 +540,12 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
             s_we[j] = e;
         }
         slots.reset_shared();
+        const int32_t nb = tile_bins(gi.maxlen);
         if (threadIdx.x == 0) {
             s_next = p0;
             my_claims += p1 - p0;
+            if (stats && !kGlobal) s_stats[4] += (unsigned long long)nb * G * sizeof(T);
         }
-        const int32_t nb = tile_bins(gi.maxlen);
         if constexpr (kGlobal) {
             tile = tiles + (size_t)g * stride * G;
             __syncthreads();
@@ -735,6 +739,7 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
             atomicAdd(&stats[3], s_stats[1]);
             atomicAdd(&stats[4], s_stats[2]);
             atomicAdd(&stats[5], s_stats[3]);
+            atomicAdd(&stats[7], s_stats[4]);
         }
     }
 }

@@ -85,11 +85,20 @@ const char *hfx_last_error(const hfx_ctx *ctx);
 #define HFX_STAGE_PACK 8        /* interleaved spectrum tiles of the groups */
 #define HFX_NSTAGES 9
 int32_t hfx_set_profiling(hfx_ctx *ctx, int32_t on);
+/* Caps the bytes of the context's search workspaces (new; the reference
+ * sizes its dense matrices to the free memory, Search.hs:427-433): a call
+ * whose workspaces would grow the context beyond `bytes` allocates nothing
+ * more and returns HFX_ERR_OOM, and the context stays usable (raise the cap
+ * and call again).  0 = no cap.  in_use (nullable) receives the bytes held
+ * now.  The database and the per-call host staging are not counted. */
+int32_t hfx_set_workspace_limit(hfx_ctx *ctx, uint64_t bytes, uint64_t *in_use);
 int32_t hfx_stage_stats(hfx_ctx *ctx, double *ms, int64_t *launches, int64_t *units, int32_t reset);
 /* Work counters of the batched list path, accumulated while profiling is on:
  * [0] ion lists built, [1] list entries built, [2] candidates scored,
  * [3] list entries streamed by the scorer, [4] peptide-spectrum pairs,
- * [5] candidate positions in the scorer's work items (active or not). */
+ * [5] candidate positions in the scorer's work items (active or not),
+ * [6] residues read by the list generator (one peptide's once per step),
+ * [7] spectrum-tile bytes staged into shared memory by the scorer. */
 int32_t hfx_search_counters(hfx_ctx *ctx, uint64_t *out8, int32_t reset);
 
 /* Digest proteins into the search database and upload it.  Replaces
@@ -198,7 +207,11 @@ int32_t hfx_set_protein_segments(hfx_ctx *ctx, const uint32_t *seg, int32_t npro
  * size (candidates per item) it supports, `reps` timed runs each after one
  * warm-up, and writes the fastest into p->group_size and p->chunk.  The
  * outputs hold the last search's results.  ms_out (nullable) receives the
- * best time per search. */
+ * best time per search.  With the environment variable HFX_AUTOTUNE_FILE
+ * naming a text file, the choice is persisted there per batch shape (the
+ * device, database and batch sizes, and the settings that pick the
+ * kernels): a later call with the same shape, in any process, reads it back
+ * and runs one search instead of timing them all. */
 int32_t hfx_autotune(hfx_ctx *ctx, hfx_search_params *p, const float *mz, const float *it, const int64_t *off,
                      const float *pcr, const float *z, const float *tol, int32_t nspec, float *out_score,
                      uint64_t *out_key, uint32_t *out_pep, int64_t *out_ncand, int32_t reps, float *ms_out);
@@ -248,13 +261,17 @@ int32_t hfx_mod_isoforms(hfx_ctx *ctx, const uint32_t *pos, const int32_t *mod, 
  *     top_n <= 32, with the keys and scores of hfx_search_* (plain matches).
  * Its only scratch is a file-scope device array of
  * HFX_NOALLOC_MAX_BLOCKS * 32 * 12 bytes (117 KB) that every GPU loading the
- * library holds until exit.  The first call on a device looks up that
- * array's device address (cudaGetSymbolAddress) and sets the kernels'
- * shared-memory limit; make that first call before any stream capture.
- * Every call shares the one array, so calls that overlap on the GPU (two
- * streams, two threads) race: serialize them.  Work is issued on `stream`
- * (a cudaStream_t; NULL = the legacy default stream) and is asynchronous.
- * Returns HFX_ERR_ARG for sizes beyond these limits. */
+ * library holds until exit.  Every call looks up that array's device
+ * address (cudaGetSymbolAddress) and sets the kernels' shared-memory limit,
+ * host calls that allocate nothing, so a call stays correct after a device
+ * reset; the first call on a device also loads the kernels there: make it
+ * before any stream capture.  Every call shares the one array, so calls
+ * that overlap on the GPU (two streams, two threads) race: serialize them.
+ * Work is issued on `stream` (a cudaStream_t; NULL = the legacy default
+ * stream) and is asynchronous.  Returns HFX_ERR_ARG for sizes beyond these
+ * limits, and HFX_ERR_CUDA without launching anything when a CUDA error of
+ * earlier work is already pending on the calling thread (that error is left
+ * pending for its owner). */
 #define HFX_NOALLOC_MAX_BLOCKS 304
 int32_t hfx_score_spectrum_noalloc(const uint8_t *ions, const float *r_sorted, const uint32_t *tc_sorted,
                                    const uint32_t *tn_sorted, const uint32_t *idx_sorted, uint32_t num_pep,

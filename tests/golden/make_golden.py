@@ -1,7 +1,8 @@
 """Generate the golden fixtures of tests/golden from the REFERENCE's own code.
 
 Run where the reference checkout is (not on a GPU machine): it needs it and
-oracle/_ref/libhfx_ref.so, which `make -C oracle ref` compiles from the
+oracle/_ref/libhfx_ref.so, which `HFX_REFERENCE=<checkout> make -C oracle ref`
+compiles from the
 reference's unmodified Thrust sources (filter.cu, filter_by_mod.cu,
 calc_mod_cands.cu, prepare_gen_mod.cu, gen_mod_pep.cu, prepare_scoring.cu,
 sort.cu, prepare_ions_test.cu) with Thrust's host (CPP) system.

@@ -1,13 +1,15 @@
 """Writes pretty_tables.json: the text blocks of the reference's own output
 files (tests/spectra/*.out: the search header, the results table and the
 header details), which pin the table layout of include/hfx_report.h.
-Run in a checkout that has the reference at REF (default below)."""
+Run with the reference checkout as the argument or in HFX_REFERENCE."""
 import glob
 import json
 import os
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HFX_REFERENCE", "")
+if not REF:
+    sys.exit("usage: make_tables.py <reference checkout> (or set HFX_REFERENCE)")
 out = {}
 for path in sorted(glob.glob(os.path.join(REF, "tests", "spectra", "*.out"))):
     lines = open(path).read().split("\n")

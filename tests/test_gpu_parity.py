@@ -412,6 +412,39 @@ def test_autotune_picks_a_valid_shape(full_engine):
     assert np.array_equal(res.score.view(np.uint32), ref.score.view(np.uint32))
 
 
+def test_autotune_choice_persisted(full_engine, tmp_path, monkeypatch):
+    """With HFX_AUTOTUNE_FILE set, hfx_autotune writes its choice for the
+    batch shape once and later calls read it back instead of timing: the same
+    group and work-item sizes, one line in the file, the same results."""
+    import hfx_gb300
+    eng, prot, sp = full_engine
+    path = tmp_path / "autotune.tsv"
+    monkeypatch.setenv("HFX_AUTOTUNE_FILE", str(path))
+    sub = sp.subset(np.arange(64))
+    dev = _dev(sub)
+
+    def out():
+        return dict(score=torch.empty((64, 10), dtype=torch.float32, device="cuda"),
+                    key=torch.empty((64, 10), dtype=torch.int64, device="cuda"),
+                    pep=torch.empty((64, 10), dtype=torch.int32, device="cuda"),
+                    ncand=torch.empty(64, dtype=torch.int64, device="cuda"))
+    p1 = hfx_gb300.default_params(top_n=10, batch_mode=1, precision=1)
+    o1 = out()
+    ms1 = eng.autotune(dev, p1, o1, reps=1)
+    lines = path.read_text().splitlines()
+    assert len(lines) == 1 and lines[0].split("\t")[1:3] == [str(p1.group_size), str(p1.chunk)]
+    p2 = hfx_gb300.default_params(top_n=10, batch_mode=1, precision=1)
+    o2 = out()
+    ms2 = eng.autotune(dev, p2, o2, reps=1)
+    assert (p2.group_size, p2.chunk) == (p1.group_size, p1.chunk) and abs(ms2 - ms1) < 1e-3
+    assert len(path.read_text().splitlines()) == 1
+    assert torch.equal(o1["key"], o2["key"]) and torch.equal(o1["score"], o2["score"])
+    # another batch shape is tuned and appended
+    p3 = hfx_gb300.default_params(top_n=10, batch_mode=1, precision=0)
+    eng.autotune(dev, p3, out(), reps=1)
+    assert len(path.read_text().splitlines()) == 2
+
+
 @pytest.mark.parametrize("G", [4, 8])
 def test_keep_64_candidates(full_engine, oracle, G):
     """Up to 64 candidates kept per spectrum for FP32 rescoring (two member
