@@ -1688,6 +1688,28 @@ int32_t hfx_ion_bins(hfx_ctx *ctx, const uint32_t *pos, const int32_t *charges, 
     return HFX_OK;
 }
 
+int32_t hfx_selftest_charge_division(hfx_ctx *ctx, int32_t exp_lo, int32_t exp_hi, uint64_t *mismatches,
+                                     uint32_t *example) {
+    if (!ctx || !mismatches) return fail(ctx, HFX_ERR_ARG, "bad hfx_selftest_charge_division arguments");
+    HFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaError_t e;
+    unsigned long long *cnt = ctx->buf<unsigned long long>("selftest", 2, e);
+    if (e) return cuda_fail(ctx, e, "alloc");
+    HFX_CUDA(cudaMemsetAsync(cnt, 0, 16, ctx->stream), "memset");
+    const int rc = hfx_launch_selftest_division(exp_lo, exp_hi, cnt, ctx->stream);
+    if (rc == (int)cudaErrorInvalidValue) return fail(ctx, HFX_ERR_ARG, "exponents must satisfy 1 <= lo <= hi <= 254");
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_selftest_division");
+    unsigned long long h[2];
+    HFX_CUDA(cudaMemcpyAsync(h, cnt, 16, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    *mismatches = h[0];
+    if (example) {
+        example[0] = (uint32_t)h[1];          // the dividend's bits
+        example[1] = (uint32_t)(h[1] >> 56);  // the charge
+    }
+    return HFX_OK;
+}
+
 int32_t hfx_mod_isoforms(hfx_ctx *ctx, const uint32_t *pos, const int32_t *mod, const uint32_t *rank, int32_t n,
                          int32_t cap, uint32_t *count, uint32_t *unrank, uint8_t *modded) {
     if (!ctx || n < 0 || cap < 0 || !pos || !mod || !rank || !count || !unrank || !modded)

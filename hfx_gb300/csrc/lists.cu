@@ -257,13 +257,6 @@ __global__ void __launch_bounds__(256) k_gen_lists(DevDB db, const int32_t *__re
 // 6: 2->3 (+25); 0 is a pad entry of weight 0.  Levels 1, 2, 3 are the
 // reference's intensities 10, 25, 50 (ion_series.cu:78-123), max-deduped as
 // its atomicMax into the dense row (ion_series.cu:71-75).
-constexpr uint64_t kSegCodeTab = (1ull << 4) | (2ull << 8) | (3ull << 12) | (4ull << 24) | (5ull << 28) |
-                                 (6ull << 44);
-
-__device__ __forceinline__ uint32_t seg_code(uint32_t before, uint32_t after) {
-    return (uint32_t)(kSegCodeTab >> ((before * 4u + after) * 4u)) & 7u;
-}
-
 // Offset of a peptide's segment slot: kLevels x lstart[p] (slots of
 // kLevels x round8(10 (tn - tc)) entries, 16-byte aligned).
 __device__ __forceinline__ uint64_t seg_offset(const uint32_t *__restrict__ lstart, uint32_t p) {
@@ -319,23 +312,40 @@ __device__ __forceinline__ WordRange build_charge_planes(uint32_t *planes, int32
     return WordRange{lo >> 5, (hi >> 5) + 1};
 }
 
-// Words of level z (cumulative over charges 1..z) and the bits that change
-// from level z-1 to level z.
+// Words of level z (cumulative over charges 1..z): any ion, weight >= 25,
+// weight 50.
 struct SegWords {
     uint32_t a, h, t;
 };
 
+// The code bits of every bit position of a word whose level goes from
+// `p` to `c` (positions whose level does not change are not emitted):
+// bit 0 for codes 1, 3, 5; bit 1 for 2, 3, 6; bit 2 for 4, 5, 6.
+struct SegCodes {
+    uint32_t changed, c0, c1, c2;
+};
+__device__ __forceinline__ SegCodes seg_codes(const SegWords &p, const SegWords &c) {
+    const uint32_t p0 = ~p.a, p1 = p.a & ~p.h, p2 = p.h & ~p.t;  // level before: 0, 1, 2
+    const uint32_t a1 = c.a & ~c.h, a2 = c.h & ~c.t, a3 = c.t;  // level after: 1, 2, 3
+    SegCodes r;
+    r.changed = (c.a ^ p.a) | (c.h ^ p.h) | (c.t ^ p.t);
+    r.c0 = (p0 & (a1 | a3)) | (p1 & a3);
+    r.c1 = (p0 & (a2 | a3)) | (p2 & a3);
+    r.c2 = (p1 & (a2 | a3)) | (p2 & a3);
+    return r;
+}
+
 // Warp-cooperative compaction of the charge planes, words [wr.lo, wr.hi),
 // into the segments 1..zmax (clearing the words): lane l takes ceil(words /
 // 32) consecutive words; a warp scan per level places every lane's entries.
-// cum[z-1] receives the entries of segments 1..z.  Returns the total (may
-// exceed cap; entries beyond cap are dropped).
+// cum_lane receives, in lane z-1 < zmax, the entries of segments 1..z (0 in
+// the other lanes).  Returns the total (may exceed cap; entries beyond cap
+// are dropped).
 __device__ __forceinline__ int compact_segments(uint32_t *planes, int32_t words, int zmax, WordRange wr,
-                                                uint16_t *list, int cap, int (&cum)[kLevels]) {
+                                                uint16_t *list, int cap, int &cum_lane) {
     const int lane = threadIdx.x & 31;
     const int nwords = wr.hi - wr.lo;
-#pragma unroll
-    for (int z = 0; z < kLevels; ++z) cum[z] = 0;
+    cum_lane = 0;
     if (nwords <= 0) return 0;
     const int k = (nwords + 31) >> 5;
     const int w0 = wr.lo + lane * k;
@@ -361,7 +371,7 @@ __device__ __forceinline__ int compact_segments(uint32_t *planes, int32_t words,
         const int incl = warp_incl_scan(cnt[z]);
         pos[z] = base + incl - cnt[z];
         base += __shfl_sync(kFullMask, incl, 31);
-        cum[z] = z < zmax ? base : 0;
+        if (lane == z && z < zmax) cum_lane = base;
     }
     for (int w = w0; w < w1; ++w) {
         SegWords prev{0u, 0u, 0u};
@@ -375,13 +385,13 @@ __device__ __forceinline__ int compact_segments(uint32_t *planes, int32_t words,
                 pc[w] = 0u;
                 pc[words + w] = 0u;
                 pc[2 * words + w] = 0u;
-                uint32_t ch = (cur.a ^ prev.a) | (cur.h ^ prev.h) | (cur.t ^ prev.t);
+                const SegCodes sc = seg_codes(prev, cur);
+                uint32_t ch = sc.changed;
                 while (ch) {
                     const int b = __ffs(ch) - 1;
                     ch &= ch - 1u;
-                    const uint32_t before = ((prev.a >> b) & 1u) + ((prev.h >> b) & 1u) + ((prev.t >> b) & 1u);
-                    const uint32_t after = ((cur.a >> b) & 1u) + ((cur.h >> b) & 1u) + ((cur.t >> b) & 1u);
-                    if (pos[z] < cap) list[pos[z]] = (uint16_t)(bin0 + ((uint32_t)b << 3) + seg_code(before, after));
+                    const uint32_t code = ((sc.c0 >> b) & 1u) | (((sc.c1 >> b) & 1u) << 1) | (((sc.c2 >> b) & 1u) << 2);
+                    if (pos[z] < cap) list[pos[z]] = (uint16_t)(bin0 + ((uint32_t)b << 3) + code);
                     ++pos[z];
                 }
                 prev = cur;
@@ -428,8 +438,8 @@ __global__ void __launch_bounds__(256) k_gen_seglists(DevDB db, const int32_t *_
         const float r = db.r_sorted[p];
         my_res += tn > tc ? tn - tc : 0u;
         const WordRange wr = build_charge_planes<FastDiv>(planes, words, db.ions, tc, tn, r, zmax, nbins, mt_lane);
-        int cum[kLevels];
-        int n = compact_segments(planes, words, zmax, wr, list, list_cap, cum);
+        int cum_lane;
+        int n = compact_segments(planes, words, zmax, wr, list, list_cap, cum_lane);
         if (n > list_cap) {
             if (lane == 0) atomicOr(err, kErrListOverflow);
             n = list_cap;
@@ -439,7 +449,7 @@ __global__ void __launch_bounds__(256) k_gen_seglists(DevDB db, const int32_t *_
         const uint4 *src = reinterpret_cast<const uint4 *>(list);
         uint4 *dst = reinterpret_cast<uint4 *>(lists + seg_offset(lstart, p));
         for (int i = lane; i < ((n + 7) >> 3); i += 32) dst[i] = src[i];
-        if (lane < kLevels) list_len[(size_t)lane * db.num_pep + p] = (uint16_t)min(cum[lane], n);
+        if (lane < kLevels) list_len[(size_t)lane * db.num_pep + p] = (uint16_t)min(cum_lane, n);
         my_lists += (unsigned long long)__popc(need);
         my_entries += (unsigned long long)n;
         __syncwarp();
@@ -500,33 +510,42 @@ __global__ void __launch_bounds__(256) k_rescore_seglists(const uint16_t *__rest
                 const uint32_t p = (uint32_t)kk;
                 const int n = list_len[(size_t)(z - 1) * num_pep + p];
                 const uint16_t *lp = lists + seg_offset(lstart, p);
-                int32_t lo = 0x7FFFFFFF, hi = -1;
-                for (int i = lane; i < n; i += 32) {
-                    const uint32_t e = __ldg(lp + i);
-                    const int32_t bin = (int32_t)(e >> 3);
-                    const uint32_t after = (0x3323210u >> (4u * (e & 7u))) & 0xFu;  // level after the change
-                    if (bin < nbins && after) {
-                        atomicOr(&pl.A[bin >> 5], 1u << (bin & 31));
-                        if (after >= 2u) atomicOr(&pl.H[bin >> 5], 1u << (bin & 31));
-                        if (after == 3u) atomicOr(&pl.T[bin >> 5], 1u << (bin & 31));
-                        lo = min(lo, bin);
-                        hi = max(hi, bin);
+                if (z == 1) {
+                    // segment 1 is the level-1 list itself (codes 1..3 are the levels)
+                    for (int i = lane; i < n; i += 32) {
+                        const uint32_t e = __ldg(lp + i);
+                        if ((int32_t)(e >> 3) < m.len)
+                            acc = __fmaf_rn(level_weight(e & 3u), __ldg(row + (e >> 3)), acc);
                     }
+                } else {
+                    int32_t lo = 0x7FFFFFFF, hi = -1;
+                    for (int i = lane; i < n; i += 32) {
+                        const uint32_t e = __ldg(lp + i);
+                        const int32_t bin = (int32_t)(e >> 3);
+                        const uint32_t after = (0x3323210u >> (4u * (e & 7u))) & 0xFu;  // level after the change
+                        if (bin < nbins && after) {
+                            atomicOr(&pl.A[bin >> 5], 1u << (bin & 31));
+                            if (after >= 2u) atomicOr(&pl.H[bin >> 5], 1u << (bin & 31));
+                            if (after == 3u) atomicOr(&pl.T[bin >> 5], 1u << (bin & 31));
+                            lo = min(lo, bin);
+                            hi = max(hi, bin);
+                        }
+                    }
+                    __syncwarp();
+                    lo = __reduce_min_sync(kFullMask, lo);
+                    hi = __reduce_max_sync(kFullMask, hi);
+                    const WordRange wr = hi < 0 ? WordRange{0, 0} : WordRange{lo >> 5, (hi >> 5) + 1};
+                    int nl = compact_planes(pl, wr, true, list, list_cap);
+                    if (nl > list_cap) {
+                        if (lane == 0) atomicOr(err, kErrListOverflow);
+                        nl = list_cap;
+                    }
+                    for (int i = lane; i < nl; i += 32) {
+                        const uint32_t e = list[i];
+                        acc = __fmaf_rn(level_weight(e & 3u), __ldg(row + (e >> 2)), acc);
+                    }
+                    __syncwarp();
                 }
-                __syncwarp();
-                lo = __reduce_min_sync(kFullMask, lo);
-                hi = __reduce_max_sync(kFullMask, hi);
-                const WordRange wr = hi < 0 ? WordRange{0, 0} : WordRange{lo >> 5, (hi >> 5) + 1};
-                int nl = compact_planes(pl, wr, true, list, list_cap);
-                if (nl > list_cap) {
-                    if (lane == 0) atomicOr(err, kErrListOverflow);
-                    nl = list_cap;
-                }
-                for (int i = lane; i < nl; i += 32) {
-                    const uint32_t e = list[i];
-                    acc = __fmaf_rn(level_weight(e & 3u), __ldg(row + (e >> 2)), acc);
-                }
-                __syncwarp();
             } else if (kk >> 63) {
                 if (lane == 0) atomicOr(err, kErrBounds);
             }
@@ -1112,21 +1131,29 @@ int hfx_lists_generate(const DevDB &db, const int32_t *cover, int64_t npep1, int
 int hfx_lists_generate_seg(const DevDB &db, const int32_t *cover, int64_t npep1, int32_t nbins,
                            const uint32_t *lstart, uint16_t *lists, uint16_t *list_len, int32_t list_cap, int fastdiv,
                            unsigned long long *stats, uint32_t *err, cudaStream_t st) {
-    const int nw = 8;
     const int32_t words = (nbins + 31) / 32;
     list_cap = (std::max(32, std::min(list_cap, kMaxListLen)) + 7) & ~7;  // 16-byte staging lists
-    // per warp: the bit planes of kLevels charges and a staging list
-    const size_t smem = (size_t)nw * kLevels * 3 * words * 4 + (size_t)nw * list_cap * 2;
+    // per warp: the bit planes of kLevels charges and a staging list; the
+    // CTA size (4, 6 or 8 warps) that keeps the most warps resident
+    const size_t per_warp = (size_t)kLevels * 3 * words * 4 + (size_t)list_cap * 2;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     auto f = fastdiv ? k_gen_seglists<true> : k_gen_seglists<false>;
-    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(8 * per_warp));
     if (e != cudaSuccess) return (int)e;
-    int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, nw * 32, smem);
-    f<<<sms * (per > 0 ? per : 1), nw * 32, smem, st>>>(db, cover, npep1, nbins, lstart, lists, list_len, list_cap,
-                                                        stats, err);
+    int nw = 8, per = 0, best = -1;
+    for (int cand : {8, 6, 4}) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, cand * 32, cand * per_warp);
+        if (b * cand > best) {
+            best = b * cand;
+            nw = cand;
+            per = b;
+        }
+    }
+    f<<<sms * (per > 0 ? per : 1), nw * 32, nw * per_warp, st>>>(db, cover, npep1, nbins, lstart, lists, list_len,
+                                                                 list_cap, stats, err);
     return (int)cudaGetLastError();
 }
 
