@@ -33,7 +33,7 @@ EXPORTED = [
     "hfx_set_mods", "hfx_mod_table", "hfx_search_host", "hfx_search_device", "hfx_search_evalues",
     "hfx_preprocess", "hfx_find_windows", "hfx_ion_bins", "hfx_mod_isoforms", "hfx_digest", "hfx_pack_ions",
     "hfx_set_profiling", "hfx_stage_stats", "hfx_search_counters", "hfx_set_workspace_limit",
-    "hfx_selftest_charge_division",
+    "hfx_selftest_charge_division", "hfx_digest_gpu",
 ]
 STAGES = ["layout", "preprocess", "windows", "score", "topn", "rescore", "mods", "lists", "pack"]
 
@@ -113,6 +113,7 @@ def load_library(path: str = LIB_PATH):
         "hfx_search_counters": (i32, [P, P, i32]),
         "hfx_set_workspace_limit": (i32, [P, u64, C.POINTER(u64)]),
         "hfx_selftest_charge_division": (i32, [P, i32, i32, C.POINTER(u64), P]),
+        "hfx_digest_gpu": (C.c_int64, [P, P, P, i32, P, i32, i32, f32, f32, i32, i32, i32, P, P, P, C.c_int64]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -262,6 +263,26 @@ class Engine:
         used = C.c_uint64()
         self._check(self.lib.hfx_set_workspace_limit(self.h, int(nbytes), C.byref(used)))
         return used.value
+
+    def digest(self, seq, seg, mass_table, rule=1, missed=2, min_mass=400.0, max_mass=7200.0, proline_rule=False,
+               min_len=0, max_len=0):
+        """hfx_digest_gpu: the database digest on this context's GPU; the same
+        (r, tc, tn) as the host `digest`."""
+        seq = np.ascontiguousarray(seq, np.uint8)
+        seg = np.ascontiguousarray(seg, np.uint32)
+        mt = np.ascontiguousarray(mass_table, np.float32)
+        args = (_ptr(seq), _ptr(seg), len(seg) - 1, _ptr(mt), rule, missed, min_mass, max_mass, int(proline_rule),
+                min_len, max_len)
+        n = self.lib.hfx_digest_gpu(self.h, *args, None, None, None, 0)
+        if n < 0:
+            raise HfxError(HFX_ERR_ARG, self.lib.hfx_last_error(self.h).decode())
+        r = np.empty(n, np.float32)
+        tc = np.empty(n, np.uint32)
+        tn = np.empty(n, np.uint32)
+        m = self.lib.hfx_digest_gpu(self.h, *args, _ptr(r), _ptr(tc), _ptr(tn), n)
+        if m != n:
+            raise HfxError(HFX_ERR_CUDA, self.lib.hfx_last_error(self.h).decode())
+        return r, tc, tn
 
     def selftest_charge_division(self, exp_lo: int = 67, exp_hi: int = 187):
         """hfx_selftest_charge_division: (mismatches, (dividend bits, charge))

@@ -13,6 +13,12 @@
 #include "mods.h"
 #include "evalues.h"
 #include "ions.h"
+
+int hfx_digest_launch(const uint8_t *d_seq, const uint32_t *d_seg, int32_t nprot, uint32_t nres, const float *mt26,
+                      int32_t rule_mask, int32_t missed, float min_mass, float max_mass, int32_t proline,
+                      int32_t min_len, int32_t max_len, float *pm, uint32_t *ptn, uint32_t *plen, uint32_t *pnext,
+                      int32_t *cnt, int32_t *incl, int32_t *partial, float *r, uint32_t *tc, uint32_t *tn,
+                      int64_t cap, int pass, cudaStream_t st);
 #include "../../include/hfx_gpu.h"
 
 #include <nvtx3/nvToolsExt.h>
@@ -634,8 +640,9 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
                                          ctx->d_err.as<uint32_t>(), ctx->stream);
         else if (!rc && seg_lists)
             rc = hfx_lists_generate_seg(db, cover, npep1, (int32_t)std::min<int64_t>(stride, kMaxWords * 32),
-                                        ctx->d_lstart.as<uint32_t>(), (uint16_t *)lists, llen, list_cap, p->fastdiv,
-                                        stats, ctx->d_err.as<uint32_t>(), ctx->stream);
+                                        ctx->d_lstart.as<uint32_t>(), (uint16_t *)lists, llen,
+                                        (int32_t)ctx->max_ladder, p->fastdiv, stats, ctx->d_err.as<uint32_t>(),
+                                        ctx->stream);
         else if (!rc)
             rc = hfx_lists_generate(db, cover, npep1, (int32_t)std::min<int64_t>(stride, kMaxWords * 32),
                                     ctx->d_lstart.as<uint32_t>(), total10, (uint16_t *)lists, llen, list_cap,
@@ -1082,6 +1089,102 @@ int64_t hfx_digest(const uint8_t *seq, const uint32_t *seg, int32_t nprot, const
     return nf;
 }
 
+namespace {
+
+uint32_t rule_mask(int rule) {
+    uint32_t m = 0;
+    for (int c = 'A'; c <= 'Z'; ++c)
+        if (cleaves_after(rule, (uint8_t)c)) m |= 1u << (c - 'A');
+    return m;
+}
+
+// The digest on the device (digest.cu): counts, then, with `r`, resizes
+// the three host vectors and fills them.  Returns the fragment count, -1 for
+// bad arguments or -3 for a CUDA failure (ctx->err says which).
+int64_t digest_device(hfx_ctx *ctx, const uint8_t *seq, const uint32_t *seg, int32_t nprot, const float *mt26,
+                      int32_t rule, int32_t missed, float min_mass, float max_mass, int32_t proline_rule,
+                      int32_t min_len, int32_t max_len, std::vector<float> *r, std::vector<uint32_t> *tc,
+                      std::vector<uint32_t> *tn) {
+    const uint32_t nres = nprot > 0 ? seg[nprot] : 0u;
+    for (int32_t p = 0; p < nprot; ++p)
+        if (seg[p + 1] < seg[p]) return fail(ctx, HFX_ERR_ARG, "protein offsets must not decrease"), -1;
+    for (uint32_t i = nprot > 0 ? seg[0] : 0u; i < nres; ++i)
+        if (seq[i] < 'A' || seq[i] > 'Z') return fail(ctx, HFX_ERR_ARG, "residue outside A-Z"), -1;
+    if (nres == 0) {
+        if (r) r->clear(), tc->clear(), tn->clear();
+        return 0;
+    }
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HFX_ERR_CUDA, "cudaSetDevice"), -3;
+    cudaError_t e;
+    uint8_t *d_seq = ctx->buf<uint8_t>("dg_seq", nres, e);
+    uint32_t *d_seg = e ? nullptr : ctx->buf<uint32_t>("dg_seg", (size_t)nprot + 1, e);
+    float *pm = e ? nullptr : ctx->buf<float>("dg_pm", nres, e);
+    uint32_t *ptn = e ? nullptr : ctx->buf<uint32_t>("dg_ptn", nres, e);
+    uint32_t *plen = e ? nullptr : ctx->buf<uint32_t>("dg_plen", nres, e);
+    uint32_t *pnext = e ? nullptr : ctx->buf<uint32_t>("dg_pnext", nres, e);
+    int32_t *cnt = e ? nullptr : ctx->buf<int32_t>("dg_cnt", nres, e);
+    int32_t *incl = e ? nullptr : ctx->buf<int32_t>("dg_incl", nres, e);
+    int32_t *partial = e ? nullptr : ctx->buf<int32_t>("dg_partial", hfx_scan_partials_needed(nres), e);
+    if (e) return cuda_fail(ctx, e, "alloc digest"), -3;
+    if ((e = cudaMemcpyAsync(d_seq, seq, nres, cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(d_seg, seg, 4ull * (nprot + 1), cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess)
+        return cuda_fail(ctx, e, "H2D digest"), -3;
+    const int32_t mask = (int32_t)rule_mask(rule);
+    int rc = hfx_digest_launch(d_seq, d_seg, nprot, nres, mt26, mask, missed, min_mass, max_mass, proline_rule,
+                               min_len, max_len, pm, ptn, plen, pnext, cnt, incl, partial, nullptr, nullptr, nullptr,
+                               0, 1, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_digest"), -3;
+    int32_t total = 0;
+    if ((e = cudaMemcpyAsync(&total, incl + nres - 1, 4, cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess)
+        return cuda_fail(ctx, e, "digest count"), -3;
+    if (!r) return total;
+    r->resize(total);
+    tc->resize(total);
+    tn->resize(total);
+    if (total == 0) return 0;
+    float *d_r = ctx->buf<float>("dg_r", total, e);
+    uint32_t *d_tc = e ? nullptr : ctx->buf<uint32_t>("dg_tc", total, e);
+    uint32_t *d_tn = e ? nullptr : ctx->buf<uint32_t>("dg_tn", total, e);
+    if (e) return cuda_fail(ctx, e, "alloc digest output"), -3;
+    rc = hfx_digest_launch(d_seq, d_seg, nprot, nres, mt26, mask, missed, min_mass, max_mass, proline_rule, min_len,
+                           max_len, pm, ptn, plen, pnext, cnt, incl, partial, d_r, d_tc, d_tn, total, 2, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_digest_splice"), -3;
+    if ((e = cudaMemcpyAsync(r->data(), d_r, 4ull * total, cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(tc->data(), d_tc, 4ull * total, cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(tn->data(), d_tn, 4ull * total, cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess)
+        return cuda_fail(ctx, e, "D2H digest"), -3;
+    return total;
+}
+
+}  // namespace
+
+int64_t hfx_digest_gpu(hfx_ctx *ctx, const uint8_t *seq, const uint32_t *seg, int32_t nprot, const float *mt26,
+                       int32_t rule, int32_t missed, float min_mass, float max_mass, int32_t proline_rule,
+                       int32_t min_len, int32_t max_len, float *r, uint32_t *tc, uint32_t *tn, int64_t cap) {
+    if (!ctx || !seq || !seg || !mt26 || nprot < 0 || missed < 0 || rule < 0 || rule > 13) {
+        if (ctx) fail(ctx, HFX_ERR_ARG, "bad hfx_digest_gpu arguments");
+        return -1;
+    }
+    if (!r) {
+        const int64_t n = digest_device(ctx, seq, seg, nprot, mt26, rule, missed, min_mass, max_mass, proline_rule,
+                                        min_len, max_len, nullptr, nullptr, nullptr);
+        return n < 0 ? -1 : n;
+    }
+    if (!tc || !tn) return fail(ctx, HFX_ERR_ARG, "bad hfx_digest_gpu arguments"), -1;
+    std::vector<float> hr;
+    std::vector<uint32_t> htc, htn;
+    const int64_t n = digest_device(ctx, seq, seg, nprot, mt26, rule, missed, min_mass, max_mass, proline_rule,
+                                    min_len, max_len, &hr, &htc, &htn);
+    if (n < 0) return -1;
+    if (n > cap) return fail(ctx, HFX_ERR_ARG, "output capacity below the fragment count"), -2;
+    std::memcpy(r, hr.data(), 4ull * n);
+    std::memcpy(tc, htc.data(), 4ull * n);
+    std::memcpy(tn, htn.data(), 4ull * n);
+    return n;
+}
+
 int32_t hfx_pack_ions(const uint8_t *ascii, uint64_t n, const uint8_t *ma, int32_t num_ma, uint8_t *out) {
     if (!ascii || !out || num_ma < 0 || num_ma > 7) return HFX_ERR_ARG;
     std::vector<uint8_t> in(ascii, ascii + n), packed;
@@ -1106,17 +1209,14 @@ int32_t hfx_build_db(hfx_ctx *ctx, const uint8_t *seq, const uint32_t *seg, int3
     const uint32_t nion = seg[nprot];
     for (uint32_t i = 0; i < nion; ++i)
         if (seq[i] < 'A' || seq[i] > 'Z') return fail(ctx, HFX_ERR_ARG, "residue outside A-Z");
-    const int64_t nf = hfx_digest(seq, seg, nprot, ctx->mt, rule, missed, min_mass, max_mass, proline_rule,
-                                  min_len, max_len, nullptr, nullptr, nullptr, 0);
-    if (nf < 0) return fail(ctx, HFX_ERR_ARG, "digest failed");
+    // the digest runs on the device; its fragments come back for the
+    // mass-order sort and the list layout of upload_db
+    const int64_t nf = digest_device(ctx, seq, seg, nprot, ctx->mt, rule, missed, min_mass, max_mass, proline_rule,
+                                     min_len, max_len, &ctx->h_r, &ctx->h_tc, &ctx->h_tn);
+    if (nf < 0) return nf == -1 ? HFX_ERR_ARG : HFX_ERR_CUDA;
     if (nf >= (1ll << 27)) return fail(ctx, HFX_ERR_UNSUPPORTED, "more than 2^27 fragments");
     ctx->h_ascii.assign(seq, seq + nion);
     ctx->h_seg.assign(seg, seg + nprot + 1);
-    ctx->h_r.resize(nf);
-    ctx->h_tc.resize(nf);
-    ctx->h_tn.resize(nf);
-    hfx_digest(seq, seg, nprot, ctx->mt, rule, missed, min_mass, max_mass, proline_rule, min_len, max_len,
-               ctx->h_r.data(), ctx->h_tc.data(), ctx->h_tn.data(), nf);
     ctx->num_ions = nion;
     ctx->num_pep = (uint64_t)nf;
     return upload_db(ctx);

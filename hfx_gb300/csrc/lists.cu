@@ -263,56 +263,7 @@ __device__ __forceinline__ uint64_t seg_offset(const uint32_t *__restrict__ lsta
     return (uint64_t)kLevels * lstart[p];
 }
 
-// The ion bit planes of charges 1..zmax, each charge into its own plane set
-// (planes + (c - 1) * 3 * words: A, H, T as in Planes), with every
-// (prefix, charge) item of the peptide spread over the lanes in one pass.
-// The b-ladder is the reference warp scan's (build_planes_range).  Returns
-// the range of plane words that may hold set bits.
-template <bool FastDiv>
-__device__ __forceinline__ WordRange build_charge_planes(uint32_t *planes, int32_t words,
-                                                         const uint8_t *__restrict__ ions, uint32_t tc, uint32_t tn,
-                                                         float residual, int zmax, int32_t nbins, float mt_lane) {
-    const int lane = threadIdx.x & 31;
-    BinRange br;
-    float carry = 0.0f;
-    for (uint32_t base = tc; base < tn; base += 32) {
-        const int cnt = (int)min(32u, tn - base);
-        uint32_t byte = 0;
-        if (lane < cnt) byte = __ldg(ions + base + lane);
-        float v = residue_mass(mt_lane, byte);
-        if (lane >= cnt) v = 0.0f;
-        if (lane == 0) v = __fadd_rn(v, carry);
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const float t = __shfl_up_sync(kFullMask, v, d);
-            if (lane >= d) v = __fadd_rn(v, t);
-        }
-        carry = __shfl_sync(kFullMask, v, cnt - 1);
-        const float y = __fsub_rn(residual, v);
-        // items (prefix k, charge c): item = (c-1)*cnt + k
-        const int items = cnt * zmax;
-        const uint32_t inv = (65536u + (uint32_t)cnt - 1u) / (uint32_t)cnt;
-        for (int it0 = 0; it0 < items; it0 += 32) {
-            const int it = it0 + lane;
-            const int cm1 = (int)(((uint32_t)it * inv) >> 16);
-            const int k = it - cm1 * cnt;
-            const float bk = __shfl_sync(kFullMask, v, k & 31);
-            const float yk = __shfl_sync(kFullMask, y, k & 31);
-            if (it < items) {
-                uint32_t *pc = planes + (size_t)cm1 * 3 * words;
-                const Planes pl{pc, pc + words, pc + 2 * words};
-                emit_ions<FastDiv>(pl, bk, yk, charge_const<FastDiv>(cm1 + 1), nbins, br);
-            }
-        }
-    }
-    __syncwarp();
-    const int32_t lo = __reduce_min_sync(kFullMask, br.lo);
-    const int32_t hi = __reduce_max_sync(kFullMask, br.hi);
-    if (hi < 0) return WordRange{0, 0};
-    return WordRange{lo >> 5, (hi >> 5) + 1};
-}
-
-// Words of level z (cumulative over charges 1..z): any ion, weight >= 25,
+// Words of a level (cumulative over charges 1..z): any ion, weight >= 25,
 // weight 50.
 struct SegWords {
     uint32_t a, h, t;
@@ -335,93 +286,80 @@ __device__ __forceinline__ SegCodes seg_codes(const SegWords &p, const SegWords 
     return r;
 }
 
-// Warp-cooperative compaction of the charge planes, words [wr.lo, wr.hi),
-// into the segments 1..zmax (clearing the words): lane l takes ceil(words /
-// 32) consecutive words; a warp scan per level places every lane's entries.
-// cum_lane receives, in lane z-1 < zmax, the entries of segments 1..z (0 in
-// the other lanes).  Returns the total (may exceed cap; entries beyond cap
-// are dropped).
-__device__ __forceinline__ int compact_segments(uint32_t *planes, int32_t words, int zmax, WordRange wr,
-                                                uint16_t *list, int cap, int &cum_lane) {
+// Segment z of a peptide: the bins whose level changes when the charge-z
+// planes `cur` join the planes of levels < z (`cum`), over the words [wr)
+// where `cur` has bits, in ascending bin order.  Warp-cooperative: lane l
+// takes ceil(words / 32) consecutive words, one scan places every lane's
+// entries.  Folds `cur` into `cum` and clears `cur`.  Returns the entries
+// (may exceed cap; entries beyond cap are dropped).
+__device__ __forceinline__ int compact_segment(const Planes &cum, const Planes &cur, WordRange wr, uint16_t *list,
+                                               int cap) {
     const int lane = threadIdx.x & 31;
     const int nwords = wr.hi - wr.lo;
-    cum_lane = 0;
     if (nwords <= 0) return 0;
     const int k = (nwords + 31) >> 5;
     const int w0 = wr.lo + lane * k;
     const int w1 = min(w0 + k, wr.hi);
-    int cnt[kLevels] = {0, 0, 0, 0};
+    int cnt = 0;
     for (int w = w0; w < w1; ++w) {
-        SegWords prev{0u, 0u, 0u};
-#pragma unroll
-        for (int z = 0; z < kLevels; ++z) {
-            if (z < zmax) {
-                const uint32_t *pc = planes + (size_t)z * 3 * words;
-                const uint32_t H = pc[words + w];
-                const SegWords cur{prev.a | pc[w] | H, prev.h | H, prev.t | pc[2 * words + w]};
-                cnt[z] += __popc((cur.a ^ prev.a) | (cur.h ^ prev.h) | (cur.t ^ prev.t));
-                prev = cur;
-            }
-        }
+        const uint32_t ph = cum.H[w], ch = cur.H[w];
+        const uint32_t pa = cum.A[w] | ph, pt = cum.T[w];
+        cnt += __popc(((pa | cur.A[w] | ch) ^ pa) | ((ph | ch) ^ ph) | ((pt | cur.T[w]) ^ pt));
     }
-    int pos[kLevels];
-    int base = 0;
-#pragma unroll
-    for (int z = 0; z < kLevels; ++z) {
-        const int incl = warp_incl_scan(cnt[z]);
-        pos[z] = base + incl - cnt[z];
-        base += __shfl_sync(kFullMask, incl, 31);
-        if (lane == z && z < zmax) cum_lane = base;
-    }
+    const int incl = warp_incl_scan(cnt);
+    int pos = incl - cnt;
     for (int w = w0; w < w1; ++w) {
-        SegWords prev{0u, 0u, 0u};
+        const uint32_t cA = cur.A[w], cH = cur.H[w], cT = cur.T[w];
+        const uint32_t pA = cum.A[w], pH = cum.H[w], pT = cum.T[w];
+        const SegWords pw{pA | pH, pH, pT};
+        const SegWords cw{pA | pH | cA | cH, pH | cH, pT | cT};
+        cum.A[w] = pA | cA;
+        cum.H[w] = pH | cH;
+        cum.T[w] = pT | cT;
+        cur.A[w] = 0u;
+        cur.H[w] = 0u;
+        cur.T[w] = 0u;
+        const SegCodes sc = seg_codes(pw, cw);
         const uint32_t bin0 = (uint32_t)w << 8;  // (w * 32) << 3
-#pragma unroll
-        for (int z = 0; z < kLevels; ++z) {
-            if (z < zmax) {
-                uint32_t *pc = planes + (size_t)z * 3 * words;
-                const uint32_t H = pc[words + w];
-                const SegWords cur{prev.a | pc[w] | H, prev.h | H, prev.t | pc[2 * words + w]};
-                pc[w] = 0u;
-                pc[words + w] = 0u;
-                pc[2 * words + w] = 0u;
-                const SegCodes sc = seg_codes(prev, cur);
-                uint32_t ch = sc.changed;
-                while (ch) {
-                    const int b = __ffs(ch) - 1;
-                    ch &= ch - 1u;
-                    const uint32_t code = ((sc.c0 >> b) & 1u) | (((sc.c1 >> b) & 1u) << 1) | (((sc.c2 >> b) & 1u) << 2);
-                    if (pos[z] < cap) list[pos[z]] = (uint16_t)(bin0 + ((uint32_t)b << 3) + code);
-                    ++pos[z];
-                }
-                prev = cur;
-            }
+        uint32_t chg = sc.changed;
+        while (chg) {
+            const int b = __ffs(chg) - 1;
+            chg &= chg - 1u;
+            const uint32_t code = ((sc.c0 >> b) & 1u) | (((sc.c1 >> b) & 1u) << 1) | (((sc.c2 >> b) & 1u) << 2);
+            if (pos < cap) list[pos] = (uint16_t)(bin0 + ((uint32_t)b << 3) + code);
+            ++pos;
         }
     }
+    const int n = __shfl_sync(kFullMask, incl, 31);
     __syncwarp();
-    return base;
+    return n;
 }
 
-// One warp per candidate peptide that some spectrum of the batch needs: the
-// segments of charge levels 1..zmax (zmax = the highest level needed), in
-// the peptide's slot; list_len[z-1][p] = entries of segments 1..z.
+// One warp per candidate peptide that some spectrum of the batch needs: for
+// z = 1..zmax (zmax = the highest level needed) the charge-z ions go into
+// the `cur` planes (the reference warp scan's b-ladder, build_planes_range),
+// segment z is compacted against the `cum` planes of the lower levels and
+// appended to the peptide's slot; list_len[z-1][p] = entries of segments
+// 1..z.  Segments are copied out by 2-byte lanes (64 contiguous bytes per
+// warp store): they start anywhere in the slot.
 template <bool FastDiv>
 __global__ void __launch_bounds__(256) k_gen_seglists(DevDB db, const int32_t *__restrict__ cover, int64_t npep1,
                                                       int32_t nbins, const uint32_t *__restrict__ lstart,
                                                       uint16_t *__restrict__ lists, uint16_t *__restrict__ list_len,
-                                                      int32_t list_cap, unsigned long long *__restrict__ stats,
+                                                      int32_t seg_cap, unsigned long long *__restrict__ stats,
                                                       uint32_t *__restrict__ err) {
     extern __shared__ __align__(16) uint8_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int32_t words = (nbins + 31) / 32;
-    const size_t per_warp = (size_t)kLevels * 3 * words;
-    uint32_t *planes = reinterpret_cast<uint32_t *>(smem) + (size_t)warp * per_warp;
-    uint16_t *list = reinterpret_cast<uint16_t *>(reinterpret_cast<uint32_t *>(smem) + (size_t)nw * per_warp) +
-                     (size_t)warp * list_cap;
+    uint32_t *pw = reinterpret_cast<uint32_t *>(smem) + (size_t)warp * 6 * words;
+    uint16_t *stage = reinterpret_cast<uint16_t *>(reinterpret_cast<uint32_t *>(smem) + (size_t)nw * 6 * words) +
+                      (size_t)warp * seg_cap;
     __shared__ unsigned long long s_stats[3];
     if (threadIdx.x < 3) s_stats[threadIdx.x] = 0ull;
-    for (size_t i = lane; i < per_warp; i += 32) planes[i] = 0u;
+    for (int32_t i = lane; i < 6 * words; i += 32) pw[i] = 0u;
     __syncthreads();
+    const Planes cum{pw, pw + words, pw + 2 * words};
+    const Planes cur{pw + 3 * words, pw + 4 * words, pw + 5 * words};
     const float mt_lane = db.mt[lane];
     unsigned long long my_lists = 0, my_entries = 0, my_res = 0;
     for (int64_t t = (int64_t)blockIdx.x * nw + warp; t < (int64_t)db.num_pep; t += (int64_t)gridDim.x * nw) {
@@ -437,22 +375,37 @@ __global__ void __launch_bounds__(256) k_gen_seglists(DevDB db, const int32_t *_
         const uint32_t tc = db.tc_sorted[p], tn = db.tn_sorted[p];
         const float r = db.r_sorted[p];
         my_res += tn > tc ? tn - tc : 0u;
-        const WordRange wr = build_charge_planes<FastDiv>(planes, words, db.ions, tc, tn, r, zmax, nbins, mt_lane);
-        int cum_lane;
-        int n = compact_segments(planes, words, zmax, wr, list, list_cap, cum_lane);
-        if (n > list_cap) {
-            if (lane == 0) atomicOr(err, kErrListOverflow);
-            n = list_cap;
+        uint16_t *slot = lists + seg_offset(lstart, p);
+        const uint32_t slot_cap = (uint32_t)kLevels * (((tn > tc ? tn - tc : 0u) * 10u + 7u) & ~7u);
+        uint32_t base = 0;
+        WordRange all{0x7FFFFFFF, 0};
+        for (int z = 1; z <= zmax; ++z) {
+            const WordRange wr = build_planes_range<FastDiv>(cur, db.ions, tc, tn, r, z, z, nbins, mt_lane, NoMods{});
+            if (wr.hi > wr.lo) {
+                all.lo = min(all.lo, wr.lo);
+                all.hi = max(all.hi, wr.hi);
+            }
+            int n = compact_segment(cum, cur, wr, stage, seg_cap);
+            if (n > seg_cap || base + (uint32_t)n > slot_cap) {
+                if (lane == 0) atomicOr(err, kErrListOverflow);
+                n = min(n, seg_cap);
+                n = (int)min((uint32_t)n, slot_cap - base);
+            }
+            for (int i = lane; i < n; i += 32) slot[base + i] = stage[i];
+            base += (uint32_t)n;
+            if (lane == 0) list_len[(size_t)(z - 1) * db.num_pep + p] = (uint16_t)base;
+            __syncwarp();
         }
-        // 16-byte copies: the slot and the staging list start on 16-byte
-        // boundaries; the slot holds kLevels x round8(10 (tn - tc)) entries
-        const uint4 *src = reinterpret_cast<const uint4 *>(list);
-        uint4 *dst = reinterpret_cast<uint4 *>(lists + seg_offset(lstart, p));
-        for (int i = lane; i < ((n + 7) >> 3); i += 32) dst[i] = src[i];
-        if (lane < kLevels) list_len[(size_t)lane * db.num_pep + p] = (uint16_t)min(cum_lane, n);
-        my_lists += (unsigned long long)__popc(need);
-        my_entries += (unsigned long long)n;
+        if (lane >= zmax && lane < kLevels) list_len[(size_t)lane * db.num_pep + p] = 0;
+        // the cumulative planes, back to zero
+        for (int32_t w = all.lo + lane; w < all.hi; w += 32) {
+            cum.A[w] = 0u;
+            cum.H[w] = 0u;
+            cum.T[w] = 0u;
+        }
         __syncwarp();
+        my_lists += (unsigned long long)__popc(need);
+        my_entries += (unsigned long long)base;
     }
     if (stats) {
         if (lane == 0) {
@@ -1129,13 +1082,15 @@ int hfx_lists_generate(const DevDB &db, const int32_t *cover, int64_t npep1, int
 }
 
 int hfx_lists_generate_seg(const DevDB &db, const int32_t *cover, int64_t npep1, int32_t nbins,
-                           const uint32_t *lstart, uint16_t *lists, uint16_t *list_len, int32_t list_cap, int fastdiv,
-                           unsigned long long *stats, uint32_t *err, cudaStream_t st) {
+                           const uint32_t *lstart, uint16_t *lists, uint16_t *list_len, int32_t max_ladder,
+                           int fastdiv, unsigned long long *stats, uint32_t *err, cudaStream_t st) {
     const int32_t words = (nbins + 31) / 32;
-    list_cap = (std::max(32, std::min(list_cap, kMaxListLen)) + 7) & ~7;  // 16-byte staging lists
-    // per warp: the bit planes of kLevels charges and a staging list; the
-    // CTA size (4, 6 or 8 warps) that keeps the most warps resident
-    const size_t per_warp = (size_t)kLevels * 3 * words * 4 + (size_t)list_cap * 2;
+    // one segment holds at most 10 ions per prefix of the longest ladder
+    const int32_t seg_cap = (std::max(32, std::min(10 * max_ladder, kMaxListLen)) + 7) & ~7;
+    // per warp: the cumulative and the current charge's bit planes and a
+    // staging segment; the CTA size (4, 6 or 8 warps) that keeps the most
+    // warps resident
+    const size_t per_warp = (size_t)6 * words * 4 + (size_t)seg_cap * 2;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1153,7 +1108,7 @@ int hfx_lists_generate_seg(const DevDB &db, const int32_t *cover, int64_t npep1,
         }
     }
     f<<<sms * (per > 0 ? per : 1), nw * 32, nw * per_warp, st>>>(db, cover, npep1, nbins, lstart, lists, list_len,
-                                                                 list_cap, stats, err);
+                                                                 seg_cap, stats, err);
     return (int)cudaGetLastError();
 }
 

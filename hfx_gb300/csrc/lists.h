@@ -24,8 +24,8 @@ int hfx_lists_generate(const hfx::DevDB &db, const int32_t *cover, int64_t npep1
 // peptide at kLevels * lstart[p] holding segments 1..zmax of entries
 // bin << 3 | code; list_len[z-1][p] = entries of segments 1..z.
 int hfx_lists_generate_seg(const hfx::DevDB &db, const int32_t *cover, int64_t npep1, int32_t nbins,
-                           const uint32_t *lstart, uint16_t *lists, uint16_t *list_len, int32_t list_cap, int fastdiv,
-                           unsigned long long *stats, uint32_t *err, cudaStream_t st);
+                           const uint32_t *lstart, uint16_t *lists, uint16_t *list_len, int32_t max_ladder,
+                           int fastdiv, unsigned long long *stats, uint32_t *err, cudaStream_t st);
 // FP32 rescoring of kept unmodified candidates from segment lists, in the
 // canonical order.
 int hfx_rescore_seglists(const uint16_t *lists, const uint32_t *lstart, const uint16_t *list_len, uint32_t num_pep,

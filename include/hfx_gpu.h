@@ -108,6 +108,17 @@ int32_t hfx_search_counters(hfx_ctx *ctx, uint64_t *out8, int32_t reset);
  * static modifications (Config.hs:204-218), mono: aa-mass-type.
  * proline_rule / min_len / max_len extend the reference digest (its rule 1
  * ignores P and it has no length filter; 0 = off). */
+/* The same digest on the device (new; the reference digests on the host,
+ * Fragment.hs:197-233, 363-405): every residue that starts a piece walks
+ * it, every piece start walks its joins, the kept fragments are placed by a
+ * scan of their counts, so the output equals hfx_digest's element for
+ * element (order, masses, tc, tn).  Host buffers in and out; r == NULL
+ * returns the count only.  Returns the fragment count, -1 on bad arguments
+ * or a CUDA failure (hfx_last_error says which), -2 when cap is too small.
+ * hfx_build_db digests with it. */
+int64_t hfx_digest_gpu(hfx_ctx *ctx, const uint8_t *seq, const uint32_t *seg, int32_t nprot, const float *mt26,
+                       int32_t rule, int32_t missed, float min_mass, float max_mass, int32_t proline_rule,
+                       int32_t min_len, int32_t max_len, float *r, uint32_t *tc, uint32_t *tn, int64_t cap);
 int32_t hfx_build_db(hfx_ctx *ctx, const uint8_t *seq, const uint32_t *seg, int32_t nprot,
                      const float *static_add26, int32_t mono, int32_t rule, int32_t missed,
                      float min_mass, float max_mass, int32_t proline_rule, int32_t min_len,

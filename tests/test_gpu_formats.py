@@ -98,3 +98,45 @@ def test_index_file(direct, tmp_path):
         _same(eng.search(sub, hfx_gb300.default_params(top_n=10, batch_mode=1)), ref)
     finally:
         eng.close()
+
+
+@pytest.mark.parametrize("mono,rule,missed,pr,lo,hi", [(True, 1, 1, True, 6, 50), (True, 1, 2, False, 0, 0),
+                                                      (False, 2, 0, False, 0, 0), (True, 0, 0, False, 0, 0),
+                                                      (True, 13, 1, True, 3, 30), (True, 6, 3, True, 0, 0),
+                                                      (True, 8, 1, False, 7, 0), (True, 12, 2, False, 0, 20)])
+def test_device_digest_matches_oracle(gpulib, oracle, tiny, mono, rule, missed, pr, lo, hi):
+    """The database digest on the device (hfx_digest_gpu, used by
+    hfx_build_db) equals the oracle's restatement of makeSeqDB's digest
+    element for element: order, FP32 masses, tc and tn."""
+    import hfx_gb300
+    prot, _, _ = tiny
+    mt = oracle.mass_table(mono, synth.static_mods())
+    eng = hfx_gb300.Engine(0)
+    try:
+        a = eng.digest(prot.seq, prot.seg, mt, rule=rule, missed=missed, proline_rule=pr, min_len=lo, max_len=hi)
+        b = oracle.digest(prot.seq, prot.seg, mt, rule=rule, missed=missed, proline_rule=pr, min_len=lo, max_len=hi)
+        assert len(a[0]) == len(b[0]) > 0
+        for x, y in zip(a, b):
+            assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+    finally:
+        eng.close()
+
+
+def test_device_digest_edges(gpulib, oracle):
+    """Empty proteins, a protein of one residue, cleavage at the last residue
+    and proline after the cleavage site."""
+    import hfx_gb300
+    seqs = [b"", b"K", b"PEPTIDEK", b"AKPRKRP", b"", b"MKWVTFISLLLLFSSAYSRGVFRRDTHK", b"R"]
+    seq = np.frombuffer(b"".join(seqs), np.uint8).copy()
+    seg = np.cumsum([0] + [len(x) for x in seqs]).astype(np.uint32)
+    mt = oracle.mass_table(True, synth.static_mods())
+    eng = hfx_gb300.Engine(0)
+    try:
+        for pr in (False, True):
+            for missed in (0, 1, 2):
+                a = eng.digest(seq, seg, mt, rule=1, missed=missed, proline_rule=pr, min_mass=0.0, max_mass=1e6)
+                b = oracle.digest(seq, seg, mt, rule=1, missed=missed, proline_rule=pr, min_mass=0.0, max_mass=1e6)
+                for x, y in zip(a, b):
+                    assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (pr, missed)
+    finally:
+        eng.close()
