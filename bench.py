@@ -81,6 +81,8 @@ def _args():
     ap.add_argument("--group-size", type=int, default=0, help="spectra per batched work item (0 = default)")
     ap.add_argument("--chunk", type=int, default=0, help="candidates per batched work item (0 = default)")
     ap.add_argument("--no-graph", action="store_true", help="eager launches instead of CUDA-graph replays")
+    ap.add_argument("--evalues", action="store_true",
+                    help="also time hfx_search_evalues (the search plus every pair's FP32 score and the fits)")
     ap.add_argument("--shard", action="store_true",
                     help="N > 1: split ONE batch across the ranks by candidate counts (strong scaling) instead of "
                          "one batch per rank (weak scaling)")
@@ -631,6 +633,35 @@ def main():
     }
     if strong:
         line["config"]["shard"] = f"one batch split by candidate counts; rank 0 spectra {shard_range}"
+    if a.evalues:
+        # the search with E-values (eager), against the same search without
+        pe = hfx_gb300.default_params(top_n=cfg["top_n"], precision=prec, batch_mode=1, rescore_k=rk,
+                                      group_size=p.group_size, chunk=p.chunk, **_pkw(cfg))
+        oe = dict(out, ev=torch.empty((ns, tn_), dtype=torch.float64, device=d),
+                  fit=torch.empty((ns, 3), dtype=torch.float64, device=d))
+        eng.search_evalues(dev, pe, oe)
+        torch.cuda.synchronize()
+        n_e = max(1, min(3, a.steps))
+        t_ev = t_plain = 0.0
+        for _ in range(n_e):
+            for which in (0, 1):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                if which:
+                    eng.search_evalues(dev, pe, oe)
+                else:
+                    eng.search_device(dev, pe, out)
+                e1.record(stream)
+                e1.synchronize()
+                if which:
+                    t_ev += e0.elapsed_time(e1)
+                else:
+                    t_plain += e0.elapsed_time(e1)
+        fitted = oe["fit"][:, 2].cpu().numpy()
+        line["evalues"] = {"ms_per_search": t_ev / n_e, "ms_search_alone": t_plain / n_e,
+                           "ratio": t_ev / max(1e-9, t_plain), "spectra_with_fit": float(np.mean(fitted >= 2)),
+                           "launch": "eager"}
     if plain is not None:
         line["plain_fp32"] = plain
     if rank == 0 and not a.no_cpu:

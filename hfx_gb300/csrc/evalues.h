@@ -10,12 +10,11 @@
 int hfx_evalue_offsets(const uint32_t *wb, const uint32_t *we, int plain, const unsigned long long *isoforms,
                        int32_t ns, uint64_t *size, uint64_t *off, uint64_t *end, unsigned long long *cursor,
                        cudaStream_t st);
-// Every spectrum's scores sorted ascending (segmented).
-int hfx_evalue_sort(const float *scores, float *sorted, uint64_t total, const uint64_t *off, const uint64_t *end,
-                    int32_t ns, cudaStream_t st);
-// fit[s] = (alpha, beta, histogram points) of spectrum s.
-int hfx_evalue_fit(const float *sorted, const uint64_t *off, const uint64_t *size, int32_t ns, int32_t bin_width,
-                   float cutoff_perc, double *fit, cudaStream_t st);
+// fit[s] = (alpha, beta, histogram points) of spectrum s, from its unsorted
+// scores scores[off[s] .. off[s] + size[s]) (order statistics by radix
+// select, histogram in shared memory).
+int hfx_evalue_select_fit(const float *scores, const uint64_t *off, const uint64_t *size, int32_t ns,
+                          int32_t bin_width, float cutoff_perc, double *fit, cudaStream_t st);
 // ev[s][i] = 10 ** (alpha + beta * out_s[s][i] / 10000) (NaN for empty slots).
 int hfx_evalue_apply(const float *out_s, const uint64_t *out_k, const double *fit, int32_t ns, int32_t topn,
                      double *ev, cudaStream_t st);

@@ -1348,8 +1348,6 @@ int32_t hfx_search_evalues(hfx_ctx *ctx, const hfx_search_params *p, const float
     HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
     float *sink = ctx->buf<float>("e_sink", total + 1, e);
     if (e) return cuda_fail(ctx, e, "alloc E-value scores");
-    float *sorted = ctx->buf<float>("e_sorted", total + 1, e);
-    if (e) return cuda_fail(ctx, e, "alloc E-value scores");
     // re-plan with FP32 groups of 4 over the search's workspace
     BatchedWs ws;
     ws.hist = ctx->buf<uint32_t>("b_hist", kBucketCount + 1, e);
@@ -1439,8 +1437,7 @@ int32_t hfx_search_evalues(hfx_ctx *ctx, const hfx_search_params *p, const float
             if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_mods (all pairs)");
         }
     }
-    rc = hfx_evalue_sort(sink, sorted, total, soff, send, ns, ctx->stream);
-    if (!rc) rc = hfx_evalue_fit(sorted, soff, size, ns, bin_width, cutoff_perc, out_fit, ctx->stream);
+    rc = hfx_evalue_select_fit(sink, soff, size, ns, bin_width, cutoff_perc, out_fit, ctx->stream);
     if (!rc) rc = hfx_evalue_apply(out_s, out_k, out_fit, ns, p->top_n, out_ev, ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "E-values");
     return search_finish(ctx);
