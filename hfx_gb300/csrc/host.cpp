@@ -206,6 +206,13 @@ struct hfx_ctx {
         for (const auto &kv : ws) t += kv.second.n;
         return t;
     }
+    // Frees a workspace (one-time scratch such as the digest's).
+    void drop(const char *name) {
+        auto it = ws.find(name);
+        if (it == ws.end()) return;
+        it->second.release();
+        ws.erase(it);
+    }
     template <typename T> T *buf(const char *name, size_t count, cudaError_t &e) {
         DBuf &b = ws[name];
         const size_t want = count * sizeof(T) + 16;
@@ -1101,10 +1108,30 @@ uint32_t rule_mask(int rule) {
 // The digest on the device (digest.cu): counts, then, with `r`, resizes
 // the three host vectors and fills them.  Returns the fragment count, -1 for
 // bad arguments or -3 for a CUDA failure (ctx->err says which).
+int64_t digest_device_run(hfx_ctx *ctx, const uint8_t *seq, const uint32_t *seg, int32_t nprot, const float *mt26,
+                          int32_t rule, int32_t missed, float min_mass, float max_mass, int32_t proline_rule,
+                          int32_t min_len, int32_t max_len, std::vector<float> *r, std::vector<uint32_t> *tc,
+                          std::vector<uint32_t> *tn);
+
+// The digest's scratch is freed when it returns (a one-time step of the
+// database build, not a search workspace).
 int64_t digest_device(hfx_ctx *ctx, const uint8_t *seq, const uint32_t *seg, int32_t nprot, const float *mt26,
                       int32_t rule, int32_t missed, float min_mass, float max_mass, int32_t proline_rule,
                       int32_t min_len, int32_t max_len, std::vector<float> *r, std::vector<uint32_t> *tc,
                       std::vector<uint32_t> *tn) {
+    const int64_t n = digest_device_run(ctx, seq, seg, nprot, mt26, rule, missed, min_mass, max_mass, proline_rule,
+                                        min_len, max_len, r, tc, tn);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (const char *name : {"dg_seq", "dg_seg", "dg_pm", "dg_ptn", "dg_plen", "dg_pnext", "dg_cnt", "dg_incl",
+                             "dg_partial", "dg_r", "dg_tc", "dg_tn"})
+        ctx->drop(name);
+    return n;
+}
+
+int64_t digest_device_run(hfx_ctx *ctx, const uint8_t *seq, const uint32_t *seg, int32_t nprot, const float *mt26,
+                          int32_t rule, int32_t missed, float min_mass, float max_mass, int32_t proline_rule,
+                          int32_t min_len, int32_t max_len, std::vector<float> *r, std::vector<uint32_t> *tc,
+                          std::vector<uint32_t> *tn) {
     const uint32_t nres = nprot > 0 ? seg[nprot] : 0u;
     for (int32_t p = 0; p < nprot; ++p)
         if (seg[p + 1] < seg[p]) return fail(ctx, HFX_ERR_ARG, "protein offsets must not decrease"), -1;
