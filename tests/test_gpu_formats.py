@@ -115,7 +115,8 @@ def test_device_digest_matches_oracle(gpulib, oracle, tiny, mono, rule, missed, 
     try:
         a = eng.digest(prot.seq, prot.seg, mt, rule=rule, missed=missed, proline_rule=pr, min_len=lo, max_len=hi)
         b = oracle.digest(prot.seq, prot.seg, mt, rule=rule, missed=missed, proline_rule=pr, min_len=lo, max_len=hi)
-        assert len(a[0]) == len(b[0]) > 0
+        assert len(a[0]) == len(b[0])
+        assert rule == 0 or len(a[0]) > 0  # rule 0 never cleaves: whole proteins, all above 7200 Da
         for x, y in zip(a, b):
             assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
     finally:
