@@ -378,34 +378,10 @@ __device__ __forceinline__ uint16_t level_weight_f16(uint32_t lvl) {
     return (uint16_t)(r & 0xFFFFu);
 }
 
-// Weight of a segment-list entry's code (lists.cu): 0, 10, 25, 50, 15, 40,
-// 25, 0 for codes 0..7, the BF16 / FP16 bits of each picked byte by byte
-// (two byte permutes over 8-byte tables of the high and low bytes).
-__device__ __forceinline__ uint16_t seg_weight_bf16(uint32_t code) {
-    uint32_t hi, lo;
-    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(hi) : "r"(0x42414100u), "r"(0x00414241u), "r"(code));
-    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(lo) : "r"(0x48C82000u), "r"(0x00C82070u), "r"(code));
-    return (uint16_t)(((hi & 0xFFu) << 8) | (lo & 0xFFu));
-}
-__device__ __forceinline__ uint16_t seg_weight_f16(uint32_t code) {
-    uint32_t hi, lo;
-    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(hi) : "r"(0x524E4900u), "r"(0x004E514Bu), "r"(code));
-    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(lo) : "r"(0x40400000u), "r"(0x00400080u), "r"(code));
-    return (uint16_t)(((hi & 0xFFu) << 8) | (lo & 0xFFu));
-}
-__device__ __forceinline__ float seg_weight(uint32_t code) {
-    return __uint_as_float((uint32_t)seg_weight_bf16(code) << 16);
-}
-
 template <typename T, int G>
 struct TileFma {
     __device__ __forceinline__ static void fma(const T *t, uint32_t bin, uint32_t lvl, float (&acc)[G]) {
-        fma_w(t, bin, level_weight(lvl), acc);
-    }
-    __device__ __forceinline__ static void fma_code(const T *t, uint32_t bin, uint32_t code, float (&acc)[G]) {
-        fma_w(t, bin, seg_weight(code), acc);
-    }
-    __device__ __forceinline__ static void fma_w(const T *t, uint32_t bin, float w, float (&acc)[G]) {
+        const float w = level_weight(lvl);
         float x[G];
         TileLoad<T, G>::load(t, bin, x);
 #pragma unroll
@@ -437,22 +413,11 @@ template <> struct TileFma<__nv_bfloat16, 8> {
         const uint16_t w = level_weight_bf16(lvl);
         HFX_MIXED_FMA8("bf16");
     }
-    __device__ __forceinline__ static void fma_code(const __nv_bfloat16 *t, uint32_t bin, uint32_t code,
-                                                    float (&acc)[8]) {
-        const uint4 v = *reinterpret_cast<const uint4 *>(t + (size_t)bin * 8);
-        const uint16_t w = seg_weight_bf16(code);
-        HFX_MIXED_FMA8("bf16");
-    }
 };
 template <> struct TileFma<__half, 8> {
     __device__ __forceinline__ static void fma(const __half *t, uint32_t bin, uint32_t lvl, float (&acc)[8]) {
         const uint4 v = *reinterpret_cast<const uint4 *>(t + (size_t)bin * 8);
         const uint16_t w = level_weight_f16(lvl);
-        HFX_MIXED_FMA8("f16");
-    }
-    __device__ __forceinline__ static void fma_code(const __half *t, uint32_t bin, uint32_t code, float (&acc)[8]) {
-        const uint4 v = *reinterpret_cast<const uint4 *>(t + (size_t)bin * 8);
-        const uint16_t w = seg_weight_f16(code);
         HFX_MIXED_FMA8("f16");
     }
 };
@@ -497,22 +462,11 @@ template <> struct TileFma<__nv_bfloat16, 4> {
         const uint16_t w = level_weight_bf16(lvl);
         HFX_MIXED_FMA4("bf16");
     }
-    __device__ __forceinline__ static void fma_code(const __nv_bfloat16 *t, uint32_t bin, uint32_t code,
-                                                    float (&acc)[4]) {
-        const uint2 v = *reinterpret_cast<const uint2 *>(t + (size_t)bin * 4);
-        const uint16_t w = seg_weight_bf16(code);
-        HFX_MIXED_FMA4("bf16");
-    }
 };
 template <> struct TileFma<__half, 4> {
     __device__ __forceinline__ static void fma(const __half *t, uint32_t bin, uint32_t lvl, float (&acc)[4]) {
         const uint2 v = *reinterpret_cast<const uint2 *>(t + (size_t)bin * 4);
         const uint16_t w = level_weight_f16(lvl);
-        HFX_MIXED_FMA4("f16");
-    }
-    __device__ __forceinline__ static void fma_code(const __half *t, uint32_t bin, uint32_t code, float (&acc)[4]) {
-        const uint2 v = *reinterpret_cast<const uint2 *>(t + (size_t)bin * 4);
-        const uint16_t w = seg_weight_f16(code);
         HFX_MIXED_FMA4("f16");
     }
 };

@@ -198,9 +198,6 @@ struct hfx_ctx {
     // that would take the context's total beyond it is not allocated and the
     // call reports HFX_ERR_OOM, as when cudaMalloc itself fails.
     size_t ws_limit = 0;
-    // whether the last batched search left segment lists (else per-level
-    // lists) in "l_lists"
-    bool last_seg_lists = false;
     size_t ws_total() const {
         size_t t = 0;
         for (const auto &kv : ws) t += kv.second.n;
@@ -592,11 +589,6 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     const void *lists_out = nullptr;  // the step's lists, which the FP32 rescoring reads
     const uint16_t *llen_out = nullptr;
     uint64_t total10_out = 0;
-    // the BF16/FP16 two-per-warp scorer over shared tiles reads segment lists
-    // (one slot per peptide for all levels); FP32, 16-spectrum groups, long
-    // rows and the E-value search keep the per-level lists
-    const bool seg_lists = elem_kind != 0 && G <= 8 && !long_rows;
-    ctx->last_seg_lists = false;
     const int32_t list_cap = (int32_t)std::min<uint64_t>(40ull * ctx->max_ladder, kMaxListLen);
     const bool mods_on = p->search_mods != 0 && ctx->num_mod > 0;
     ctx->stage_begin(HFX_STAGE_PACK);
@@ -645,17 +637,11 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
                                          (uint32_t *)lists, llen, p->fastdiv,
                                          p->ion_bins_custom ? p->bin_width : 0.0f, stats,
                                          ctx->d_err.as<uint32_t>(), ctx->stream);
-        else if (!rc && seg_lists)
-            rc = hfx_lists_generate_seg(db, cover, npep1, (int32_t)std::min<int64_t>(stride, kMaxWords * 32),
-                                        ctx->d_lstart.as<uint32_t>(), (uint16_t *)lists, llen,
-                                        (int32_t)ctx->max_ladder, p->fastdiv, stats, ctx->d_err.as<uint32_t>(),
-                                        ctx->stream);
         else if (!rc)
             rc = hfx_lists_generate(db, cover, npep1, (int32_t)std::min<int64_t>(stride, kMaxWords * 32),
                                     ctx->d_lstart.as<uint32_t>(), total10, (uint16_t *)lists, llen, list_cap,
                                     p->fastdiv, stats, ctx->d_err.as<uint32_t>(), ctx->stream);
         if (rc) return cuda_fail(ctx, (cudaError_t)rc, "ion lists");
-        ctx->last_seg_lists = seg_lists;
         ctx->stage_end(HFX_STAGE_LISTS, 5, 0);
         ctx->stage_begin(HFX_STAGE_SCORE);
         rc = hfx_lists_score(lists, long_rows, ctx->d_lstart.as<uint32_t>(), total10, llen, (uint32_t)ctx->num_pep,
@@ -748,12 +734,7 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
         ctx->stage_begin(HFX_STAGE_RESCORE);
         // unmodified keys only: rescore from the step's lists; modified keys
         // (and the fused mode, which keeps no lists) rebuild their ions
-        if (lists_out && !mods_on && seg_lists)
-            rc = hfx_rescore_seglists((const uint16_t *)lists_out, ctx->d_lstart.as<uint32_t>(), llen_out,
-                                      (uint32_t)ctx->num_pep, ctx->d_idx.as<uint32_t>(), rows, stride, meta, kk, ns,
-                                      K, p->top_n, list_cap, out_s, out_k, out_pep, ctx->d_err.as<uint32_t>(),
-                                      ctx->stream);
-        else if (lists_out && (long_rows || !mods_on))
+        if (lists_out && (long_rows || !mods_on))
             rc = hfx_rescore_lists(lists_out, long_rows, ctx->d_lstart.as<uint32_t>(), total10_out, llen_out,
                                    (uint32_t)ctx->num_pep, ctx->d_idx.as<uint32_t>(), rows, stride, meta, kk, ns, K,
                                    p->top_n, out_s, out_k, out_pep, ctx->d_err.as<uint32_t>(), ctx->stream);
@@ -1407,21 +1388,8 @@ int32_t hfx_search_evalues(hfx_ctx *ctx, const hfx_search_params *p, const float
         const uint64_t total10 = ctx->list_units;
         const void *lists = long_rows ? (const void *)ctx->buf<uint32_t>("l_lists32", total10 * 10 + 64, e)
                                       : (const void *)ctx->buf<uint16_t>("l_lists", total10 * 10 + 64, e);
-        uint16_t *llen = ctx->buf<uint16_t>("l_len", (size_t)kLevels * ctx->num_pep, e);
+        const uint16_t *llen = ctx->buf<uint16_t>("l_len", (size_t)kLevels * ctx->num_pep, e);
         if (e) return cuda_fail(ctx, e, "lists");
-        if (ctx->last_seg_lists) {
-            // the search's BF16/FP16 pass left segment lists: the FP32 scores
-            // of every pair need the per-level lists of the same candidates
-            const int64_t npep1 = (int64_t)ctx->num_pep + 1;
-            const int32_t *cover = ctx->buf<int32_t>("l_cover", (size_t)kLevels * npep1, e);
-            if (e) return cuda_fail(ctx, e, "lists");
-            rc = hfx_lists_generate(ctx->devdb(), cover, npep1, (int32_t)std::min<int64_t>(stride, kMaxWords * 32),
-                                    ctx->d_lstart.as<uint32_t>(), total10, (uint16_t *)lists, llen,
-                                    (int32_t)std::min<uint64_t>(40ull * ctx->max_ladder, kMaxListLen), p->fastdiv,
-                                    nullptr, ctx->d_err.as<uint32_t>(), ctx->stream);
-            if (rc) return cuda_fail(ctx, (cudaError_t)rc, "ion lists (all pairs)");
-            ctx->last_seg_lists = false;
-        }
         rc = hfx_lists_score(lists, long_rows, ctx->d_lstart.as<uint32_t>(), total10, llen, (uint32_t)ctx->num_pep,
                              0, stride, wb, we, ws, tiles, G, K, 0, ps, pk, nullptr, ctx->d_err.as<uint32_t>(),
                              ctx->stream, sink, soff);

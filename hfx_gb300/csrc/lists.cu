@@ -238,293 +238,6 @@ __global__ void __launch_bounds__(256) k_gen_lists(DevDB db, const int32_t *__re
     }
 }
 
-// ---- segment lists: one slot per peptide for every charge level ----
-//
-// The level-z list is the level-(z-1) list plus the charge-z ions, with the
-// larger weight where they meet.  So instead of one list per needed level,
-// one slot per peptide holds segments 1..zmax back to back: segment z lists,
-// in ascending bin order, the bins whose weight changes at level z (a new
-// bin, or a bin whose weight rises), each with the weight it adds.  A level-z
-// candidate streams the slot's prefix [0, len_z): the sum over its entries of
-// added weight x row value equals the level-z list's sum in real arithmetic.
-// The FP32 order differs from the canonical one, which the BF16/FP16 pass
-// allows (its scores only pick the kept candidates, which are rescored in FP32
-// in the canonical order).  Every ion bin is emitted, compacted and written
-// once per peptide instead of once per level that contains it.
-//
-// Entries: bin << 3 | code, code = (level before, level after) of the bin:
-// 1: 0->1 (+10), 2: 0->2 (+25), 3: 0->3 (+50), 4: 1->2 (+15), 5: 1->3 (+40),
-// 6: 2->3 (+25); 0 is a pad entry of weight 0.  Levels 1, 2, 3 are the
-// reference's intensities 10, 25, 50 (ion_series.cu:78-123), max-deduped as
-// its atomicMax into the dense row (ion_series.cu:71-75).
-// Offset of a peptide's segment slot: kLevels x lstart[p] (slots of
-// kLevels x round8(10 (tn - tc)) entries, 16-byte aligned).
-__device__ __forceinline__ uint64_t seg_offset(const uint32_t *__restrict__ lstart, uint32_t p) {
-    return (uint64_t)kLevels * lstart[p];
-}
-
-// Words of a level (cumulative over charges 1..z): any ion, weight >= 25,
-// weight 50.
-struct SegWords {
-    uint32_t a, h, t;
-};
-
-// The code bits of every bit position of a word whose level goes from
-// `p` to `c` (positions whose level does not change are not emitted):
-// bit 0 for codes 1, 3, 5; bit 1 for 2, 3, 6; bit 2 for 4, 5, 6.
-struct SegCodes {
-    uint32_t changed, c0, c1, c2;
-};
-__device__ __forceinline__ SegCodes seg_codes(const SegWords &p, const SegWords &c) {
-    const uint32_t p0 = ~p.a, p1 = p.a & ~p.h, p2 = p.h & ~p.t;  // level before: 0, 1, 2
-    const uint32_t a1 = c.a & ~c.h, a2 = c.h & ~c.t, a3 = c.t;  // level after: 1, 2, 3
-    SegCodes r;
-    r.changed = (c.a ^ p.a) | (c.h ^ p.h) | (c.t ^ p.t);
-    r.c0 = (p0 & (a1 | a3)) | (p1 & a3);
-    r.c1 = (p0 & (a2 | a3)) | (p2 & a3);
-    r.c2 = (p1 & (a2 | a3)) | (p2 & a3);
-    return r;
-}
-
-// Segment z of a peptide: the bins whose level changes when the charge-z
-// planes `cur` join the planes of levels < z (`cum`), over the words [wr)
-// where `cur` has bits, in ascending bin order.  Warp-cooperative: lane l
-// takes ceil(words / 32) consecutive words, one scan places every lane's
-// entries.  Folds `cur` into `cum` and clears `cur`.  Returns the entries
-// (may exceed cap; entries beyond cap are dropped).
-__device__ __forceinline__ int compact_segment(const Planes &cum, const Planes &cur, WordRange wr, uint16_t *list,
-                                               int cap) {
-    const int lane = threadIdx.x & 31;
-    const int nwords = wr.hi - wr.lo;
-    if (nwords <= 0) return 0;
-    const int k = (nwords + 31) >> 5;
-    const int w0 = wr.lo + lane * k;
-    const int w1 = min(w0 + k, wr.hi);
-    int cnt = 0;
-    for (int w = w0; w < w1; ++w) {
-        const uint32_t ph = cum.H[w], ch = cur.H[w];
-        const uint32_t pa = cum.A[w] | ph, pt = cum.T[w];
-        cnt += __popc(((pa | cur.A[w] | ch) ^ pa) | ((ph | ch) ^ ph) | ((pt | cur.T[w]) ^ pt));
-    }
-    const int incl = warp_incl_scan(cnt);
-    int pos = incl - cnt;
-    for (int w = w0; w < w1; ++w) {
-        const uint32_t cA = cur.A[w], cH = cur.H[w], cT = cur.T[w];
-        const uint32_t pA = cum.A[w], pH = cum.H[w], pT = cum.T[w];
-        const SegWords pw{pA | pH, pH, pT};
-        const SegWords cw{pA | pH | cA | cH, pH | cH, pT | cT};
-        cum.A[w] = pA | cA;
-        cum.H[w] = pH | cH;
-        cum.T[w] = pT | cT;
-        cur.A[w] = 0u;
-        cur.H[w] = 0u;
-        cur.T[w] = 0u;
-        const SegCodes sc = seg_codes(pw, cw);
-        const uint32_t bin0 = (uint32_t)w << 8;  // (w * 32) << 3
-        uint32_t chg = sc.changed;
-        while (chg) {
-            const int b = __ffs(chg) - 1;
-            chg &= chg - 1u;
-            const uint32_t code = ((sc.c0 >> b) & 1u) | (((sc.c1 >> b) & 1u) << 1) | (((sc.c2 >> b) & 1u) << 2);
-            if (pos < cap) list[pos] = (uint16_t)(bin0 + ((uint32_t)b << 3) + code);
-            ++pos;
-        }
-    }
-    const int n = __shfl_sync(kFullMask, incl, 31);
-    __syncwarp();
-    return n;
-}
-
-// One warp per candidate peptide that some spectrum of the batch needs: for
-// z = 1..zmax (zmax = the highest level needed) the charge-z ions go into
-// the `cur` planes (the reference warp scan's b-ladder, build_planes_range),
-// segment z is compacted against the `cum` planes of the lower levels and
-// appended to the peptide's slot; list_len[z-1][p] = entries of segments
-// 1..z.  Segments are copied out by 2-byte lanes (64 contiguous bytes per
-// warp store): they start anywhere in the slot.
-template <bool FastDiv>
-__global__ void __launch_bounds__(256) k_gen_seglists(DevDB db, const int32_t *__restrict__ cover, int64_t npep1,
-                                                      int32_t nbins, const uint32_t *__restrict__ lstart,
-                                                      uint16_t *__restrict__ lists, uint16_t *__restrict__ list_len,
-                                                      int32_t seg_cap, unsigned long long *__restrict__ stats,
-                                                      uint32_t *__restrict__ err) {
-    extern __shared__ __align__(16) uint8_t smem[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int32_t words = (nbins + 31) / 32;
-    uint32_t *pw = reinterpret_cast<uint32_t *>(smem) + (size_t)warp * 6 * words;
-    uint16_t *stage = reinterpret_cast<uint16_t *>(reinterpret_cast<uint32_t *>(smem) + (size_t)nw * 6 * words) +
-                      (size_t)warp * seg_cap;
-    __shared__ unsigned long long s_stats[3];
-    if (threadIdx.x < 3) s_stats[threadIdx.x] = 0ull;
-    for (int32_t i = lane; i < 6 * words; i += 32) pw[i] = 0u;
-    __syncthreads();
-    const Planes cum{pw, pw + words, pw + 2 * words};
-    const Planes cur{pw + 3 * words, pw + 4 * words, pw + 5 * words};
-    const float mt_lane = db.mt[lane];
-    unsigned long long my_lists = 0, my_entries = 0, my_res = 0;
-    for (int64_t t = (int64_t)blockIdx.x * nw + warp; t < (int64_t)db.num_pep; t += (int64_t)gridDim.x * nw) {
-        const uint32_t p = (uint32_t)t;
-        uint32_t need = 0;
-        if (lane < kLevels && cover[(int64_t)lane * npep1 + p] > 0) need = 1u;
-        need = __ballot_sync(kFullMask, need) & ((1u << kLevels) - 1u);
-        if (!need) {
-            if (lane < kLevels) list_len[(size_t)lane * db.num_pep + p] = 0;
-            continue;
-        }
-        const int zmax = 32 - __clz(need);
-        const uint32_t tc = db.tc_sorted[p], tn = db.tn_sorted[p];
-        const float r = db.r_sorted[p];
-        my_res += tn > tc ? tn - tc : 0u;
-        uint16_t *slot = lists + seg_offset(lstart, p);
-        const uint32_t slot_cap = (uint32_t)kLevels * (((tn > tc ? tn - tc : 0u) * 10u + 7u) & ~7u);
-        uint32_t base = 0;
-        WordRange all{0x7FFFFFFF, 0};
-        for (int z = 1; z <= zmax; ++z) {
-            const WordRange wr = build_planes_range<FastDiv>(cur, db.ions, tc, tn, r, z, z, nbins, mt_lane, NoMods{});
-            if (wr.hi > wr.lo) {
-                all.lo = min(all.lo, wr.lo);
-                all.hi = max(all.hi, wr.hi);
-            }
-            int n = compact_segment(cum, cur, wr, stage, seg_cap);
-            if (n > seg_cap || base + (uint32_t)n > slot_cap) {
-                if (lane == 0) atomicOr(err, kErrListOverflow);
-                n = min(n, seg_cap);
-                n = (int)min((uint32_t)n, slot_cap - base);
-            }
-            for (int i = lane; i < n; i += 32) slot[base + i] = stage[i];
-            base += (uint32_t)n;
-            if (lane == 0) list_len[(size_t)(z - 1) * db.num_pep + p] = (uint16_t)base;
-            __syncwarp();
-        }
-        if (lane >= zmax && lane < kLevels) list_len[(size_t)lane * db.num_pep + p] = 0;
-        // the cumulative planes, back to zero
-        for (int32_t w = all.lo + lane; w < all.hi; w += 32) {
-            cum.A[w] = 0u;
-            cum.H[w] = 0u;
-            cum.T[w] = 0u;
-        }
-        __syncwarp();
-        my_lists += (unsigned long long)__popc(need);
-        my_entries += (unsigned long long)base;
-    }
-    if (stats) {
-        if (lane == 0) {
-            atomicAdd(&s_stats[0], my_lists);
-            atomicAdd(&s_stats[1], my_entries);
-            atomicAdd(&s_stats[2], my_res);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            atomicAdd(&stats[0], s_stats[0]);
-            atomicAdd(&stats[1], s_stats[1]);
-            atomicAdd(&stats[6], s_stats[2]);
-        }
-    }
-}
-
-// FP32 rescoring of kept unmodified candidates from their segment lists: a
-// warp per kept candidate rebuilds the level-z bit planes from segments
-// 1..z (a bin's final level is the level after its last change), compacts
-// them into the ascending distinct-bin list and gathers the FP32 row in the
-// canonical order (entry i by lane i % 32, XOR butterfly).  One CTA per
-// spectrum; the CTA orders the kept candidates and keeps the top-N.
-__global__ void __launch_bounds__(256) k_rescore_seglists(const uint16_t *__restrict__ lists,
-                                                          const uint32_t *__restrict__ lstart,
-                                                          const uint16_t *__restrict__ list_len, uint32_t num_pep,
-                                                          const uint32_t *__restrict__ idx_sorted,
-                                                          const float *__restrict__ rows32, int64_t stride,
-                                                          const SpecMeta *__restrict__ meta,
-                                                          const uint64_t *__restrict__ kept_k, int32_t K,
-                                                          int32_t topn, int32_t words, int32_t list_cap,
-                                                          float *__restrict__ out_s, uint64_t *__restrict__ out_k,
-                                                          uint32_t *__restrict__ out_pep,
-                                                          uint32_t *__restrict__ err) {
-    extern __shared__ __align__(16) uint8_t smem[];
-    __shared__ float res_s[kMaxKept];
-    __shared__ uint64_t res_k[kMaxKept];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    uint32_t *pw = reinterpret_cast<uint32_t *>(smem) + (size_t)warp * 3 * words;
-    uint16_t *list = reinterpret_cast<uint16_t *>(reinterpret_cast<uint32_t *>(smem) + (size_t)nw * 3 * words) +
-                     (size_t)warp * list_cap;
-    for (int32_t i = lane; i < 3 * words; i += 32) pw[i] = 0u;
-    __syncwarp();
-    const Planes pl{pw, pw + words, pw + 2 * words};
-    const int32_t s = blockIdx.x;
-    const SpecMeta m = meta[s];
-    const float *row = rows32 + (size_t)s * stride;
-    const int z = m.charges_plain;
-    const int32_t nbins = min((int32_t)m.len, words * 32);
-    for (int t = warp; t < K; t += nw) {
-        const uint64_t kk = kept_k[(size_t)s * K + t];
-        float sc = -INFINITY;
-        if (kk != ~0ull) {
-            float acc = 0.0f;
-            if (!(kk >> 63) && z >= 1 && z <= kLevels && kk < num_pep) {
-                const uint32_t p = (uint32_t)kk;
-                const int n = list_len[(size_t)(z - 1) * num_pep + p];
-                const uint16_t *lp = lists + seg_offset(lstart, p);
-                if (z == 1) {
-                    // segment 1 is the level-1 list itself (codes 1..3 are the levels)
-                    for (int i = lane; i < n; i += 32) {
-                        const uint32_t e = __ldg(lp + i);
-                        if ((int32_t)(e >> 3) < m.len)
-                            acc = __fmaf_rn(level_weight(e & 3u), __ldg(row + (e >> 3)), acc);
-                    }
-                } else {
-                    int32_t lo = 0x7FFFFFFF, hi = -1;
-                    for (int i = lane; i < n; i += 32) {
-                        const uint32_t e = __ldg(lp + i);
-                        const int32_t bin = (int32_t)(e >> 3);
-                        const uint32_t after = (0x3323210u >> (4u * (e & 7u))) & 0xFu;  // level after the change
-                        if (bin < nbins && after) {
-                            atomicOr(&pl.A[bin >> 5], 1u << (bin & 31));
-                            if (after >= 2u) atomicOr(&pl.H[bin >> 5], 1u << (bin & 31));
-                            if (after == 3u) atomicOr(&pl.T[bin >> 5], 1u << (bin & 31));
-                            lo = min(lo, bin);
-                            hi = max(hi, bin);
-                        }
-                    }
-                    __syncwarp();
-                    lo = __reduce_min_sync(kFullMask, lo);
-                    hi = __reduce_max_sync(kFullMask, hi);
-                    const WordRange wr = hi < 0 ? WordRange{0, 0} : WordRange{lo >> 5, (hi >> 5) + 1};
-                    int nl = compact_planes(pl, wr, true, list, list_cap);
-                    if (nl > list_cap) {
-                        if (lane == 0) atomicOr(err, kErrListOverflow);
-                        nl = list_cap;
-                    }
-                    for (int i = lane; i < nl; i += 32) {
-                        const uint32_t e = list[i];
-                        acc = __fmaf_rn(level_weight(e & 3u), __ldg(row + (e >> 2)), acc);
-                    }
-                    __syncwarp();
-                }
-            } else if (kk >> 63) {
-                if (lane == 0) atomicOr(err, kErrBounds);
-            }
-#pragma unroll
-            for (int o = 16; o >= 1; o >>= 1) acc = __fadd_rn(acc, __shfl_xor_sync(kFullMask, acc, o));
-            sc = acc;
-        }
-        if (lane == 0) {
-            res_s[t] = sc;
-            res_k[t] = kk;
-        }
-    }
-    __syncthreads();
-    if (warp == 0) {
-        WarpTopK tk;
-        tk.init();
-        for (int t = 0; t < K; ++t)
-            if (res_k[t] != ~0ull) tk.insert(res_s[t], res_k[t], topn);
-        if (lane < topn) {
-            out_s[(size_t)s * topn + lane] = tk.s;
-            out_k[(size_t)s * topn + lane] = tk.k;
-            out_pep[(size_t)s * topn + lane] = (tk.k != ~0ull && tk.k < num_pep) ? idx_sorted[tk.k] : ~0u;
-        }
-    }
-}
-
 // ---- long rows: 32-bit list entries built by sorting ----
 //
 // With ~10^5 bins per row the three bit planes no longer fit in shared
@@ -777,9 +490,6 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
               uint32_t *__restrict__ err) {
     static_assert(!kPair || G <= 8, "half-warp candidates take up to 8 spectra per group");
     constexpr int kW = kPair ? 16 : 32;  // lanes per candidate
-    // the two-per-warp pass over shared tiles streams segment lists (one slot
-    // per peptide, entries bin << 3 | code, not in ascending order overall)
-    constexpr bool kSeg = kPair && !kGlobal && std::is_same<E, uint16_t>::value;
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int hl = lane & (kW - 1), half = kPair ? lane >> 4 : 0;
@@ -867,7 +577,7 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
         // entry past a list's end: the zero bin `stride` of the shared tile
         // (beyond every group's bins, so it also ends the scan), or an
         // out-of-range bin for tiles in global memory
-        const uint32_t pad = kSeg ? 0u : (kGlobal ? 0xFFFFFFFFu : ((uint32_t)stride << 2));
+        const uint32_t pad = kGlobal ? 0xFFFFFFFFu : ((uint32_t)stride << 2);
         const int z = (int)gi.charges;
         const uint16_t *llen = list_len + (size_t)(z >= 1 ? z - 1 : 0) * num_pep;
         // Three-stage software pipeline over the warp's candidates: while
@@ -918,8 +628,7 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
             c.live = m.live;
             c.lp = lists;
             if (m.act && z >= 1) {
-                const uint64_t off = kSeg ? (uint64_t)kLevels * m.ls
-                                          : total10 * (uint64_t)(z * (z - 1) / 2) + (uint64_t)z * m.ls;
+                const uint64_t off = total10 * (uint64_t)(z * (z - 1) / 2) + (uint64_t)z * m.ls;
                 if (m.p >= num_pep || off + (uint64_t)c.n > list_total) {
                     if (hl == 0) atomicOr(err, kErrBounds);
                     c.n = 0;
@@ -957,20 +666,16 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
             for (int i0 = 0; i0 < nmax; i0 += 4 * kW) {
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    if constexpr (kSeg) {
-                        TileFma<T, G>::fma_code(tile, e[k] >> 3, e[k] & 7u, acc);  // zero beyond nb
-                    } else if constexpr (kGlobal) {
-                        const uint32_t bin = e[k] >> 2;
+                    const uint32_t bin = e[k] >> 2;
+                    if constexpr (kGlobal) {
                         if ((int32_t)bin < nb) TileFma<T, G>::fma(tile, bin, e[k] & 3u, acc);
                     } else {
-                        TileFma<T, G>::fma(tile, e[k] >> 2, e[k] & 3u, acc);  // zero beyond nb
+                        TileFma<T, G>::fma(tile, bin, e[k] & 3u, acc);  // zero beyond nb
                     }
                 }
-                if constexpr (!kSeg) {
-                    // lists ascend: once an entry lies beyond the tile, so do the rest
-                    const uint32_t last = __shfl_sync(kFullMask, e[3], (lane & ~(kW - 1)) | (kW - 1));
-                    if (__all_sync(kFullMask, (last >> 2) >= (uint32_t)nb)) break;
-                }
+                // lists ascend: once an entry lies beyond the tile, so do the rest
+                const uint32_t last = __shfl_sync(kFullMask, e[3], (lane & ~(kW - 1)) | (kW - 1));
+                if (__all_sync(kFullMask, (last >> 2) >= (uint32_t)nb)) break;
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     e[k] = f[k];
@@ -1078,55 +783,6 @@ int hfx_lists_generate(const DevDB &db, const int32_t *cover, int64_t npep1, int
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, nw * 32, smem);
     f<<<sms * (per > 0 ? per : 1), nw * 32, smem, st>>>(db, cover, npep1, nbins, lstart, total10, lists, list_len,
                                                         list_cap, stats, err);
-    return (int)cudaGetLastError();
-}
-
-int hfx_lists_generate_seg(const DevDB &db, const int32_t *cover, int64_t npep1, int32_t nbins,
-                           const uint32_t *lstart, uint16_t *lists, uint16_t *list_len, int32_t max_ladder,
-                           int fastdiv, unsigned long long *stats, uint32_t *err, cudaStream_t st) {
-    const int32_t words = (nbins + 31) / 32;
-    // one segment holds at most 10 ions per prefix of the longest ladder
-    const int32_t seg_cap = (std::max(32, std::min(10 * max_ladder, kMaxListLen)) + 7) & ~7;
-    // per warp: the cumulative and the current charge's bit planes and a
-    // staging segment; the CTA size (4, 6 or 8 warps) that keeps the most
-    // warps resident
-    const size_t per_warp = (size_t)6 * words * 4 + (size_t)seg_cap * 2;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    auto f = fastdiv ? k_gen_seglists<true> : k_gen_seglists<false>;
-    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(8 * per_warp));
-    if (e != cudaSuccess) return (int)e;
-    int nw = 8, per = 0, best = -1;
-    for (int cand : {8, 6, 4}) {
-        int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, cand * 32, cand * per_warp);
-        if (b * cand > best) {
-            best = b * cand;
-            nw = cand;
-            per = b;
-        }
-    }
-    f<<<sms * (per > 0 ? per : 1), nw * 32, nw * per_warp, st>>>(db, cover, npep1, nbins, lstart, lists, list_len,
-                                                                 seg_cap, stats, err);
-    return (int)cudaGetLastError();
-}
-
-int hfx_rescore_seglists(const uint16_t *lists, const uint32_t *lstart, const uint16_t *list_len, uint32_t num_pep,
-                         const uint32_t *idx_sorted, const float *rows32, int64_t stride, const SpecMeta *meta,
-                         const uint64_t *kept_k, int32_t nspec, int32_t K, int32_t topn, int32_t list_cap,
-                         float *out_s, uint64_t *out_k, uint32_t *out_pep, uint32_t *err, cudaStream_t st) {
-    if (nspec <= 0) return 0;
-    if (K > kMaxKept) return (int)cudaErrorInvalidValue;
-    const int nw = 8;
-    const int32_t words = (int32_t)((std::min<int64_t>(stride, (int64_t)kMaxWords * 32) + 31) / 32);
-    list_cap = (std::max(32, std::min(list_cap, kMaxListLen)) + 7) & ~7;
-    const size_t smem = (size_t)nw * 3 * words * 4 + (size_t)nw * list_cap * 2;
-    cudaError_t e = cudaFuncSetAttribute(k_rescore_seglists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return (int)e;
-    k_rescore_seglists<<<nspec, nw * 32, smem, st>>>(lists, lstart, list_len, num_pep, idx_sorted, rows32, stride,
-                                                     meta, kept_k, K, topn, words, list_cap, out_s, out_k, out_pep,
-                                                     err);
     return (int)cudaGetLastError();
 }
 

@@ -20,23 +20,9 @@ int hfx_lists_mark(const hfx::SpecMeta *meta, const uint32_t *wb, const uint32_t
 int hfx_lists_generate(const hfx::DevDB &db, const int32_t *cover, int64_t npep1, int32_t nbins,
                        const uint32_t *lstart, uint64_t total10, uint16_t *lists, uint16_t *list_len,
                        int32_t list_cap, int fastdiv, unsigned long long *stats, uint32_t *err, cudaStream_t st);
-// Segment lists (the BF16/FP16 two-per-warp scorer's format): one slot per
-// peptide at kLevels * lstart[p] holding segments 1..zmax of entries
-// bin << 3 | code; list_len[z-1][p] = entries of segments 1..z.
-int hfx_lists_generate_seg(const hfx::DevDB &db, const int32_t *cover, int64_t npep1, int32_t nbins,
-                           const uint32_t *lstart, uint16_t *lists, uint16_t *list_len, int32_t max_ladder,
-                           int fastdiv, unsigned long long *stats, uint32_t *err, cudaStream_t st);
-// FP32 rescoring of kept unmodified candidates from segment lists, in the
-// canonical order.
-int hfx_rescore_seglists(const uint16_t *lists, const uint32_t *lstart, const uint16_t *list_len, uint32_t num_pep,
-                         const uint32_t *idx_sorted, const float *rows32, int64_t stride, const hfx::SpecMeta *meta,
-                         const uint64_t *kept_k, int32_t nspec, int32_t K, int32_t topn, int32_t list_cap,
-                         float *out_s, uint64_t *out_k, uint32_t *out_pep, uint32_t *err, cudaStream_t st);
 // Scorer over the lists; long_rows: 32-bit entries and group tiles read
 // from global memory (rows too long for shared memory), else 16-bit entries
-// and tiles staged in shared memory.  BF16/FP16 rows in groups of up to 8
-// over shared tiles read segment lists (hfx_lists_generate_seg), every
-// other combination the per-level lists of hfx_lists_generate.
+// and tiles staged in shared memory.
 // With a sink, every pair's score is written to sink[sink_off[s] + p - wb[s]]
 // instead of the top-K.
 int hfx_lists_score(const void *lists, int long_rows, const uint32_t *lstart, uint64_t total10,
