@@ -594,19 +594,21 @@ __device__ __forceinline__ float reduce_scatter(float (&acc)[G]) {
     return s;
 }
 
-// reduce_scatter<G> within each half-warp (lanes 0-15 and 16-31 reduce
-// separately): member j's sum ends in lanes j * (16 / G) .. of each half.
-template <int G>
-__device__ __forceinline__ float reduce_scatter16(float (&acc)[G]) {
+// reduce_scatter<G> within each group of W lanes (W = 32, 16 or 8: one
+// candidate per group; the groups reduce separately): member j's sum ends in
+// lanes j * W / G .. (j + 1) * W / G - 1 of each group.
+template <int G, int W>
+__device__ __forceinline__ float reduce_scatter_lanes(float (&acc)[G]) {
+    static_assert(G <= W, "a lane group holds at most one sum per lane");
     const int lane = threadIdx.x & 31;
     float v[G];
 #pragma unroll
     for (int g = 0; g < G; ++g) v[g] = acc[g];
     int n = G;
-    int off = 8;
+    int off = W / 2;
 #pragma unroll
-    for (int step = 0; step < 4; ++step) {
-        if (n == 1) break;
+    for (int step = 0; step < 5; ++step) {
+        if (n == 1 || off == 0) break;
         const int half = n / 2;
         const bool hi = (lane & off) != 0;
 #pragma unroll
@@ -623,6 +625,12 @@ __device__ __forceinline__ float reduce_scatter16(float (&acc)[G]) {
     float s = v[0];
     for (; off >= 1; off >>= 1) s = __fadd_rn(s, __shfl_xor_sync(kFullMask, s, off));
     return s;
+}
+
+// Within each half-warp (lanes 0-15 and 16-31 reduce separately).
+template <int G>
+__device__ __forceinline__ float reduce_scatter16(float (&acc)[G]) {
+    return reduce_scatter_lanes<G, 16>(acc);
 }
 
 // Compact the planes (clearing them) into the sorted distinct-bin list and

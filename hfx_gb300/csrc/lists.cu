@@ -471,13 +471,13 @@ __global__ void __launch_bounds__(256) k_rescore_lists(const E *__restrict__ lis
 // E = list entry type (uint16_t up to 16,383 bins, uint32_t for long rows);
 // kGlobal: the group tile is read from global memory (L2) instead of being
 // staged in shared memory (rows too long for shared memory).
-// kPair: two candidates per warp, one per half-warp (entry i of a list by
-// lane i % 16 of its half).  The per-candidate work around the list --
-// the claim, the reduction, the admission -- is then shared by two
-// candidates.  It changes the order of the sums, so it serves the BF16/FP16
-// pass only, whose scores pick the candidates that FP32 rescoring orders;
-// FP32 scoring keeps the canonical order (kPair false).
-template <typename T, int G, typename E, bool kGlobal, bool kPair, int L>
+// kC: candidates per warp (1, 2 or 4), one per group of 32 / kC lanes (entry
+// i of a list by lane i % (32 / kC) of its group).  The per-candidate work
+// around the list -- the claim, the reduction, the admission -- is then
+// shared by kC candidates.  It changes the order of the sums, so kC > 1
+// serves the BF16/FP16 pass only, whose scores pick the candidates that FP32
+// rescoring orders; FP32 scoring keeps the canonical order (kC = 1).
+template <typename T, int G, typename E, bool kGlobal, int kC, int L>
 __global__ void __launch_bounds__(1024, 1)
 k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, uint64_t total10,
               uint64_t list_total, const uint16_t *__restrict__ list_len, uint32_t num_pep,
@@ -488,11 +488,12 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
               float *__restrict__ part_s, uint64_t *__restrict__ part_k, unsigned long long *__restrict__ stats,
               float *__restrict__ sink, const uint64_t *__restrict__ sink_off, uint32_t qoff,
               uint32_t *__restrict__ err) {
-    static_assert(!kPair || G <= 8, "half-warp candidates take up to 8 spectra per group");
-    constexpr int kW = kPair ? 16 : 32;  // lanes per candidate
+    static_assert(kC == 1 || kC == 2 || kC == 4, "1, 2 or 4 candidates per warp");
+    constexpr int kW = 32 / kC;  // lanes per candidate
+    static_assert(G <= kW, "a lane group takes up to one spectrum of the group per lane");
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int hl = lane & (kW - 1), half = kPair ? lane >> 4 : 0;
+    const int hl = lane & (kW - 1), half = lane / kW;  // `half`: the lane's candidate group
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     T *stile = reinterpret_cast<T *>(smem + 128);
     const T *tile = stile;
@@ -604,14 +605,14 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
             m.ls = 0u;
             while (true) {
                 uint32_t q = 0;
-                if (lane == 0) q = atomicAdd(&s_next, kPair ? 2u : 1u);
+                if (lane == 0) q = atomicAdd(&s_next, (uint32_t)kC);
                 const uint32_t base = __shfl_sync(kFullMask, q, 0);
                 m.live = base < p1;
                 m.p = base + (uint32_t)half;
                 if (!m.live) break;
                 const uint32_t bal =
                     __ballot_sync(kFullMask, hl < G && m.p < p1 && my_b <= m.p && m.p < my_e);
-                m.act = (bal >> (16 * half)) & ((1u << G) - 1u);
+                m.act = (bal >> (kW * half)) & ((1u << G) - 1u);
                 if (bal) break;
             }
             if (m.act && z >= 1 && m.p < num_pep) {
@@ -654,7 +655,9 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
 #pragma unroll
             for (int j = 0; j < G; ++j) acc[j] = 0.0f;
             const int n = cur.n;
-            const int nmax = kPair ? max(n, __shfl_xor_sync(kFullMask, n, 16)) : n;
+            int nmax = n;
+#pragma unroll
+            for (int o = kW; o < 32; o <<= 1) nmax = max(nmax, __shfl_xor_sync(kFullMask, nmax, o));
             // entries [i0, i0 + 4 kW) in e, the next 4 kW already in flight in f
             uint32_t e[4], f[4];
 #pragma unroll
@@ -683,25 +686,24 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
                     f[k] = i < n ? (uint32_t)__ldg(cur.lp + i) : pad;
                 }
             }
-            if constexpr (kPair) {
-                const float sc = reduce_scatter16<G>(acc);
-                const uint32_t act_a = __shfl_sync(kFullMask, cur.act, 0), act_b = __shfl_sync(kFullMask, cur.act, 16);
-                const uint32_t p_a = __shfl_sync(kFullMask, cur.p, 0), p_b = __shfl_sync(kFullMask, cur.p, 16);
-                const int n_a = __shfl_sync(kFullMask, n, 0), n_b = __shfl_sync(kFullMask, n, 16);
-                my_cand += (act_a != 0u) + (act_b != 0u);
-                my_entries += (uint32_t)(n_a + n_b);
-                my_psm += (uint32_t)(__popc(act_a) + __popc(act_b));
-                // member j's sums sit in lanes j * 16 / G of each half; its
-                // admission lane is j * 32 / G
-                const float sc_a = __shfl_sync(kFullMask, sc, lane >> 1);
-                const float sc_b = __shfl_sync(kFullMask, sc, 16 + (lane >> 1));
+            if constexpr (kC > 1) {
+                const float sc = reduce_scatter_lanes<G, kW>(acc);
                 const bool owner = (lane & (32 / G - 1)) == 0;
-                const bool want_a = owner && ((act_a >> my_slot) & 1u) &&
-                                    score_order(sc_a) >= *(volatile uint32_t *)(thr_u + my_slot);
-                slots.offer(want_a, sc_a, p_a, my_slot, K);
-                const bool want_b = owner && ((act_b >> my_slot) & 1u) &&
-                                    score_order(sc_b) >= *(volatile uint32_t *)(thr_u + my_slot);
-                slots.offer(want_b, sc_b, p_b, my_slot, K);
+#pragma unroll
+                for (int q = 0; q < kC; ++q) {
+                    const uint32_t act_q = __shfl_sync(kFullMask, cur.act, q * kW);
+                    const uint32_t p_q = __shfl_sync(kFullMask, cur.p, q * kW);
+                    const int n_q = __shfl_sync(kFullMask, n, q * kW);
+                    my_cand += act_q != 0u;
+                    my_entries += (uint32_t)n_q;
+                    my_psm += (uint32_t)__popc(act_q);
+                    // member j's sums sit in lanes j * kW / G of candidate q's
+                    // group; its admission lane is j * 32 / G
+                    const float sc_q = __shfl_sync(kFullMask, sc, q * kW + (lane / (32 / G)) * (kW / G));
+                    const bool want = owner && ((act_q >> my_slot) & 1u) &&
+                                      score_order(sc_q) >= *(volatile uint32_t *)(thr_u + my_slot);
+                    slots.offer(want, sc_q, p_q, my_slot, K);
+                }
             } else {
                 my_cand += 1u;
                 my_entries += (uint32_t)n;
@@ -786,6 +788,9 @@ int hfx_lists_generate(const DevDB &db, const int32_t *cover, int64_t npep1, int
     return (int)cudaGetLastError();
 }
 
+// Candidates per warp in the BF16/FP16 pass (groups of up to 8 spectra).
+constexpr int kLowpCands = 4;
+
 // Warps per list-scorer CTA: 16 (two CTAs per SM) up to 8 spectra per
 // group, 32 (one CTA per SM, the tile taking most of shared memory) for 16.
 constexpr int list_warps(int G) { return G >= 16 ? 32 : 16; }
@@ -798,7 +803,7 @@ static size_t lists_queue_offset(bool global_tile, int64_t stride, int G, size_t
     return 128 + (global_tile ? 0 : (((size_t)(stride + 8) * G * elem_bytes + 15) & ~(size_t)15));
 }
 
-template <typename T, int G, typename E, bool kGlobal, bool kPair, int L>
+template <typename T, int G, typename E, bool kGlobal, int kC, int L>
 static int launch_lists_t(const E *lists, const uint32_t *lstart, uint64_t total10, const uint16_t *list_len,
                           uint32_t num_pep, int64_t stride, const uint32_t *wb, const uint32_t *we,
                           const BatchedWs &ws, void *tiles, int32_t K, int nw,
@@ -812,7 +817,7 @@ static int launch_lists_t(const E *lists, const uint32_t *lstart, uint64_t total
     const size_t qoff = lists_queue_offset(kGlobal, stride, G, sizeof(T));
     const size_t smem = qoff + (size_t)nw * CtaSlots<G>::warp_bytes();
     if (smem > (size_t)smem_max) return (int)cudaErrorInvalidValue;
-    auto fn = k_score_lists<T, G, E, kGlobal, kPair, L>;
+    auto fn = k_score_lists<T, G, E, kGlobal, kC, L>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
     int per = 0;
@@ -832,8 +837,8 @@ int hfx_lists_group_fits(int32_t G, int long_rows, int64_t stride, int elem_byte
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaFuncAttributes fa{};
     const cudaError_t e =
-        long_rows ? cudaFuncGetAttributes(&fa, k_score_lists<__nv_bfloat16, 16, uint32_t, true, false, 32>)
-                  : cudaFuncGetAttributes(&fa, k_score_lists<__nv_bfloat16, 16, uint16_t, false, false, 32>);
+        long_rows ? cudaFuncGetAttributes(&fa, k_score_lists<__nv_bfloat16, 16, uint32_t, true, 1, 32>)
+                  : cudaFuncGetAttributes(&fa, k_score_lists<__nv_bfloat16, 16, uint16_t, false, 1, 32>);
     if (e != cudaSuccess) return 0;
     const size_t smem = lists_queue_offset(long_rows != 0, stride, 16, (size_t)elem_bytes) +
                         (size_t)list_warps(16) * CtaSlots<16>::warp_bytes();
@@ -853,7 +858,7 @@ int hfx_lists_score(const void *lists, int long_rows, const uint32_t *lstart, ui
     if (K > kMaxKept || (K > 32 && (elem_kind == 0 || G > 8))) return (int)cudaErrorInvalidValue;
 #define HFX_LL(T, GG, LL)                                                                                      \
     do {                                                                                                       \
-        constexpr bool kP = !std::is_same<T, float>::value && GG <= 8;                                         \
+        constexpr int kP = std::is_same<T, float>::value || GG > 8 ? 1 : kLowpCands;                           \
         if (long_rows)                                                                                         \
             return launch_lists_t<T, GG, uint32_t, true, kP, LL>((const uint32_t *)lists, lstart, total10,     \
                                                                  list_len, num_pep, stride, wb, we, ws, tiles, \
