@@ -311,11 +311,11 @@ __global__ void __launch_bounds__(256) k_gen_lists_long(DevDB db, const int32_t 
     extern __shared__ __align__(16) uint32_t keybuf[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     uint32_t *kb = keybuf + (size_t)warp * kLongKeys;
-    __shared__ unsigned long long s_stats[2];
-    if (threadIdx.x < 2) s_stats[threadIdx.x] = 0ull;
+    __shared__ unsigned long long s_stats[3];
+    if (threadIdx.x < 3) s_stats[threadIdx.x] = 0ull;
     __syncthreads();
     const float mt_lane = db.mt[lane];
-    uint32_t my_lists = 0, my_entries = 0;
+    uint32_t my_lists = 0, my_entries = 0, my_res = 0;
     for (int64_t t = (int64_t)blockIdx.x * nw + warp; t < (int64_t)db.num_pep; t += (int64_t)gridDim.x * nw) {
         const uint32_t p = (uint32_t)t;
         uint32_t need = 0;
@@ -326,6 +326,7 @@ __global__ void __launch_bounds__(256) k_gen_lists_long(DevDB db, const int32_t 
         const int zmax = 32 - __clz(need);
         const uint32_t tc = db.tc_sorted[p], tn = db.tn_sorted[p];
         const float r = db.r_sorted[p];
+        my_res += tn > tc ? tn - tc : 0u;
         const uint32_t nchunk = (tn - tc + 31u) / 32u;
         // keys of (prefix k, charge c) at 10 (k z + c - 1), padded to a power of two
         uint32_t nmax = 32u;
@@ -395,11 +396,13 @@ __global__ void __launch_bounds__(256) k_gen_lists_long(DevDB db, const int32_t 
         if (lane == 0) {
             atomicAdd(&s_stats[0], (unsigned long long)my_lists);
             atomicAdd(&s_stats[1], (unsigned long long)my_entries);
+            atomicAdd(&s_stats[2], (unsigned long long)my_res);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
             atomicAdd(&stats[0], s_stats[0]);
             atomicAdd(&stats[1], s_stats[1]);
+            atomicAdd(&stats[6], s_stats[2]);
         }
     }
 }
