@@ -539,6 +539,18 @@ __global__ void k_clamp_items(uint32_t *__restrict__ off, int64_t n1, uint32_t c
     }
 }
 
+__global__ void k_clamp_groups(uint32_t *__restrict__ ngroups, uint32_t cap, uint32_t *__restrict__ err) {
+    if (threadIdx.x == 0 && *ngroups > cap) {
+        *ngroups = cap;
+        atomicOr(err, kErrBounds);
+    }
+}
+
+int hfx_clamp_groups(uint32_t *ngroups, uint32_t cap, uint32_t *err, cudaStream_t st) {
+    k_clamp_groups<<<1, 32, 0, st>>>(ngroups, cap, err);
+    return (int)cudaGetLastError();
+}
+
 int hfx_clamp_items(uint32_t *off, int64_t n1, uint32_t cap, uint32_t *err, cudaStream_t st) {
     if (n1 <= 0) return 0;
     k_clamp_items<<<(unsigned)((n1 + 255) / 256), 256, 0, st>>>(off, n1, cap, err);

@@ -40,6 +40,9 @@ int hfx_batched_score(const hfx::DevDB &db, const void *rows, int elem_kind, int
                       void *tiles, uint32_t ngroups, int32_t G, int32_t chunk, int32_t K, int nw, int grid,
                       int fastdiv, float *part_s, uint64_t *part_k, uint32_t *err, cudaStream_t st);
 int hfx_clamp_items(uint32_t *off, int64_t n1, uint32_t cap, uint32_t *err, cudaStream_t st);
+// Graph replays: a planned group count above the tiles' capacity is cut to
+// it and sets kErrBounds in the error word.
+int hfx_clamp_groups(uint32_t *ngroups, uint32_t cap, uint32_t *err, cudaStream_t st);
 int hfx_batched_merge(const float *part_s, const uint64_t *part_k, const hfx::BatchedWs &ws,
                       const hfx::SpecMeta *meta, int32_t nspec, int32_t G, int32_t K, int32_t kout, float *out_s,
                       uint64_t *out_k, cudaStream_t st);

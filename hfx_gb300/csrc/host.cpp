@@ -137,6 +137,7 @@ struct hfx_ctx {
     // from the capacities; device-side overflow checks)
     int gmode = 0;
     int64_t cap_stride = 0;
+    int32_t last_G = 0;  // spectra per group of the last batched search (after every adjustment)
     uint32_t cap_groups = 0, cap_items = 0, cap_mitems = 0;
     int64_t last_stride = 0;
     // the preprocessed rows ("rows32", "meta") of the last search: their stride and spectrum count
@@ -528,6 +529,7 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     }
     if (long_rows && p->search_mods && ctx->num_mod > 0)
         return fail(ctx, HFX_ERR_UNSUPPORTED, "modification search on rows longer than 8192 bins");
+    ctx->last_G = G;
     if (p->ion_bins_custom && !long_rows)
         return fail(ctx, HFX_ERR_UNSUPPORTED, "custom ion bin width needs rows longer than 8192 bins");
     uint32_t *wb = ctx->buf<uint32_t>("wb", ns, e);
@@ -566,7 +568,11 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
         // capacities of the graph; a batch that needs more is reported (k_clamp_items)
         ngroups = ctx->cap_groups;
         total_items = ctx->cap_items;
-        rc = hfx_clamp_items(ws.item_off, (int64_t)ns + 1, total_items, ctx->d_err.as<uint32_t>(), ctx->stream);
+        // a batch with more groups than the tiles were sized for is cut to
+        // the capacity and reported (the replay is then planned again)
+        rc = hfx_clamp_groups(ws.ngroups, ngroups, ctx->d_err.as<uint32_t>(), ctx->stream);
+        if (!rc)
+            rc = hfx_clamp_items(ws.item_off, (int64_t)ns + 1, total_items, ctx->d_err.as<uint32_t>(), ctx->stream);
         if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_clamp_items");
     } else {
         uint32_t hs[4];
@@ -860,7 +866,9 @@ int32_t search_graph(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, f
     int32_t rc = search_enqueue(ctx, p, b, out_s, out_k, out_pep, out_ncand);
     if (!rc) rc = search_finish(ctx);
     if (rc) return restore(rc);
-    const int32_t G = p->group_size > 0 ? p->group_size : (p->precision == 0 ? 4 : 8);
+    // the group size the eager search used (a requested 16 falls back to 8
+    // when more than 32 candidates are kept or the tile does not fit)
+    const int32_t G = ctx->last_G > 0 ? ctx->last_G : (p->precision == 0 ? 4 : 8);
     ctx->cap_stride = ctx->last_stride;
     ctx->cap_groups = (uint32_t)((b.nspec + G - 1) / G + 24);  // <= one partial group per class
     ctx->cap_items = ctx->last_items + ctx->last_items / 4 + 64;

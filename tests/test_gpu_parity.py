@@ -504,3 +504,20 @@ def test_charge_division_equals_ieee(gpulib):
         assert bad == 0, example
     finally:
         eng.close()
+
+
+def test_graph_replay_with_fallen_back_group_size(gpulib, oracle):
+    """A requested group size of 16 falls back to 8 when more than 32
+    candidates are kept for rescoring; the CUDA graph's tiles must be sized
+    for the groups of 8 actually planned (twice as many), so a replayed
+    search of a large batch still equals the oracle's."""
+    import hfx_gb300
+    prot, sp, _ = synth.workload("tiny", n_spectra=1000)
+    eng = _engine(prot)
+    try:
+        ref = oracle.search(*_oracle_db(oracle, eng, prot), sp, topn=10)
+        p = hfx_gb300.default_params(top_n=10, batch_mode=1, precision=1, rescore_k=50, group_size=16, use_graph=1)
+        for rep in range(3):  # sizing, capture, replay
+            _compare(eng.search(sp, p), ref, f"graph replay {rep}")
+    finally:
+        eng.close()
