@@ -33,7 +33,7 @@ EXPORTED = [
     "hfx_set_mods", "hfx_mod_table", "hfx_search_host", "hfx_search_device", "hfx_search_evalues",
     "hfx_preprocess", "hfx_find_windows", "hfx_ion_bins", "hfx_mod_isoforms", "hfx_digest", "hfx_pack_ions",
     "hfx_set_profiling", "hfx_stage_stats", "hfx_search_counters", "hfx_set_workspace_limit",
-    "hfx_selftest_charge_division", "hfx_digest_gpu",
+    "hfx_digest_gpu",
 ]
 STAGES = ["layout", "preprocess", "windows", "score", "topn", "rescore", "mods", "lists", "pack"]
 
@@ -112,7 +112,6 @@ def load_library(path: str = LIB_PATH):
         "hfx_stage_stats": (i32, [P, P, P, P, i32]),
         "hfx_search_counters": (i32, [P, P, i32]),
         "hfx_set_workspace_limit": (i32, [P, u64, C.POINTER(u64)]),
-        "hfx_selftest_charge_division": (i32, [P, i32, i32, C.POINTER(u64), P]),
         "hfx_digest_gpu": (C.c_int64, [P, P, P, i32, P, i32, i32, f32, f32, i32, i32, i32, P, P, P, C.c_int64]),
     }
     for name, (res, args) in sig.items():
@@ -283,16 +282,6 @@ class Engine:
         if m != n:
             raise HfxError(HFX_ERR_CUDA, self.lib.hfx_last_error(self.h).decode())
         return r, tc, tn
-
-    def selftest_charge_division(self, exp_lo: int = 67, exp_hi: int = 187):
-        """hfx_selftest_charge_division: (mismatches, (dividend bits, charge))
-        of the branch-free ion-charge division against the IEEE quotient over
-        every float with a biased exponent in [exp_lo, exp_hi] (default
-        2^-60 <= |a| < 2^61)."""
-        n = C.c_uint64()
-        ex = np.zeros(2, np.uint32)
-        self._check(self.lib.hfx_selftest_charge_division(self.h, exp_lo, exp_hi, C.byref(n), _ptr(ex)))
-        return n.value, (int(ex[0]), int(ex[1]))
 
     def search_batches(self, spectra, params: SearchParams | None = None, batch: int = 4096, cancel=None,
                        on_batch=None) -> SearchResult:

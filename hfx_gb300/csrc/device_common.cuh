@@ -39,26 +39,13 @@ __device__ __forceinline__ float dev_div(float a, float b) {
     else return __fdiv_rn(a, b);
 }
 
-// The IEEE quotient a / c for an ion charge c in 1..4, without a branch on c
-// and without a division: q0 = RN(a * y) with y = RN(1 / c), the residual
-// r = a - q0 c exactly (one FMA), and q = RN(q0 + r y) (one FMA).  For c = 1,
-// 2, 4 the reciprocal is exact, r = 0 and q = q0 = a / c.  For c = 3 the last
-// step is Markstein's correction, which yields the correctly rounded quotient
-// from a correctly rounded reciprocal and a first quotient within one ulp
-// (P. Markstein, IBM J. Res. Develop. 34(1):111-119, 1990, Theorem 1).
-// hfx_selftest_charge_division compares it with the IEEE division over every
-// float of 2^-60 <= |a| < 2^61 on the device (tests).
-constexpr float kInvThree = 0.333333343267440796f;  // RN(1/3) = 0x3EAAAAAB
-__device__ __forceinline__ float div_charge_exact(float a, int c) {
-    const float y = c == 1 ? 1.0f : (c == 2 ? 0.5f : (c == 4 ? 0.25f : kInvThree));
-    const float q0 = __fmul_rn(a, y);
-    const float r = __fmaf_rn(-q0, (float)c, a);
-    return __fmaf_rn(r, y, q0);
-}
+// The IEEE quotient a / c for an ion charge c in 1..4: the powers of two are
+// exact scalings, only c = 3 needs a division.
 template <bool FastDiv>
 __device__ __forceinline__ float div_charge(float a, int c) {
     if constexpr (FastDiv) return __fdividef(a, (float)c);
-    return div_charge_exact(a, c);
+    if (c == 3) return __fdiv_rn(a, 3.0f);
+    return __fmul_rn(a, c == 1 ? 1.0f : (c == 2 ? 0.5f : 0.25f));
 }
 
 // float -> uint32 conversion (saturating, NaN -> 0) reinterpreted as int32.

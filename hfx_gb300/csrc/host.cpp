@@ -757,9 +757,9 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
     return HFX_OK;
 }
 
-// Failure-detection test: HFX_TEST_HOLD_LOCK=n (1..255) makes every scorer
-// CTA start with member 0's admission lock held by nobody and give up on it
-// after n attempts, so the bounded wait runs out, the CTA records a timeout
+// Failure-detection test: HFX_TEST_HOLD_LOCK=1 makes every scorer CTA start
+// with member 0's admission lock held by nobody, so each merge into it gives
+// up after its bounded number of attempts (2^20), the CTA records a timeout
 // in the error word and goes on, and the search returns HFX_ERR_TIMEOUT.
 // Read at each search (eager searches; a captured graph keeps the value of
 // its capture).  Off (0) by default.
@@ -1785,28 +1785,6 @@ int32_t hfx_ion_bins(hfx_ctx *ctx, const uint32_t *pos, const int32_t *charges, 
                                  count, ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_ion_bins");
     HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
-    return HFX_OK;
-}
-
-int32_t hfx_selftest_charge_division(hfx_ctx *ctx, int32_t exp_lo, int32_t exp_hi, uint64_t *mismatches,
-                                     uint32_t *example) {
-    if (!ctx || !mismatches) return fail(ctx, HFX_ERR_ARG, "bad hfx_selftest_charge_division arguments");
-    HFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
-    cudaError_t e;
-    unsigned long long *cnt = ctx->buf<unsigned long long>("selftest", 2, e);
-    if (e) return cuda_fail(ctx, e, "alloc");
-    HFX_CUDA(cudaMemsetAsync(cnt, 0, 16, ctx->stream), "memset");
-    const int rc = hfx_launch_selftest_division(exp_lo, exp_hi, cnt, ctx->stream);
-    if (rc == (int)cudaErrorInvalidValue) return fail(ctx, HFX_ERR_ARG, "exponents must satisfy 1 <= lo <= hi <= 254");
-    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_selftest_division");
-    unsigned long long h[2];
-    HFX_CUDA(cudaMemcpyAsync(h, cnt, 16, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
-    HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
-    *mismatches = h[0];
-    if (example) {
-        example[0] = (uint32_t)h[1];          // the dividend's bits
-        example[1] = (uint32_t)(h[1] >> 56);  // the charge
-    }
     return HFX_OK;
 }
 

@@ -259,34 +259,3 @@ int hfx_launch_ion_bins(const DevDB &db, const uint32_t *pos, const int32_t *cha
     return (int)cudaGetLastError();
 }
 
-// Self-test of the charge division: every float a with a biased exponent in
-// [exp_lo, exp_hi], both signs, divided by c = 1..4 with div_charge_exact and
-// with the IEEE division; count[0] += mismatches, count[1] = the bits of one
-// mismatching a (c in the top byte).
-__global__ void k_selftest_division(int32_t exp_lo, int32_t exp_hi, unsigned long long *__restrict__ count) {
-    const uint64_t n = (uint64_t)(exp_hi - exp_lo + 1) << 24;  // 2^23 mantissas x 2 signs per exponent
-    unsigned long long bad = 0;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t e = (uint32_t)exp_lo + (uint32_t)(i >> 24);
-        const uint32_t bits = (uint32_t)(i & 0x7FFFFFu) | (e << 23) | ((uint32_t)((i >> 23) & 1u) << 31);
-        const float a = __uint_as_float(bits);
-#pragma unroll
-        for (int c = 1; c <= 4; ++c) {
-            const float q = div_charge_exact(a, c), ref = __fdiv_rn(a, (float)c);
-            if (__float_as_uint(q) != __float_as_uint(ref)) {
-                ++bad;
-                count[1] = (unsigned long long)bits | ((unsigned long long)c << 56);
-            }
-        }
-    }
-    if (bad) atomicAdd(count, bad);
-}
-
-int hfx_launch_selftest_division(int32_t exp_lo, int32_t exp_hi, unsigned long long *count, cudaStream_t st) {
-    if (exp_lo < 1 || exp_hi > 254 || exp_lo > exp_hi) return (int)cudaErrorInvalidValue;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    k_selftest_division<<<sms * 8, 256, 0, st>>>(exp_lo, exp_hi, count);
-    return (int)cudaGetLastError();
-}

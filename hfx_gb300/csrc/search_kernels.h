@@ -13,6 +13,3 @@ int hfx_launch_merge_parts(const float *part_s, const uint64_t *part_k, const in
 int hfx_launch_ion_bins(const hfx::DevDB &db, const uint32_t *pos, const int32_t *charges,
                         const int32_t *lens, int32_t n, int32_t maxlen, int32_t cap, int fastdiv,
                         uint32_t *out_bins, uint8_t *out_lvl, int32_t *out_n, cudaStream_t st);
-// Self-test of the exact charge division (div_charge_exact against the IEEE
-// quotient) over every float of biased exponent exp_lo..exp_hi, both signs.
-int hfx_launch_selftest_division(int32_t exp_lo, int32_t exp_hi, unsigned long long *count, cudaStream_t st);

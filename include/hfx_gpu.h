@@ -256,15 +256,6 @@ int32_t hfx_ion_bins(hfx_ctx *ctx, const uint32_t *pos, const int32_t *charges, 
 int32_t hfx_mod_isoforms(hfx_ctx *ctx, const uint32_t *pos, const int32_t *mod, const uint32_t *rank,
                          int32_t n, int32_t cap, uint32_t *count, uint32_t *unrank, uint8_t *modded);
 
-/* Self-test (new): the ion m/z arithmetic divides by the ion charge without
- * a division instruction (a reciprocal multiply and one FMA correction step,
- * Markstein 1990).  This compares it, on the device, with the IEEE quotient
- * for c = 1..4 over every float whose biased exponent lies in
- * [exp_lo, exp_hi] (1..254), both signs; *mismatches receives the count and
- * example (nullable, 2 words) one mismatching dividend's bits and charge. */
-int32_t hfx_selftest_charge_division(hfx_ctx *ctx, int32_t exp_lo, int32_t exp_hi, uint64_t *mismatches,
-                                     uint32_t *example);
-
 /* Allocation-free scoring of ONE spectrum.  It has no counterpart in the
  * reference.  It is for callers that cannot call cudaMalloc: code running
  * inside another framework's memory pool or allocator hooks, host runtimes

@@ -4,10 +4,10 @@ between batches must each reach the caller as a status (HFX_ERR_TIMEOUT,
 HFX_ERR_OOM, SearchCancelled), and the context must stay usable: the next
 search returns the same results as before the failure.
 
-The timeout is made on purpose with HFX_TEST_HOLD_LOCK=n: every scorer CTA
+The timeout is made on purpose with HFX_TEST_HOLD_LOCK=1: every scorer CTA
 starts with one member's admission lock held by nobody and gives up on it
-after n attempts (a bounded loop), records the timeout in the error word and
-finishes its work.  Nothing waits without a bound, and no kernel traps."""
+after its bounded number of attempts, records the timeout in the error word
+and finishes its work.  Nothing waits without a bound, and no kernel traps."""
 import threading
 
 import numpy as np
@@ -35,7 +35,7 @@ def test_lock_wait_runs_out_reports_timeout(engine, monkeypatch, mode, prec):
     eng, prot, sp = engine
     p = hfx_gb300.default_params(top_n=10, batch_mode=mode, precision=prec)
     ref = eng.search(sp, p)
-    monkeypatch.setenv("HFX_TEST_HOLD_LOCK", "4")
+    monkeypatch.setenv("HFX_TEST_HOLD_LOCK", "1")
     with pytest.raises(hfx_gb300.HfxError) as ei:
         eng.search(sp, p)
     assert ei.value.code == hfx_gb300.HFX_ERR_TIMEOUT
@@ -56,7 +56,7 @@ def test_lock_wait_in_modification_scorer(gpulib, tiny, monkeypatch):
         sub = sp.subset(np.arange(12))
         p = hfx_gb300.default_params(top_n=10, batch_mode=1, precision=1, search_plain=0, search_mods=1)
         ref = eng.search(sub, p)
-        monkeypatch.setenv("HFX_TEST_HOLD_LOCK", "2")
+        monkeypatch.setenv("HFX_TEST_HOLD_LOCK", "1")
         with pytest.raises(hfx_gb300.HfxError) as ei:
             eng.search(sub, p)
         assert ei.value.code == hfx_gb300.HFX_ERR_TIMEOUT

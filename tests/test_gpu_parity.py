@@ -492,20 +492,6 @@ def test_keep_more_than_32_capped_with_mods(gpulib, tiny, oracle):
         eng.close()
 
 
-def test_charge_division_equals_ieee(gpulib):
-    """The ion m/z divides by the charge with a reciprocal multiply and one
-    FMA correction (no division instruction, no branch on the charge); it must
-    equal the IEEE quotient for every float from 2^-60 to 2^61 in magnitude,
-    which covers every mass the ion arithmetic forms."""
-    import hfx_gb300
-    eng = hfx_gb300.Engine(0)
-    try:
-        bad, example = eng.selftest_charge_division(67, 187)
-        assert bad == 0, example
-    finally:
-        eng.close()
-
-
 def test_graph_replay_with_fallen_back_group_size(gpulib, oracle):
     """A requested group size of 16 falls back to 8 when more than 32
     candidates are kept for rescoring; the CUDA graph's tiles must be sized
