@@ -25,7 +25,7 @@ NVCC_FLAGS = [
     "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include"), "-I", CSRC,
 ]
 SOURCES = ["host.cpp", "preprocess.cu", "search.cu", "batched.cu", "lists.cu", "mods.cu", "no_alloc.cu", "legacy.cu",
-           "evalues.cu", "ions.cu", "digest.cu", "io.cpp", "report.cpp"]
+           "evalues.cu", "ions.cu", "digest.cu", "iso_lists.cu", "io.cpp", "report.cpp"]
 
 
 def nvcc() -> str:

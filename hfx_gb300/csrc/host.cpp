@@ -13,6 +13,7 @@
 #include "mods.h"
 #include "evalues.h"
 #include "ions.h"
+#include "iso_lists.h"
 
 int hfx_digest_launch(const uint8_t *d_seq, const uint32_t *d_seg, int32_t nprot, uint32_t nres, const float *mt26,
                       int32_t rule_mask, int32_t missed, float min_mass, float max_mass, int32_t proline,
@@ -139,6 +140,7 @@ struct hfx_ctx {
     int64_t cap_stride = 0;
     int32_t last_G = 0;  // spectra per group of the last batched search (after every adjustment)
     uint32_t cap_groups = 0, cap_items = 0, cap_mitems = 0;
+    uint64_t cap_iso = 0, cap_iso_entries = 0, last_iso = 0, last_iso_entries = 0;  // isoform lists
     int64_t last_stride = 0;
     // the preprocessed rows ("rows32", "meta") of the last search: their stride and spectrum count
     int64_t rows_stride = 0;
@@ -319,8 +321,10 @@ int32_t upload_db(hfx_ctx *ctx) {
     HFX_CUDA(cudaMemcpy(ctx->d_tc.p, tcs.data(), np * 4, cudaMemcpyHostToDevice), "H2D tc");
     HFX_CUDA(cudaMemcpy(ctx->d_tn.p, tns.data(), np * 4, cudaMemcpyHostToDevice), "H2D tn");
     HFX_CUDA(cudaMemcpy(ctx->d_idx.p, ctx->h_idx.data(), np * 4, cudaMemcpyHostToDevice), "H2D idx");
+    // one entry past the last position: the end of its slot (slot sizes by difference)
+    lstart.push_back((uint32_t)ctx->list_units);
     HFX_CUDA(ctx->d_lstart.ensure(np * 4 + 16), "alloc lstart");
-    HFX_CUDA(cudaMemcpy(ctx->d_lstart.p, lstart.data(), np * 4, cudaMemcpyHostToDevice), "H2D lstart");
+    HFX_CUDA(cudaMemcpy(ctx->d_lstart.p, lstart.data(), (np + 1) * 4, cudaMemcpyHostToDevice), "H2D lstart");
     return HFX_OK;
 }
 
@@ -495,6 +499,73 @@ int32_t search_plain_per_spectrum(hfx_ctx *ctx, const hfx_search_params *p, cons
                  "H2D ncand");
         HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
     }
+    return HFX_OK;
+}
+
+// The modification search over isoform lists (iso_lists.cu): coverage and
+// isoform counts, one record per isoform, their ion lists, the scorer.  The
+// totals come back to the host in eager searches; graph replays use the
+// capacities of their capture and report a batch that outgrows them.
+int32_t search_isoform_lists(hfx_ctx *ctx, const hfx_search_params *p, const SpecMeta *meta, int32_t ns,
+                             const uint32_t *mb, const uint32_t *me, const BatchedWs &ws, const uint32_t *mlo,
+                             const uint32_t *mhi, const uint32_t *mch, const uint32_t *mitem_off, int32_t n_gm,
+                             int elem_kind, const void *tiles, int64_t stride, int32_t G, int32_t K, float *ms,
+                             uint64_t *mk, unsigned long long *ncm) {
+    cudaError_t e;
+    const DevDB db = ctx->devdb();
+    const DevMods dm = ctx->devmods();
+    const int64_t npep1 = (int64_t)ctx->num_pep + 1;
+    const int64_t ncover = (int64_t)ctx->num_mod * kLevels * npep1;
+    const int64_t n = (int64_t)ctx->num_mod * (int64_t)ctx->num_pep;
+    int32_t *cover = ctx->buf<int32_t>("i_cover", (size_t)ncover, e);
+    int32_t *cpart = e ? nullptr : ctx->buf<int32_t>("i_cpart", hfx_scan_partials_needed(ncover), e);
+    int32_t *count = e ? nullptr : ctx->buf<int32_t>("i_count", (size_t)n + 1, e);
+    int32_t *incl = e ? nullptr : ctx->buf<int32_t>("i_incl", (size_t)n + 1, e);
+    int32_t *npart = e ? nullptr : ctx->buf<int32_t>("i_npart", hfx_scan_partials_needed(n + 1), e);
+    unsigned long long *units = e ? nullptr : ctx->buf<unsigned long long>("i_units", (size_t)n, e);
+    unsigned long long *iunits = e ? nullptr : ctx->buf<unsigned long long>("i_iunits", (size_t)n, e);
+    unsigned long long *upart =
+        e ? nullptr : ctx->buf<unsigned long long>("i_upart", hfx_iso_scan64_partials_needed(n), e);
+    if (e) return cuda_fail(ctx, e, "alloc isoform plan");
+    int rc = hfx_iso_plan(db, dm, meta, ns, mb, me, ctx->d_lstart.as<uint32_t>(), cover, cpart, count, incl, npart,
+                          units, iunits, upart, ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "isoform plan");
+    uint64_t cap_iso = 0, cap_entries = 0;
+    if (ctx->gmode >= 1) {
+        cap_iso = ctx->cap_iso;
+        cap_entries = ctx->cap_iso_entries;
+    } else {
+        int32_t total = 0;
+        unsigned long long entries = 0;
+        HFX_CUDA(cudaMemcpyAsync(&total, incl + n, 4, cudaMemcpyDeviceToHost, ctx->stream), "D2H isoforms");
+        if (n > 0)
+            HFX_CUDA(cudaMemcpyAsync(&entries, iunits + n - 1, 8, cudaMemcpyDeviceToHost, ctx->stream), "D2H entries");
+        HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+        if (total < 0) return fail(ctx, HFX_ERR_UNSUPPORTED, "more than 2^31 modified isoforms in one batch");
+        cap_iso = (uint64_t)total;
+        cap_entries = entries;
+        ctx->last_iso = cap_iso;
+        ctx->last_iso_entries = cap_entries;
+    }
+    if (cap_iso > 0xFFFFFFF0ull) return fail(ctx, HFX_ERR_UNSUPPORTED, "more than 2^32 modified isoforms");
+    uint64_t *key = ctx->buf<uint64_t>("i_key", cap_iso + 1, e);
+    uint64_t *off = e ? nullptr : ctx->buf<uint64_t>("i_off", cap_iso + 1, e);
+    uint16_t *len = e ? nullptr : ctx->buf<uint16_t>("i_len", (cap_iso + 1) * kLevels, e);
+    uint16_t *lists = e ? nullptr : ctx->buf<uint16_t>("i_lists", cap_entries + 64, e);
+    if (e) return cuda_fail(ctx, e, "alloc isoform lists");
+    rc = hfx_iso_expand(db, dm, cover, ctx->d_lstart.as<uint32_t>(), count, incl, units, iunits, (uint32_t)cap_iso,
+                        cap_entries, key, off, ctx->d_err.as<uint32_t>(), ctx->stream);
+    if (!rc)
+        rc = hfx_iso_generate(db, dm, cover, (int32_t)std::min<int64_t>(stride, kMaxWords * 32),
+                              ctx->d_lstart.as<uint32_t>(), incl + n, (uint32_t)cap_iso, key, off, lists, cap_entries,
+                              len, (int32_t)std::min<uint64_t>(40ull * ctx->max_ladder, kMaxListLen), p->fastdiv,
+                              nullptr, ctx->d_err.as<uint32_t>(), ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "isoform lists");
+    rc = hfx_iso_score(lists, cap_entries, ctx->d_lstart.as<uint32_t>(), key, off, len, count, incl,
+                       (uint32_t)ctx->num_pep, (uint32_t)cap_iso, elem_kind, tiles, stride, mb, me, ctx->num_mod, ws,
+                       mlo, mhi, mch, mitem_off, n_gm, G, K, ms, mk, ncm, nullptr, ctx->d_err.as<uint32_t>(),
+                       ctx->stream);
+    if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_iso_lists");
     return HFX_OK;
 }
 
@@ -711,13 +782,22 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
         if (e) return cuda_fail(ctx, e, "alloc mod parts");
         mk = ctx->buf<uint64_t>("m_part_k", (size_t)mtotal * G * K + 1, e);
         if (e) return cuda_fail(ctx, e, "alloc mod parts");
-        if (mtotal > 0) {
+        int64_t launches = n_gm > 0 ? 5 : 1;  // k_mod_windows, k_mod_groups, 3 scan kernels
+        if (mtotal > 0 && p->batch_mode == 1) {
+            // isoform lists: every needed isoform's ion lists built once for
+            // the batch, then streamed by the scorer
+            rc = search_isoform_lists(ctx, p, meta, ns, mb, me, ws, mlo, mhi, mch, mitem_off, n_gm, elem_kind, tiles,
+                                      stride, G, K, ms, mk, ncm);
+            if (rc) return rc;
+            launches += 12;
+        } else if (mtotal > 0) {
+            // fused: every work item enumerates and builds its isoforms
             rc = hfx_mods_score(db, dm, tiles, elem_kind, stride, mb, me, ws, mlo, mhi, mch, mitem_off, n_gm, G, K,
                                 p->fastdiv, ms, mk, ncm, ctx->d_err.as<uint32_t>(), ctx->stream);
             if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_mods");
+            launches += 1;
         }
-        // k_mod_windows, k_mod_groups, 3 scan kernels, k_score_mods
-        ctx->stage_end(HFX_STAGE_MODS, n_gm > 0 ? 5 + (mtotal > 0 ? 1 : 0) : 1, mtotal);
+        ctx->stage_end(HFX_STAGE_MODS, launches, mtotal);
     }
     float *ks = ctx->buf<float>("kept_s", (size_t)ns * K, e);
     if (e) return cuda_fail(ctx, e, "alloc");
@@ -873,6 +953,8 @@ int32_t search_graph(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b, f
     ctx->cap_groups = (uint32_t)((b.nspec + G - 1) / G + 24);  // <= one partial group per class
     ctx->cap_items = ctx->last_items + ctx->last_items / 4 + 64;
     ctx->cap_mitems = ctx->last_mitems + ctx->last_mitems / 4 + 64;
+    ctx->cap_iso = ctx->last_iso + ctx->last_iso / 4 + 64;
+    ctx->cap_iso_entries = ctx->last_iso_entries + ctx->last_iso_entries / 4 + 4096;
     ctx->gmode = 1;
     rc = search_enqueue(ctx, p, b, out_s, out_k, out_pep, out_ncand);
     if (!rc) rc = search_finish(ctx);

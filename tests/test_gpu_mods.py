@@ -136,6 +136,20 @@ def test_search_mods_full(mods_full, oracle, G, mode):
     _compare(res, ref, f"full mods G={G} mode={mode}")
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_search_mods_graph_replay(mods_full, oracle, precision):
+    """The isoform lists under CUDA-graph replay: sizing run, capture and
+    replays (record and list capacities from the sizing run) all equal the
+    oracle."""
+    import hfx_gb300
+    eng, prot, sp = mods_full
+    ref = oracle.search(*_oracle_db(oracle, eng, prot), sp, topn=10, ma=MA, ma_mass=MA_MASS, max_ma=4)
+    p = hfx_gb300.default_params(top_n=10, batch_mode=1, precision=precision, rescore_k=32 if precision else 0,
+                                 use_graph=1)
+    for rep in range(3):
+        _compare(eng.search(sp, p), ref, f"mods graph replay {rep} precision {precision}")
+
+
 @pytest.mark.parametrize("precision", [1, 2])
 def test_search_mods_lowp_rescore(mods_full, oracle, precision):
     """BF16 / FP16 rows choose the kept candidates (modified included), FP32
