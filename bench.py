@@ -466,9 +466,11 @@ def main():
     eng.set_profiling(True)
     eng.stage_stats(reset=True)
     eng.counters(reset=True)
+    eng.mod_counters(reset=True)
     _timed(eng, dev, p_prof, out, a.steps, flush, stream)
     stats = eng.stage_stats(reset=True)
     work = {k: v // a.steps for k, v in eng.counters(reset=True).items()}
+    mwork = {k: v // a.steps for k, v in eng.mod_counters(reset=True).items()}
     eng.set_profiling(False)
     eager_same = bool(np.array_equal(out["key"].cpu().numpy().view(np.uint64), key))
     # e2e through the host-buffer C ABI (pinned buffers, copies in the timed region)
@@ -521,9 +523,10 @@ def main():
                  "scores_bitexact": bool(np.array_equal(s0.view(np.uint32), score[:n_pl].view(np.uint32)))}
     # roofline of the dominant kernel
     stage = "mods" if has_mods and stats["mods"][0] > stats["score"][0] else "score"
-    kern = "k_score_mods" if stage == "mods" else KERNELS[mode if mode in KERNELS else 1]
+    mod_kern = "k_score_iso_lists" if mode == 1 else "k_score_mods"
+    kern = mod_kern if stage == "mods" else KERNELS[mode if mode in KERNELS else 1]
     if has_mods and mode == 0:
-        kern = "k_score_mods" if stage == "mods" else "k_score_batched"
+        kern = mod_kern if stage == "mods" else "k_score_batched"
     rng = np.random.Generator(np.random.PCG64(7))
     r, tc, tn, idx, mt = eng.db_export()
     bsz = 2 if prec else 4
@@ -566,12 +569,16 @@ def main():
     # writes by design, from the run's own work counters: the generator
     # reads each needed peptide's residues and metadata and writes its lists;
     # the list scorer streams list entries, list metadata and the spectrum
-    # tiles it stages.  The per-pair figure U*s + L + 16 of the search as a
+    # tiles it stages; the isoform-list generator and scorer of the
+    # modification search likewise, plus their per-isoform records.  The
+    # per-pair figure U*s + L + 16 of the search as a
     # whole is reported for the step (`step`), where the benchmark spec's target is
     # defined.
     es = 4 if long_rows else 2
     kern_rows = {}
-    stage_of = {"lists": "k_gen_lists" + ("_long" if long_rows else ""), "score": kern, "mods": "k_score_mods"}
+    stage_of = {"lists": "k_gen_lists" + ("_long" if long_rows else ""), "score": kern, "mods": mod_kern}
+    if mode == 1 and has_mods:
+        stage_of["mod_lists"] = "k_gen_iso_lists"
     step_ms_all = sum(v[0] for v in stats.values()) / a.steps
     for st, kname in stage_of.items():
         ms_st, nl_st, _ = stats.get(st, (0.0, 0, 0))
@@ -584,6 +591,14 @@ def main():
         elif st == "score" and mode == 1:
             moved = work["entries_streamed"] * es + work["tile_bytes"] + 8 * work["candidates"]
             basis = "list entries streamed + spectrum tiles staged + 8 B per candidate"
+        elif st == "mod_lists":
+            moved = mwork["list_entries"] * 2 + mwork["residues_read"] + 40 * mwork["isoforms"]
+            basis = ("isoform list entries written + residues read + 40 B per isoform record (key and slot "
+                     "offset written and read back, level lengths)")
+        elif st == "mods" and mode == 1:
+            moved = mwork["entries_streamed"] * 2 + mwork["tile_bytes"] + 26 * mwork["candidates"]
+            basis = ("isoform list entries streamed + spectrum tiles staged + 26 B per isoform hand-out (key, "
+                     "slot offset, length, list start)")
         else:
             moved = bpp * (psm_kernel if st == stage else psm_step)
             basis = "U*s + L + 16 per pair (ions rebuilt from residues per pair)"
@@ -613,7 +628,8 @@ def main():
                    "autotuned": tuned,
                    "l2": "flushed between timed steps (512 MB write)",
                    "stage_ms_per_step": {k: v[0] / a.steps for k, v in stats.items() if v[1]},
-                   "work_per_step": work},
+                   "work_per_step": work,
+                   **({"mod_work_per_step": mwork} if has_mods and mode == 1 else {})},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "result_equals_device_run": e2e_same},
         "gpu_launches": int(launches_per_step * a.steps),

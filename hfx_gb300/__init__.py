@@ -32,10 +32,10 @@ EXPORTED = [
     "hfx_set_protein_segments", "hfx_match_ions", "hfx_mass_table",
     "hfx_set_mods", "hfx_mod_table", "hfx_search_host", "hfx_search_device", "hfx_search_evalues",
     "hfx_preprocess", "hfx_find_windows", "hfx_ion_bins", "hfx_mod_isoforms", "hfx_digest", "hfx_pack_ions",
-    "hfx_set_profiling", "hfx_stage_stats", "hfx_search_counters", "hfx_set_workspace_limit",
+    "hfx_set_profiling", "hfx_stage_stats", "hfx_search_counters", "hfx_mod_counters", "hfx_set_workspace_limit",
     "hfx_digest_gpu",
 ]
-STAGES = ["layout", "preprocess", "windows", "score", "topn", "rescore", "mods", "lists", "pack"]
+STAGES = ["layout", "preprocess", "windows", "score", "topn", "rescore", "mods", "lists", "pack", "mod_lists"]
 
 
 class HfxError(RuntimeError):
@@ -111,6 +111,7 @@ def load_library(path: str = LIB_PATH):
         "hfx_set_profiling": (i32, [P, i32]),
         "hfx_stage_stats": (i32, [P, P, P, P, i32]),
         "hfx_search_counters": (i32, [P, P, i32]),
+        "hfx_mod_counters": (i32, [P, P, i32]),
         "hfx_set_workspace_limit": (i32, [P, u64, C.POINTER(u64)]),
         "hfx_digest_gpu": (C.c_int64, [P, P, P, i32, P, i32, i32, f32, f32, i32, i32, i32, P, P, P, C.c_int64]),
     }
@@ -253,6 +254,15 @@ class Engine:
         self._check(self.lib.hfx_search_counters(self.h, _ptr(c), int(reset)))
         names = ["lists", "list_entries", "candidates", "entries_streamed", "pairs", "positions_claimed",
                  "residues_read", "tile_bytes"]
+        return {n: int(c[i]) for i, n in enumerate(names)}
+
+    def mod_counters(self, reset: bool = True):
+        """Work counters of the modification search over isoform lists (see
+        hfx_mod_counters)."""
+        c = np.zeros(8, np.uint64)
+        self._check(self.lib.hfx_mod_counters(self.h, _ptr(c), int(reset)))
+        names = ["lists", "list_entries", "candidates", "entries_streamed", "pairs", "isoforms", "residues_read",
+                 "tile_bytes"]
         return {n: int(c[i]) for i, n in enumerate(names)}
 
     def set_workspace_limit(self, nbytes: int) -> int:

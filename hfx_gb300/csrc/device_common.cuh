@@ -55,15 +55,16 @@ __device__ __forceinline__ int32_t sat_bin(float r) {
 
 // rint(fl(mz / 1.0005079)).  A multiply by the rounded reciprocal lies within
 // 2^-22 relative of the IEEE quotient, i.e. within 2^-8 for |q| < 2^14; when
-// it is farther than 1/128 from a half-integer both round to the same
-// integer, otherwise the IEEE quotient itself is computed.  Exact.
+// it is farther than 1/128 from a half-integer -- its distance to the nearest
+// integer, |q - rint(q)| (exact), is below 1/2 - 1/128 -- both round to the
+// same integer, otherwise the IEEE quotient itself is computed.  Exact.
 constexpr float kInvBinMono = 1.0f / 1.0005079f;
 template <bool FastDiv>
 __device__ __forceinline__ int32_t bin_of(float mz) {
     if constexpr (FastDiv) return sat_bin(rintf(__fdividef(mz, kBinMono)));
     const float q = __fmul_rn(mz, kInvBinMono);
-    const float f = __fsub_rn(q, floorf(q));
-    if (fabsf(q) < 16384.0f && fabsf(__fsub_rn(f, 0.5f)) > 0.0078125f) return sat_bin(rintf(q));
+    const float r = rintf(q);
+    if (fabsf(q) < 16384.0f && fabsf(__fsub_rn(q, r)) < 0.4921875f) return sat_bin(r);
     return sat_bin(rintf(__fdiv_rn(mz, kBinMono)));
 }
 

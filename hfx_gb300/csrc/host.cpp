@@ -84,7 +84,7 @@ struct DBuf {
 
 namespace {
 const char *const kStageNames[HFX_NSTAGES] = {"layout", "preprocess", "windows", "score", "topn",
-                                              "rescore", "mods", "lists", "pack"};
+                                              "rescore", "mods", "lists", "pack", "mod_lists"};
 }  // namespace
 
 struct hfx_ctx {
@@ -99,6 +99,7 @@ struct hfx_ctx {
     uint32_t max_ladder = 0;       // max over fragments of (tn - tc)
     DBuf d_lstart;                 // per mass-order position: 10 * prefix sum of (tn - tc)
     unsigned long long counters[8] = {0};
+    unsigned long long mod_counters[8] = {0};  // the modification path's (hfx_mod_counters)
     float mt[26] = {0};
     std::vector<uint8_t> h_ascii;
     std::vector<uint32_t> h_seg;   // protein residue starts (+ end); one segment if unknown
@@ -512,6 +513,12 @@ int32_t search_isoform_lists(hfx_ctx *ctx, const hfx_search_params *p, const Spe
                              int elem_kind, const void *tiles, int64_t stride, int32_t G, int32_t K, float *ms,
                              uint64_t *mk, unsigned long long *ncm) {
     cudaError_t e;
+    unsigned long long *stats = nullptr;
+    if (ctx->profile) {
+        stats = ctx->buf<unsigned long long>("i_stats", 8, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        HFX_CUDA(cudaMemsetAsync(stats, 0, 64, ctx->stream), "memset");
+    }
     const DevDB db = ctx->devdb();
     const DevMods dm = ctx->devmods();
     const int64_t npep1 = (int64_t)ctx->num_pep + 1;
@@ -552,20 +559,30 @@ int32_t search_isoform_lists(hfx_ctx *ctx, const hfx_search_params *p, const Spe
     uint64_t *off = e ? nullptr : ctx->buf<uint64_t>("i_off", cap_iso + 1, e);
     uint16_t *len = e ? nullptr : ctx->buf<uint16_t>("i_len", (cap_iso + 1) * kLevels, e);
     uint16_t *lists = e ? nullptr : ctx->buf<uint16_t>("i_lists", cap_entries + 64, e);
+    const int32_t pos_words = (int32_t)((ctx->max_ladder + 31) / 32 + 1);
+    uint32_t *pos = e ? nullptr : ctx->buf<uint32_t>("i_pos", (cap_iso + 1) * (size_t)pos_words, e);
     if (e) return cuda_fail(ctx, e, "alloc isoform lists");
     rc = hfx_iso_expand(db, dm, cover, ctx->d_lstart.as<uint32_t>(), count, incl, units, iunits, (uint32_t)cap_iso,
                         cap_entries, key, off, ctx->d_err.as<uint32_t>(), ctx->stream);
     if (!rc)
         rc = hfx_iso_generate(db, dm, cover, (int32_t)std::min<int64_t>(stride, kMaxWords * 32),
                               ctx->d_lstart.as<uint32_t>(), incl + n, (uint32_t)cap_iso, key, off, lists, cap_entries,
-                              len, (int32_t)std::min<uint64_t>(40ull * ctx->max_ladder, kMaxListLen), p->fastdiv,
-                              nullptr, ctx->d_err.as<uint32_t>(), ctx->stream);
+                              len, (int32_t)std::min<uint64_t>(40ull * ctx->max_ladder, kMaxListLen), pos_words,
+                              pos, p->fastdiv, stats, ctx->d_err.as<uint32_t>(), ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "isoform lists");
+    ctx->stage_end(HFX_STAGE_MOD_LISTS, 17, (int64_t)cap_iso);  // windows, planning, 12 isoform-list kernels
+    ctx->stage_begin(HFX_STAGE_MODS);
     rc = hfx_iso_score(lists, cap_entries, ctx->d_lstart.as<uint32_t>(), key, off, len, count, incl,
                        (uint32_t)ctx->num_pep, (uint32_t)cap_iso, elem_kind, tiles, stride, mb, me, ctx->num_mod, ws,
-                       mlo, mhi, mch, mitem_off, n_gm, G, K, ms, mk, ncm, nullptr, ctx->d_err.as<uint32_t>(),
+                       mlo, mhi, mch, mitem_off, n_gm, G, K, ms, mk, ncm, stats, ctx->d_err.as<uint32_t>(),
                        ctx->stream);
     if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_iso_lists");
+    if (stats) {
+        unsigned long long h[8];
+        HFX_CUDA(cudaMemcpyAsync(h, stats, 64, cudaMemcpyDeviceToHost, ctx->stream), "D2H stats");
+        HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+        for (int i = 0; i < 8; ++i) ctx->mod_counters[i] += h[i];
+    }
     return HFX_OK;
 }
 
@@ -761,7 +778,9 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
         ncm = ctx->buf<unsigned long long>("m_ncand", (size_t)ns, e);
         if (e) return cuda_fail(ctx, e, "alloc");
         HFX_CUDA(cudaMemsetAsync(ncm, 0, 8ull * ns, ctx->stream), "memset");
-        ctx->stage_begin(HFX_STAGE_MODS);
+        // "mod_lists": windows, planning and (batch_mode 1) the isoform
+        // lists; "mods": the scorer
+        ctx->stage_begin(HFX_STAGE_MOD_LISTS);
         rc = hfx_mods_windows(ctx->d_r.as<float>(), (uint32_t)ctx->num_pep, meta, ns, dm, mb, me, ctx->stream);
         if (!rc) rc = hfx_mods_plan(ws, ngroups, mb, me, nm, chunk, mlo, mhi, mch, nch, mitem_off, partial,
                                     ctx->stream);
@@ -782,22 +801,25 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
         if (e) return cuda_fail(ctx, e, "alloc mod parts");
         mk = ctx->buf<uint64_t>("m_part_k", (size_t)mtotal * G * K + 1, e);
         if (e) return cuda_fail(ctx, e, "alloc mod parts");
-        int64_t launches = n_gm > 0 ? 5 : 1;  // k_mod_windows, k_mod_groups, 3 scan kernels
         if (mtotal > 0 && p->batch_mode == 1) {
             // isoform lists: every needed isoform's ion lists built once for
-            // the batch, then streamed by the scorer
+            // the batch, then streamed by the scorer (which ends the
+            // mod_lists stage and begins the mods stage)
             rc = search_isoform_lists(ctx, p, meta, ns, mb, me, ws, mlo, mhi, mch, mitem_off, n_gm, elem_kind, tiles,
                                       stride, G, K, ms, mk, ncm);
             if (rc) return rc;
-            launches += 12;
-        } else if (mtotal > 0) {
-            // fused: every work item enumerates and builds its isoforms
-            rc = hfx_mods_score(db, dm, tiles, elem_kind, stride, mb, me, ws, mlo, mhi, mch, mitem_off, n_gm, G, K,
-                                p->fastdiv, ms, mk, ncm, ctx->d_err.as<uint32_t>(), ctx->stream);
-            if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_mods");
-            launches += 1;
+            ctx->stage_end(HFX_STAGE_MODS, 1, mtotal);
+        } else {
+            ctx->stage_end(HFX_STAGE_MOD_LISTS, n_gm > 0 ? 5 : 1, 0);  // k_mod_windows, k_mod_groups, 3 scans
+            if (mtotal > 0) {
+                // fused: every work item enumerates and builds its isoforms
+                ctx->stage_begin(HFX_STAGE_MODS);
+                rc = hfx_mods_score(db, dm, tiles, elem_kind, stride, mb, me, ws, mlo, mhi, mch, mitem_off, n_gm, G,
+                                    K, p->fastdiv, ms, mk, ncm, ctx->d_err.as<uint32_t>(), ctx->stream);
+                if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_mods");
+                ctx->stage_end(HFX_STAGE_MODS, 1, mtotal);
+            }
         }
-        ctx->stage_end(HFX_STAGE_MODS, launches, mtotal);
     }
     float *ks = ctx->buf<float>("kept_s", (size_t)ns * K, e);
     if (e) return cuda_fail(ctx, e, "alloc");
@@ -1095,6 +1117,15 @@ int32_t hfx_search_counters(hfx_ctx *ctx, uint64_t *out8, int32_t reset) {
     for (int i = 0; i < 8; ++i) {
         out8[i] = ctx->counters[i];
         if (reset) ctx->counters[i] = 0;
+    }
+    return HFX_OK;
+}
+
+int32_t hfx_mod_counters(hfx_ctx *ctx, uint64_t *out8, int32_t reset) {
+    if (!ctx || !out8) return HFX_ERR_ARG;
+    for (int i = 0; i < 8; ++i) {
+        out8[i] = ctx->mod_counters[i];
+        if (reset) ctx->mod_counters[i] = 0;
     }
     return HFX_OK;
 }

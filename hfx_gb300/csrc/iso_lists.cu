@@ -153,7 +153,43 @@ __global__ void k_iso_expand(DevDB db, const int32_t *__restrict__ count, const 
     }
 }
 
-// 4. one warp per isoform: the distinct-bin list of every needed level.
+// 4a. one warp per isoform: the residues it modifies (modable-acid counts,
+// isoform count, unranking, gen_mod_pep.cu:127-227 and mion_series.cu:244-286),
+// pos_words words per record in iso_pos.  Kept apart from the list builder,
+// whose registers would otherwise be sized by the unranking's state.
+__global__ void __launch_bounds__(256) k_iso_positions(DevDB db, DevMods mods, const int32_t *__restrict__ total_p,
+                                                       uint32_t cap_iso, const uint64_t *__restrict__ iso_key,
+                                                       int32_t pos_words, uint32_t *__restrict__ iso_pos,
+                                                       uint32_t *__restrict__ err) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const uint32_t total = min((uint32_t)*total_p, cap_iso);
+    for (uint32_t t = blockIdx.x * nw + warp; t < total; t += gridDim.x * nw) {
+        const uint64_t key = iso_key[t];
+        const int32_t mu = (int32_t)((key >> 54) & 0x1FFu);
+        const uint32_t p = (uint32_t)((key >> 27) & 0x7FFFFFFu), rank = (uint32_t)(key & 0x7FFFFFFu);
+        uint32_t *bits = iso_pos + (size_t)t * pos_words;
+        if (key == ~0ull || p >= db.num_pep || mu >= mods.num_mod) continue;  // a skipped record
+        const uint32_t tc = db.tc_sorted[p], tn = db.tn_sorted[p];
+        if (tn > tc && (int64_t)(tn - tc) > 32ll * pos_words) {  // longer than the database's longest peptide
+            if (lane == 0) atomicOr(err, kErrBounds);
+            for (int i = lane; i < pos_words; i += 32) bits[i] = 0u;
+            continue;
+        }
+        const int32_t *dcount = mods.counts + (size_t)mu * mods.num_ma;
+        uint32_t D[kMaxMa], scan[kMaxMa];
+        uint64_t mask[kMaxMa];
+        modable_counts(db.ions, tc, tn, mods.num_ma, D);
+        const uint32_t niso = isoform_count(D, dcount, mods.num_ma, scan);
+        if (rank >= niso || !isoform_masks(D, scan, dcount, mods.num_ma, rank, mask)) {
+            if (lane == 0) atomicOr(err, kErrKeyOverflow);
+            for (int i = lane; i < pos_words; i += 32) bits[i] = 0u;
+            continue;
+        }
+        isoform_positions(db.ions, tc, tn, mask, mods.num_ma, mods.per_type, bits);
+    }
+}
+
+// 4b. one warp per isoform: the distinct-bin list of every needed level.
 template <bool FastDiv>
 __global__ void __launch_bounds__(256) k_gen_iso_lists(DevDB db, DevMods mods, const int32_t *__restrict__ cover,
                                                        int64_t npep1, int32_t nbins,
@@ -162,10 +198,11 @@ __global__ void __launch_bounds__(256) k_gen_iso_lists(DevDB db, DevMods mods, c
                                                        const uint64_t *__restrict__ iso_key,
                                                        const uint64_t *__restrict__ iso_off, uint16_t *__restrict__ lists,
                                                        uint64_t list_total, uint16_t *__restrict__ iso_len,
-                                                       int32_t list_cap,
+                                                       int32_t list_cap, int32_t pos_words,
+                                                       const uint32_t *__restrict__ iso_pos,
                                                        unsigned long long *__restrict__ stats,
                                                        uint32_t *__restrict__ err) {
-    extern __shared__ __align__(16) uint8_t smem[];
+    extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int32_t words = (nbins + 31) / 32;
     uint32_t *planes = reinterpret_cast<uint32_t *>(smem) + (size_t)warp * 3 * words;
@@ -175,17 +212,17 @@ __global__ void __launch_bounds__(256) k_gen_iso_lists(DevDB db, DevMods mods, c
     __syncwarp();
     const Planes pl{planes, planes + words, planes + 2 * words};
     const float mt_lane = db.mt[lane];
-    ModIsoform iso;
-    iso.num_ma = mods.num_ma;
-    iso.per_type = mods.per_type;
+    float ma_lane = 0.0f;
 #pragma unroll
-    for (int i = 0; i < kMaxMa; ++i) iso.ma_mass[i] = mods.ma_mass[i];
+    for (int i = 0; i < kMaxMa; ++i)
+        if (lane == i && i < mods.num_ma) ma_lane = mods.ma_mass[i];
     const uint32_t total = min((uint32_t)*total_p, cap_iso);
-    unsigned long long my_lists = 0, my_entries = 0;
+    // per-warp work counters (a warp's share of one launch fits 32 bits)
+    uint32_t my_lists = 0, my_entries = 0, my_iso = 0, my_res = 0;
     for (uint32_t t = blockIdx.x * nw + warp; t < total; t += gridDim.x * nw) {
         const uint64_t key = iso_key[t];
         const int32_t mu = (int32_t)((key >> 54) & 0x1FFu);
-        const uint32_t p = (uint32_t)((key >> 27) & 0x7FFFFFFu), rank = (uint32_t)(key & 0x7FFFFFFu);
+        const uint32_t p = (uint32_t)((key >> 27) & 0x7FFFFFFu);
         if (key == ~0ull || p >= db.num_pep || mu >= mods.num_mod) {  // a skipped record
             if (lane < kLevels) iso_len[(size_t)t * kLevels + lane] = 0;
             continue;
@@ -195,51 +232,58 @@ __global__ void __launch_bounds__(256) k_gen_iso_lists(DevDB db, DevMods mods, c
         const uint32_t tc = db.tc_sorted[p], tn = db.tn_sorted[p];
         const uint32_t unit = lstart[p + 1] - lstart[p];
         const uint64_t off = iso_off[t];
-        if (off + iso_slot(unit, zmax) > list_total) {  // cannot happen for an expanded record
+        if (off + iso_slot(unit, zmax) > list_total ||
+            (tn > tc && (int64_t)(tn - tc) > 32ll * pos_words)) {  // neither happens for an expanded record
             if (lane == 0) atomicOr(err, kErrBounds);
             if (lane < kLevels) iso_len[(size_t)t * kLevels + lane] = 0;
             continue;
         }
-        const int32_t *dcount = mods.counts + (size_t)mu * mods.num_ma;
-        uint32_t D[kMaxMa], scan[kMaxMa];
-        modable_counts(db.ions, tc, tn, mods.num_ma, D);
-        const uint32_t niso = isoform_count(D, dcount, mods.num_ma, scan);
-        if (rank >= niso || !isoform_masks(D, scan, dcount, mods.num_ma, rank, iso.mask)) {
-            if (lane == 0) atomicOr(err, kErrKeyOverflow);
-            if (lane < kLevels) iso_len[(size_t)t * kLevels + lane] = 0;
-            continue;
-        }
+        // the residues this isoform modifies (k_iso_positions)
+        const ModPositions iso{iso_pos + (size_t)t * pos_words, ma_lane, 0u};
+        my_iso += 1;
+        my_res += tn > tc ? tn - tc : 0u;
         // mion_series.cu:226: residual + delta
         const float residual = __fadd_rn(db.r_sorted[p], mods.delta[mu]);
         WordRange all{0x7FFFFFFF, 0};
-        for (int z = 1; z <= zmax; ++z) {
-            iso.reset();
-            const WordRange wr = build_planes_range<FastDiv>(pl, db.ions, tc, tn, residual, z, z, nbins, mt_lane, iso);
+        // the level-z list from the planes, when some spectrum needs it
+        auto emit_level = [&](int z) {
+            if (!((need >> (z - 1)) & 1u)) return;
+            const WordRange use = all.hi > all.lo ? all : WordRange{0, 0};
+            uint16_t *slot = lists + off + (uint64_t)unit * (uint64_t)(z * (z - 1) / 2);
+            const int room = (int)(unit * (uint32_t)z);  // >= 10 (tn - tc) z distinct bins
+            int nl = compact_planes(pl, use, z == zmax, list, list_cap, slot, room);
+            if (nl > room) {
+                if (lane == 0) atomicOr(err, kErrListOverflow);
+                nl = room;
+            }
+            if (nl <= list_cap) {
+                const uint4 *src = reinterpret_cast<const uint4 *>(list);
+                uint4 *dst = reinterpret_cast<uint4 *>(slot);
+                for (int i = lane; i < ((nl + 7) >> 3); i += 32) dst[i] = src[i];
+            }
+            if (lane == 0) iso_len[(size_t)t * kLevels + (z - 1)] = (uint16_t)nl;
+            my_lists += 1;
+            my_entries += (uint32_t)nl;
+            __syncwarp();
+        };
+        auto widen = [&](WordRange wr) {
             if (wr.hi > wr.lo) {
                 all.lo = min(all.lo, wr.lo);
                 all.hi = max(all.hi, wr.hi);
             }
-            if (!((need >> (z - 1)) & 1u)) continue;
-            const WordRange use = all.hi > all.lo ? all : WordRange{0, 0};
-            int nl = compact_planes(pl, use, z == zmax, list, list_cap);
-            if (nl > list_cap || nl > (int)(unit * (uint32_t)z)) {
-                if (lane == 0) atomicOr(err, kErrListOverflow);
-                nl = min(list_cap, (int)(unit * (uint32_t)z));
-            }
-            const uint4 *src = reinterpret_cast<const uint4 *>(list);
-            uint4 *dst = reinterpret_cast<uint4 *>(lists + off + (uint64_t)unit * (uint64_t)(z * (z - 1) / 2));
-            for (int i = lane; i < ((nl + 7) >> 3); i += 32) dst[i] = src[i];
-            if (lane == 0) iso_len[(size_t)t * kLevels + (z - 1)] = (uint16_t)nl;
-            my_lists += 1;
-            my_entries += (unsigned long long)nl;
-            __syncwarp();
+        };
+        for (int z = 1; z <= zmax; ++z) {
+            widen(build_planes_range<FastDiv>(pl, db.ions, tc, tn, residual, z, z, nbins, mt_lane, iso));
+            emit_level(z);
         }
         if (lane >= zmax && lane < kLevels) iso_len[(size_t)t * kLevels + lane] = 0;
         if (lane < zmax && !((need >> lane) & 1u)) iso_len[(size_t)t * kLevels + lane] = 0;
     }
     if (stats && lane == 0) {
-        atomicAdd(&stats[0], my_lists);
-        atomicAdd(&stats[1], my_entries);
+        atomicAdd(&stats[0], (unsigned long long)my_lists);
+        atomicAdd(&stats[1], (unsigned long long)my_entries);
+        atomicAdd(&stats[5], (unsigned long long)my_iso);
+        atomicAdd(&stats[6], (unsigned long long)my_res);
     }
 }
 
@@ -282,7 +326,7 @@ k_score_iso_lists(const uint16_t *__restrict__ lists, uint64_t list_total, const
     __syncthreads();
     const int my_slot = reduce_slot_of_lane<G>(lane);
     uint32_t phase = 0;
-    unsigned long long my_cand = 0, my_entries = 0, my_psm = 0;
+    unsigned long long my_cand = 0, my_entries = 0, my_psm = 0, my_tile = 0;
     CtaSlots<G, uint64_t> slots;
     slots.bind(s_ls, s_lk, s_lock, thr_u, smem + qoff + (size_t)warp * CtaSlots<G, uint64_t>::warp_bytes(), err);
     while (true) {
@@ -321,6 +365,7 @@ k_score_iso_lists(const uint16_t *__restrict__ lists, uint64_t list_total, const
             const uint32_t bytes = (uint32_t)((size_t)nb * G * sizeof(T));
             mbar_arrive_expect_tx(bar, bytes);
             bulk_g2s(stile, tiles + (size_t)g * stride * G, bytes, bar);
+            my_tile += bytes;
         }
         {
             // bins [nb, stride + 8) read as zero (the pad entry's bin is stride)
@@ -420,6 +465,7 @@ k_score_iso_lists(const uint16_t *__restrict__ lists, uint64_t list_total, const
         atomicAdd(&stats[2], my_cand);
         atomicAdd(&stats[3], my_entries);
         atomicAdd(&stats[4], my_psm);
+        if (threadIdx.x == 0) atomicAdd(&stats[7], my_tile);
     }
 }
 
@@ -556,16 +602,19 @@ int hfx_iso_expand(const DevDB &db, const DevMods &m, const int32_t *cover, cons
 
 int hfx_iso_generate(const DevDB &db, const DevMods &m, const int32_t *cover, int32_t nbins, const uint32_t *lstart,
                      const int32_t *total_p, uint32_t cap_iso, const uint64_t *iso_key, const uint64_t *iso_off,
-                     uint16_t *lists, uint64_t list_total, uint16_t *iso_len, int32_t list_cap, int fastdiv,
-                     unsigned long long *stats, uint32_t *err, cudaStream_t st) {
+                     uint16_t *lists, uint64_t list_total, uint16_t *iso_len, int32_t list_cap, int32_t pos_words,
+                     uint32_t *iso_pos, int fastdiv, unsigned long long *stats, uint32_t *err, cudaStream_t st) {
     if (cap_iso == 0) return 0;
     const int nw = 8;
     const int32_t words = (nbins + 31) / 32;
-    list_cap = (std::max(32, std::min(list_cap, kMaxListLen)) + 7) & ~7;
+    // 16-byte staging lists of up to kStageCap entries (longer lists are
+    // written directly)
+    list_cap = (std::max(32, std::min(list_cap, kStageCap)) + 7) & ~7;
     const size_t smem = (size_t)nw * 3 * words * 4 + (size_t)nw * list_cap * 2;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    k_iso_positions<<<sms * 8, 256, 0, st>>>(db, m, total_p, cap_iso, iso_key, pos_words, iso_pos, err);
     auto f = fastdiv ? k_gen_iso_lists<true> : k_gen_iso_lists<false>;
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
@@ -573,7 +622,7 @@ int hfx_iso_generate(const DevDB &db, const DevMods &m, const int32_t *cover, in
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, nw * 32, smem);
     f<<<sms * (per > 0 ? per : 1), nw * 32, smem, st>>>(db, m, cover, (int64_t)db.num_pep + 1, nbins, lstart, total_p,
                                                         cap_iso, iso_key, iso_off, lists, list_total, iso_len,
-                                                        list_cap, stats, err);
+                                                        list_cap, pos_words, iso_pos, stats, err);
     return (int)cudaGetLastError();
 }
 

@@ -22,12 +22,19 @@ int hfx_iso_expand(const hfx::DevDB &db, const hfx::DevMods &m, const int32_t *c
                    uint64_t *iso_off, uint32_t *err, cudaStream_t st);
 // The isoforms' ion lists (u16 entries bin << 2 | level, ascending) of every
 // needed level; iso_len [isoform][kLevels].  total_p: the device total.
+// First the residues each isoform modifies (iso_pos, pos_words words per
+// record, at least the longest peptide's residues / 32).
+// stats (nullable, 8 counters): [0] lists, [1] entries, [5] isoform records,
+// [6] residues read.
 int hfx_iso_generate(const hfx::DevDB &db, const hfx::DevMods &m, const int32_t *cover, int32_t nbins,
                      const uint32_t *lstart, const int32_t *total_p, uint32_t cap_iso, const uint64_t *iso_key,
                      const uint64_t *iso_off, uint16_t *lists, uint64_t list_total, uint16_t *iso_len,
-                     int32_t list_cap, int fastdiv, unsigned long long *stats, uint32_t *err, cudaStream_t st);
+                     int32_t list_cap, int32_t pos_words, uint32_t *iso_pos, int fastdiv,
+                     unsigned long long *stats, uint32_t *err, cudaStream_t st);
 // The scorer over the isoform lists and the group tiles; work items and
-// partial outputs as hfx_mods_score's (without a score sink).
+// partial outputs as hfx_mods_score's (without a score sink).  stats
+// (nullable): [2] isoform hand-outs, [3] list entries streamed, [4] pairs,
+// [7] tile bytes staged.
 int hfx_iso_score(const uint16_t *lists, uint64_t list_total, const uint32_t *lstart, const uint64_t *iso_key,
                   const uint64_t *iso_off, const uint16_t *iso_len, const int32_t *count, const int32_t *incl,
                   uint32_t num_pep, uint32_t cap_iso, int elem_kind, const void *tiles, int64_t stride,

@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(256) k_gen_lists(DevDB db, const int32_t *__re
                                                    uint16_t *__restrict__ list_len, int32_t list_cap,
                                                    unsigned long long *__restrict__ stats,
                                                    uint32_t *__restrict__ err) {
-    extern __shared__ __align__(16) uint8_t smem[];
+    extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int32_t words = (nbins + 31) / 32;
     uint32_t *planes = reinterpret_cast<uint32_t *>(smem) + (size_t)warp * 3 * words;
@@ -152,29 +152,38 @@ __global__ void __launch_bounds__(256) k_gen_lists(DevDB db, const int32_t *__re
         const float r = db.r_sorted[p];
         my_res += tn > tc ? tn - tc : 0u;
         WordRange all{0x7FFFFFFF, 0};
-        for (int z = 1; z <= zmax; ++z) {
-            const WordRange wr = build_planes_range<FastDiv>(pl, db.ions, tc, tn, r, z, z, nbins, mt_lane, NoMods{});
-            if (wr.hi > wr.lo) {
-                all.lo = min(all.lo, wr.lo);
-                all.hi = max(all.hi, wr.hi);
-            }
-            if (!((need >> (z - 1)) & 1u)) continue;
+        // the level-z list from the planes, when some spectrum needs it
+        auto emit_level = [&](int z) {
+            if (!((need >> (z - 1)) & 1u)) return;
             const WordRange use = all.hi > all.lo ? all : WordRange{0, 0};
-            int n = compact_planes(pl, use, z == zmax, list, list_cap);
-            if (n > list_cap) {
-                if (lane == 0) atomicOr(err, kErrListOverflow);
-                n = list_cap;
-            }
-            // 16-byte copies: the slot and the staging list start on 16-byte
-            // boundaries and hold n rounded up to 8 entries
             const uint64_t off = list_offset(lstart, total10, z, p);
-            const uint4 *src = reinterpret_cast<const uint4 *>(list);
-            uint4 *dst = reinterpret_cast<uint4 *>(lists + off);
-            for (int i = lane; i < ((n + 7) >> 3); i += 32) dst[i] = src[i];
+            const int room = (int)((lstart[p + 1] - lstart[p]) * (uint32_t)z);  // the slot, >= 10 (tn - tc) z
+            int n = compact_planes(pl, use, z == zmax, list, list_cap, lists + off, room);
+            if (n > room) {
+                if (lane == 0) atomicOr(err, kErrListOverflow);
+                n = room;
+            }
+            if (n <= list_cap) {
+                // 16-byte copies: the slot and the staging list start on
+                // 16-byte boundaries and hold n rounded up to 8 entries
+                const uint4 *src = reinterpret_cast<const uint4 *>(list);
+                uint4 *dst = reinterpret_cast<uint4 *>(lists + off);
+                for (int i = lane; i < ((n + 7) >> 3); i += 32) dst[i] = src[i];
+            }
             if (lane == 0) list_len[(size_t)(z - 1) * db.num_pep + p] = (uint16_t)n;
             my_lists += 1;
             my_entries += (unsigned long long)n;
             __syncwarp();
+        };
+        auto widen = [&](WordRange wr) {
+            if (wr.hi > wr.lo) {
+                all.lo = min(all.lo, wr.lo);
+                all.hi = max(all.hi, wr.hi);
+            }
+        };
+        for (int z = 1; z <= zmax; ++z) {
+            widen(build_planes_range<FastDiv>(pl, db.ions, tc, tn, r, z, z, nbins, mt_lane, NoMods{}));
+            emit_level(z);
         }
     }
     if (stats) {
@@ -730,7 +739,9 @@ int hfx_lists_generate(const DevDB &db, const int32_t *cover, int64_t npep1, int
                        unsigned long long *stats, uint32_t *err, cudaStream_t st) {
     const int nw = 8;
     const int32_t words = (nbins + 31) / 32;
-    list_cap = (std::max(32, std::min(list_cap, kMaxListLen)) + 7) & ~7;  // 16-byte staging lists
+    // 16-byte staging lists of up to kStageCap entries (longer lists are
+    // written directly)
+    list_cap = (std::max(32, std::min(list_cap, kStageCap)) + 7) & ~7;
     // per warp: three bit planes and a staging list of list_cap entries
     const size_t smem = (size_t)nw * 3 * words * 4 + (size_t)nw * list_cap * 2;
     int dev = 0, sms = 0;

@@ -6,24 +6,12 @@
 
 namespace hfx {
 
-// Warp-cooperative compaction of plane words [wr.lo, wr.hi) into the
-// ascending distinct-bin list `list` (entries (bin << 2) | level); clears the
-// words when `clear`.  Lane l takes k = ceil(words / 32) consecutive words,
-// so one scan places every lane's entries and the serial bit loop runs as
-// long as the fullest lane's k words, not a 32-word stripe's fullest word
-// per stripe.  Returns the number of distinct bins (may exceed cap; entries
-// beyond cap are dropped).
-__device__ __forceinline__ int compact_planes(const Planes &pl, WordRange wr, bool clear, uint16_t *list, int cap) {
-    const int lane = threadIdx.x & 31;
-    const int nwords = wr.hi - wr.lo;
-    if (nwords <= 0) return 0;
-    const int k = (nwords + 31) >> 5;
-    const int w0 = wr.lo + lane * k;
-    const int w1 = min(w0 + k, wr.hi);
-    int pc = 0;
-    for (int w = w0; w < w1; ++w) pc += __popc(pl.A[w] | pl.H[w]);
-    const int incl = warp_incl_scan(pc);
-    int pos = incl - pc;
+// Entries of one lane's plane words [w0, w1) from list position pos on
+// (entries at or beyond cap are dropped); clears the words when `clear`.
+// Inlined once per destination so that a staging list in shared memory is
+// written with shared-memory stores.
+__device__ __forceinline__ void emit_plane_entries(const Planes &pl, int w0, int w1, bool clear, int pos,
+                                                   uint16_t *list, int cap) {
     for (int w = w0; w < w1; ++w) {
         const uint32_t h = pl.H[w], tt = pl.T[w];
         uint32_t a = pl.A[w] | h;
@@ -41,10 +29,39 @@ __device__ __forceinline__ int compact_planes(const Planes &pl, WordRange wr, bo
             ++pos;
         }
     }
-    const int n = __shfl_sync(kFullMask, incl, 31);
-    __syncwarp();
-    return n;
 }
+
+// Warp-cooperative compaction of plane words [wr.lo, wr.hi) into the
+// ascending distinct-bin list (entries (bin << 2) | level); clears the
+// words when `clear`.  Lane l takes k = ceil(words / 32) consecutive words,
+// so one scan places every lane's entries and the serial bit loop runs as
+// long as the fullest lane's k words, not a 32-word stripe's fullest word
+// per stripe.  A list of up to `stage_cap` entries goes to the shared-memory
+// staging list `stage` (the caller copies it out in 16-byte pieces); a
+// longer one straight to `direct` (global memory, room for `direct_cap`
+// entries).  Returns the number of distinct bins (entries beyond the
+// destination's room are dropped).
+__device__ __forceinline__ int compact_planes(const Planes &pl, WordRange wr, bool clear, uint16_t *stage,
+                                              int stage_cap, uint16_t *direct, int direct_cap) {
+    const int lane = threadIdx.x & 31;
+    const int nwords = wr.hi - wr.lo;
+    if (nwords <= 0) return 0;
+    const int k = (nwords + 31) >> 5;
+    const int w0 = wr.lo + lane * k;
+    const int w1 = min(w0 + k, wr.hi);
+    int pc = 0;
+    for (int w = w0; w < w1; ++w) pc += __popc(pl.A[w] | pl.H[w]);
+    const int incl = warp_incl_scan(pc);
+    const int total = __shfl_sync(kFullMask, incl, 31);
+    if (total <= stage_cap) emit_plane_entries(pl, w0, w1, clear, incl - pc, stage, stage_cap);
+    else emit_plane_entries(pl, w0, w1, clear, incl - pc, direct, direct_cap);
+    __syncwarp();
+    return total;
+}
+
+// Room of the shared-memory staging list of one warp (entries): lists up to
+// this long are copied out in 16-byte pieces, longer ones written directly.
+constexpr int kStageCap = 1024;
 
 // Offset of the list of (level z, mass-order position p): every level has a
 // static region; position p's slot holds z * (10 (tn - tc) rounded up to 8)

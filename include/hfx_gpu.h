@@ -80,10 +80,11 @@ const char *hfx_last_error(const hfx_ctx *ctx);
 #define HFX_STAGE_SCORE 3       /* stages (c)+(d): ion ladders, gather-dot  */
 #define HFX_STAGE_TOPN 4        /* stage (e): top-N merge                   */
 #define HFX_STAGE_RESCORE 5     /* FP32 rescoring of the kept candidates    */
-#define HFX_STAGE_MODS 6        /* variable-modification isoforms           */
+#define HFX_STAGE_MODS 6        /* scoring of the modified isoforms         */
 #define HFX_STAGE_LISTS 7       /* per-peptide ion lists of the batch       */
 #define HFX_STAGE_PACK 8        /* interleaved spectrum tiles of the groups */
-#define HFX_NSTAGES 9
+#define HFX_STAGE_MOD_LISTS 9   /* isoform windows, planning, ion lists     */
+#define HFX_NSTAGES 10
 int32_t hfx_set_profiling(hfx_ctx *ctx, int32_t on);
 /* Caps the bytes of the context's search workspaces (new; the reference
  * sizes its dense matrices to the free memory, Search.hs:427-433): a call
@@ -100,6 +101,13 @@ int32_t hfx_stage_stats(hfx_ctx *ctx, double *ms, int64_t *launches, int64_t *un
  * [6] residues read by the list generator (one peptide's once per step),
  * [7] spectrum-tile bytes staged into shared memory by the scorer. */
 int32_t hfx_search_counters(hfx_ctx *ctx, uint64_t *out8, int32_t reset);
+/* Work counters of the modification search over isoform lists
+ * (batch_mode 1), accumulated while profiling is on: [0] isoform ion lists
+ * built, [1] their entries, [2] isoforms handed to the scorer, [3] list
+ * entries streamed by the scorer, [4] modified peptide-spectrum pairs,
+ * [5] isoform records built, [6] residues read by the isoform-list
+ * generator, [7] spectrum-tile bytes staged by the scorer. */
+int32_t hfx_mod_counters(hfx_ctx *ctx, uint64_t *out8, int32_t reset);
 
 /* Digest proteins into the search database and upload it.  Replaces
  * Fragment.hs:197-233 makeSeqDB + :239-258 withDeviceDB + sort.cu:28-35

@@ -150,6 +150,30 @@ def test_search_mods_graph_replay(mods_full, oracle, precision):
         _compare(eng.search(sp, p), ref, f"mods graph replay {rep} precision {precision}")
 
 
+def test_mod_counters_account_for_every_pair(mods_full, oracle):
+    """With profiling on, the pairs scored by the unmodified list scorer and
+    by the isoform-list scorer add up to the oracle's candidate counts; the
+    isoform lists are timed as their own stage."""
+    import hfx_gb300
+    eng, prot, sp = mods_full
+    ref = oracle.search(*_oracle_db(oracle, eng, prot), sp, topn=10, ma=MA, ma_mass=MA_MASS, max_ma=4)
+    eng.set_profiling(True)
+    try:
+        eng.stage_stats(reset=True)
+        eng.counters(reset=True)
+        eng.mod_counters(reset=True)
+        res = eng.search(sp, hfx_gb300.default_params(top_n=10, batch_mode=1))
+        st = eng.stage_stats(reset=True)
+        plain, mods = eng.counters(reset=True), eng.mod_counters(reset=True)
+    finally:
+        eng.set_profiling(False)
+    _compare(res, ref, "mods with profiling")
+    assert plain["pairs"] + mods["pairs"] == int(ref[4].sum())
+    assert mods["pairs"] > 0 and mods["isoforms"] > 0 and mods["list_entries"] > 0
+    assert mods["entries_streamed"] > 0 and mods["tile_bytes"] > 0 and mods["residues_read"] > 0
+    assert st["mod_lists"][1] > 0 and st["mods"][1] == 1
+
+
 @pytest.mark.parametrize("precision", [1, 2])
 def test_search_mods_lowp_rescore(mods_full, oracle, precision):
     """BF16 / FP16 rows choose the kept candidates (modified included), FP32
