@@ -6,10 +6,12 @@
 
 namespace hfx {
 
-// Entries of one lane's plane words [w0, w1) from list position pos on
-// (entries at or beyond cap are dropped); clears the words when `clear`.
-// Inlined once per destination so that a staging list in shared memory is
-// written with shared-memory stores.
+// Entries of one lane's plane words [w0, w1) from list position pos on;
+// clears the words when `clear`.  kChecked drops entries at or beyond cap
+// (a list longer than its destination); otherwise the caller has checked
+// that the whole list fits.  Inlined once per destination so that a staging
+// list in shared memory is written with shared-memory stores.
+template <bool kChecked>
 __device__ __forceinline__ void emit_plane_entries(const Planes &pl, int w0, int w1, bool clear, int pos,
                                                    uint16_t *list, int cap) {
     for (int w = w0; w < w1; ++w) {
@@ -25,7 +27,7 @@ __device__ __forceinline__ void emit_plane_entries(const Planes &pl, int w0, int
             const int b = __ffs(a) - 1;
             a &= a - 1u;
             const uint32_t key = base + ((uint32_t)b << 2) + ((h >> b) & 1u) + ((tt >> b) & 1u);
-            if (pos < cap) list[pos] = (uint16_t)key;
+            if (!kChecked || pos < cap) list[pos] = (uint16_t)key;
             ++pos;
         }
     }
@@ -53,8 +55,9 @@ __device__ __forceinline__ int compact_planes(const Planes &pl, WordRange wr, bo
     for (int w = w0; w < w1; ++w) pc += __popc(pl.A[w] | pl.H[w]);
     const int incl = warp_incl_scan(pc);
     const int total = __shfl_sync(kFullMask, incl, 31);
-    if (total <= stage_cap) emit_plane_entries(pl, w0, w1, clear, incl - pc, stage, stage_cap);
-    else emit_plane_entries(pl, w0, w1, clear, incl - pc, direct, direct_cap);
+    if (total <= stage_cap) emit_plane_entries<false>(pl, w0, w1, clear, incl - pc, stage, stage_cap);
+    else if (total <= direct_cap) emit_plane_entries<false>(pl, w0, w1, clear, incl - pc, direct, direct_cap);
+    else emit_plane_entries<true>(pl, w0, w1, clear, incl - pc, direct, direct_cap);
     __syncwarp();
     return total;
 }
