@@ -48,12 +48,19 @@ METRIC = "peptide-spectrum XCorrs/s"
 UNIT = "PSM/s"
 KERNELS = {0: "k_score_spectrum", 1: "k_score_lists", 2: "k_score_batched"}
 
-# DRAM bytes (read + write) per launch, from one-pass ncu captures of the
-# default workload (summaries under profiles/), keyed by (kernel, workload,
-# precision, spectra).  Each figure carries the hash of the kernel's source
-# files at capture time; when the source has changed since, the figure is
-# not reported (traffic null, marked stale).
-KERNEL_SRC = ["hfx_gb300/csrc/lists.cu", "hfx_gb300/csrc/device_common.cuh", "hfx_gb300/csrc/batched_common.cuh"]
+# DRAM bytes (read + write) per launch, from ncu captures (summaries under
+# profiles/), keyed by (kernel, workload, precision, spectra).  Each figure
+# carries the hash of the kernel's source files at capture time; when the
+# source has changed since, the figure is not reported (traffic null, marked
+# stale).
+_COMMON_SRC = ["hfx_gb300/csrc/device_common.cuh", "hfx_gb300/csrc/batched_common.cuh",
+               "hfx_gb300/csrc/lists_device.cuh"]
+KERNEL_SRC = {
+    "k_gen_lists": ["hfx_gb300/csrc/lists.cu"] + _COMMON_SRC,
+    "k_score_lists": ["hfx_gb300/csrc/lists.cu"] + _COMMON_SRC,
+    "k_gen_iso_lists": ["hfx_gb300/csrc/iso_lists.cu", "hfx_gb300/csrc/mods_device.cuh"] + _COMMON_SRC,
+    "k_score_iso_lists": ["hfx_gb300/csrc/iso_lists.cu", "hfx_gb300/csrc/mods_device.cuh"] + _COMMON_SRC,
+}
 TRAFFIC = {}
 
 
@@ -91,8 +98,9 @@ def _args():
     return ap.parse_args()
 
 
-def _src_hash(files=KERNEL_SRC):
+def _src_hash(kern):
     import hashlib
+    files = KERNEL_SRC.get(kern, ["hfx_gb300/csrc/lists.cu"] + _COMMON_SRC)
     h = hashlib.sha1()
     for f in files:
         with open(os.path.join(ROOT, f), "rb") as fh:
@@ -105,7 +113,7 @@ def _traffic(kern, workload, prec, ns):
     t = TRAFFIC.get((kern, workload, prec, ns))
     if t is None:
         return None, "no capture for this kernel and workload"
-    if t["src"] != _src_hash():
+    if t["src"] != _src_hash(kern):
         return None, "stale: kernel source changed since the capture"
     return t["bytes"], t["profile"]
 

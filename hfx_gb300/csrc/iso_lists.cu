@@ -153,39 +153,76 @@ __global__ void k_iso_expand(DevDB db, const int32_t *__restrict__ count, const 
     }
 }
 
-// 4a. one warp per isoform: the residues it modifies (modable-acid counts,
-// isoform count, unranking, gen_mod_pep.cu:127-227 and mion_series.cu:244-286),
-// pos_words words per record in iso_pos.  Kept apart from the list builder,
-// whose registers would otherwise be sized by the unranking's state.
+// 4a. one thread per isoform: the residues it modifies (modable-acid
+// counts, isoform count, unranking, gen_mod_pep.cu:127-227, and the i-th
+// acid counter of mion_series.cu:244-286 / check_series.cu:62-100),
+// pos_words words per record in iso_pos.  The per-residue decision is
+// ModIsoform::chunk_add's, residue by residue; consecutive records are
+// mostly the ranks of one (combination, peptide), so a warp's threads run
+// the same loops.
 __global__ void __launch_bounds__(256) k_iso_positions(DevDB db, DevMods mods, const int32_t *__restrict__ total_p,
                                                        uint32_t cap_iso, const uint64_t *__restrict__ iso_key,
                                                        int32_t pos_words, uint32_t *__restrict__ iso_pos,
                                                        uint32_t *__restrict__ err) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const uint32_t total = min((uint32_t)*total_p, cap_iso);
-    for (uint32_t t = blockIdx.x * nw + warp; t < total; t += gridDim.x * nw) {
-        const uint64_t key = iso_key[t];
-        const int32_t mu = (int32_t)((key >> 54) & 0x1FFu);
-        const uint32_t p = (uint32_t)((key >> 27) & 0x7FFFFFFu), rank = (uint32_t)(key & 0x7FFFFFFu);
-        uint32_t *bits = iso_pos + (size_t)t * pos_words;
-        if (key == ~0ull || p >= db.num_pep || mu >= mods.num_mod) continue;  // a skipped record
-        const uint32_t tc = db.tc_sorted[p], tn = db.tn_sorted[p];
-        if (tn > tc && (int64_t)(tn - tc) > 32ll * pos_words) {  // longer than the database's longest peptide
-            if (lane == 0) atomicOr(err, kErrBounds);
-            for (int i = lane; i < pos_words; i += 32) bits[i] = 0u;
-            continue;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const uint64_t key = iso_key[t];
+    const int32_t mu = (int32_t)((key >> 54) & 0x1FFu);
+    const uint32_t p = (uint32_t)((key >> 27) & 0x7FFFFFFu), rank = (uint32_t)(key & 0x7FFFFFFu);
+    uint32_t *bits = iso_pos + (size_t)t * pos_words;
+    if (key == ~0ull || p >= db.num_pep || mu >= mods.num_mod) return;  // a skipped record
+    const uint32_t tc = db.tc_sorted[p], tn = db.tn_sorted[p];
+    const int num_ma = mods.num_ma;
+    if (tn > tc && (int64_t)(tn - tc) > 32ll * pos_words) {  // longer than the database's longest peptide
+        atomicOr(err, kErrBounds);
+        for (int i = 0; i < pos_words; ++i) bits[i] = 0u;
+        return;
+    }
+    // modable-acid counts (filter_by_mod.cu:216-230)
+    uint32_t D[kMaxMa];
+#pragma unroll
+    for (int i = 0; i < kMaxMa; ++i) D[i] = 0u;
+    for (uint32_t j = tc; j < tn; ++j) {
+        const uint32_t ty = ((uint32_t)__ldg(db.ions + j) >> 5) & 7u;
+#pragma unroll
+        for (int i = 0; i < kMaxMa; ++i) D[i] += (i < num_ma && ty == (uint32_t)(i + 1)) ? 1u : 0u;
+    }
+    const int32_t *dcount = mods.counts + (size_t)mu * num_ma;
+    uint32_t scan[kMaxMa];
+    uint64_t mask[kMaxMa];
+    const uint32_t niso = isoform_count(D, dcount, num_ma, scan);
+    if (rank >= niso || !isoform_masks(D, scan, dcount, num_ma, rank, mask)) {
+        atomicOr(err, kErrKeyOverflow);
+        for (int i = 0; i < pos_words; ++i) bits[i] = 0u;
+        return;
+    }
+    // the i-th acid counter, in peptide order
+    uint32_t seen_any = 0u, seen[kMaxMa];
+#pragma unroll
+    for (int i = 0; i < kMaxMa; ++i) seen[i] = 0u;
+    uint32_t word = 0u;
+    for (uint32_t j = tc; j < tn; ++j) {
+        const uint32_t ty = ((uint32_t)__ldg(db.ions + j) >> 5) & 7u;
+        uint32_t k = seen_any, ts = 0u;
+        uint64_t m = 0ull;
+#pragma unroll
+        for (int i = 0; i < kMaxMa; ++i) {
+            if (i < num_ma && ty == (uint32_t)(i + 1)) {
+                ts = seen[i];
+                m = mask[i];
+                seen[i] += 1u;
+            }
         }
-        const int32_t *dcount = mods.counts + (size_t)mu * mods.num_ma;
-        uint32_t D[kMaxMa], scan[kMaxMa];
-        uint64_t mask[kMaxMa];
-        modable_counts(db.ions, tc, tn, mods.num_ma, D);
-        const uint32_t niso = isoform_count(D, dcount, mods.num_ma, scan);
-        if (rank >= niso || !isoform_masks(D, scan, dcount, mods.num_ma, rank, mask)) {
-            if (lane == 0) atomicOr(err, kErrKeyOverflow);
-            for (int i = lane; i < pos_words; i += 32) bits[i] = 0u;
-            continue;
+        if (mods.per_type) k = ts;
+        seen_any += ty != 0u ? 1u : 0u;
+        const bool modded = ty != 0u && (int)ty <= num_ma && k < 64u && ((m >> k) & 1ull);
+        const uint32_t r = j - tc;
+        word |= (modded ? 1u : 0u) << (r & 31u);
+        if ((r & 31u) == 31u || j + 1 == tn) {
+            bits[r >> 5] = word;
+            word = 0u;
         }
-        isoform_positions(db.ions, tc, tn, mask, mods.num_ma, mods.per_type, bits);
     }
 }
 
@@ -614,7 +651,8 @@ int hfx_iso_generate(const DevDB &db, const DevMods &m, const int32_t *cover, in
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    k_iso_positions<<<sms * 8, 256, 0, st>>>(db, m, total_p, cap_iso, iso_key, pos_words, iso_pos, err);
+    k_iso_positions<<<(unsigned)((cap_iso + 255) / 256), 256, 0, st>>>(db, m, total_p, cap_iso, iso_key, pos_words,
+                                                                        iso_pos, err);
     auto f = fastdiv ? k_gen_iso_lists<true> : k_gen_iso_lists<false>;
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
