@@ -61,7 +61,24 @@ KERNEL_SRC = {
     "k_gen_iso_lists": ["hfx_gb300/csrc/iso_lists.cu", "hfx_gb300/csrc/mods_device.cuh"] + _COMMON_SRC,
     "k_score_iso_lists": ["hfx_gb300/csrc/iso_lists.cu", "hfx_gb300/csrc/mods_device.cuh"] + _COMMON_SRC,
 }
-TRAFFIC = {}
+# Scaled captures: the DRAM bytes of one launch on the 2,000-spectrum (full)
+# or 1,000-spectrum (mods) case, times the ratio of the full-size launch's
+# moved bytes (the run's work counters, per-kernel basis below) to the small
+# case's.
+TRAFFIC = {
+    ("k_gen_lists", "full", 1, 10000): {
+        "src": "832f5404fab6", "bytes": 2208155082,
+        "profile": "profiles/k_gen_lists_2k_bf16.md (2,000-spectrum capture x 1.729 moved-bytes ratio)"},
+    ("k_score_lists", "full", 1, 10000): {
+        "src": "832f5404fab6", "bytes": 3323938567,
+        "profile": "profiles/k_score_lists_2k_bf16.md (2,000-spectrum capture x 2.482 moved-bytes ratio)"},
+    ("k_gen_iso_lists", "mods", 1, 10000): {
+        "src": "1615297cc087", "bytes": 50189462418,
+        "profile": "profiles/iso_lists_mods1k_bf16.md (1,000-spectrum capture x 3.904 moved-bytes ratio)"},
+    ("k_score_iso_lists", "mods", 1, 10000): {
+        "src": "1615297cc087", "bytes": 62845138690,
+        "profile": "profiles/iso_lists_mods1k_bf16.md (1,000-spectrum capture x 4.816 moved-bytes ratio)"},
+}
 
 
 def _args():
