@@ -678,7 +678,8 @@ def main():
         # the search with E-values (eager), against the same search without
         pe = hfx_gb300.default_params(top_n=cfg["top_n"], precision=prec, batch_mode=1, rescore_k=rk,
                                       group_size=p.group_size, chunk=p.chunk, **_pkw(cfg))
-        oe = dict(out, ev=torch.empty((ns, tn_), dtype=torch.float64, device=d),
+        oe = {k: torch.empty_like(v) for k, v in out.items()}
+        oe.update(ev=torch.empty((ns, tn_), dtype=torch.float64, device=d),
                   fit=torch.empty((ns, 3), dtype=torch.float64, device=d))
         eng.search_evalues(dev, pe, oe)
         torch.cuda.synchronize()
@@ -702,7 +703,8 @@ def main():
         fitted = oe["fit"][:, 2].cpu().numpy()
         line["evalues"] = {"ms_per_search": t_ev / n_e, "ms_search_alone": t_plain / n_e,
                            "ratio": t_ev / max(1e-9, t_plain), "spectra_with_fit": float(np.mean(fitted >= 2)),
-                           "launch": "eager"}
+                           "launch": "eager",
+                           "top_keys_equal": bool(np.array_equal(oe["key"].cpu().numpy().view(np.uint64), key))}
     if plain is not None:
         line["plain_fp32"] = plain
     if rank == 0 and not a.no_cpu:

@@ -161,6 +161,11 @@ struct hfx_ctx {
 
     // HFX_DEBUG_SYNC=1: synchronize after every stage and remember the first
     // stage whose kernels reported an error (for locating device faults)
+    // hfx_search_evalues without modifications: the FP32 list search also
+    // writes every pair's score into the E-value sink (one scoring pass)
+    bool ev_single = false;
+    float *ev_sink = nullptr;
+
     bool debug_sync = false;
     std::string fault_stage;
     std::string err_stage;  // with debug_sync: the first stage after which the device error word was set
@@ -738,9 +743,29 @@ int32_t search_batched(hfx_ctx *ctx, const hfx_search_params *p, const Batch &b,
         if (rc) return cuda_fail(ctx, (cudaError_t)rc, "ion lists");
         ctx->stage_end(HFX_STAGE_LISTS, 5, 0);
         ctx->stage_begin(HFX_STAGE_SCORE);
+        float *sink = nullptr;
+        const uint64_t *sink_off = nullptr;
+        if (ctx->ev_single && elem_kind == 0 && ctx->gmode == 0) {
+            // E-values in the same pass: each spectrum's window of scores
+            // at its offset in the sink (Search.hs:116-121)
+            uint64_t *size = ctx->buf<uint64_t>("e_size", ns, e);
+            uint64_t *soff = e ? nullptr : ctx->buf<uint64_t>("e_off", ns, e);
+            uint64_t *send = e ? nullptr : ctx->buf<uint64_t>("e_end", ns, e);
+            unsigned long long *cur = e ? nullptr : ctx->buf<unsigned long long>("e_cursor", ns, e);
+            if (e) return cuda_fail(ctx, e, "alloc");
+            rc = hfx_evalue_offsets(wb, we, 1, nullptr, ns, size, soff, send, cur, ctx->stream);
+            if (rc) return cuda_fail(ctx, (cudaError_t)rc, "E-value offsets");
+            uint64_t total = 0;
+            HFX_CUDA(cudaMemcpyAsync(&total, send + ns - 1, 8, cudaMemcpyDeviceToHost, ctx->stream), "D2H total");
+            HFX_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+            sink = ctx->buf<float>("e_sink", total + 1, e);
+            if (e) return cuda_fail(ctx, e, "alloc E-value scores");
+            sink_off = soff;
+            ctx->ev_sink = sink;
+        }
         rc = hfx_lists_score(lists, long_rows, ctx->d_lstart.as<uint32_t>(), total10, llen, (uint32_t)ctx->num_pep,
                              elem_kind, stride, wb, we, ws, tiles, G, K, 0, ps, pk, stats,
-                             ctx->d_err.as<uint32_t>(), ctx->stream);
+                             ctx->d_err.as<uint32_t>(), ctx->stream, sink, sink_off);
         if (rc) return cuda_fail(ctx, (cudaError_t)rc, "k_score_lists");
         ctx->stage_end(HFX_STAGE_SCORE, 1, 0);
         if (stats) {
@@ -1438,11 +1463,36 @@ int32_t hfx_search_evalues(hfx_ctx *ctx, const hfx_search_params *p, const float
     if (nspec == 0) return HFX_OK;
     const bool mods_on = p->search_mods != 0 && ctx->num_mod > 0;
     const bool plain_on = p->search_plain != 0;
+    Batch b{mz, it, pcr, z, tol, off, nspec};
+    if (!mods_on && plain_on) {
+        // one FP32 pass over the step's ion lists scores every pair into the
+        // sink and keeps the top-N: the same top-N as a BF16/FP16 search
+        // rescored in FP32 (both are the FP32 search's), without a second
+        // scoring pass
+        hfx_search_params q = *p;
+        q.batch_mode = 1;
+        q.use_graph = 0;
+        q.precision = 0;
+        q.group_size = 0;
+        ctx->ev_single = true;
+        ctx->ev_sink = nullptr;
+        int32_t rc = search_device(ctx, &q, b, out_s, out_k, out_pep, out_ncand);
+        ctx->ev_single = false;
+        if (rc) return rc;
+        if (!ctx->ev_sink) return fail(ctx, HFX_ERR_UNSUPPORTED, "E-value scores were not written");
+        cudaError_t e;
+        const uint64_t *soff = ctx->buf<uint64_t>("e_off", nspec, e);
+        const uint64_t *size = e ? nullptr : ctx->buf<uint64_t>("e_size", nspec, e);
+        if (e) return cuda_fail(ctx, e, "alloc");
+        rc = hfx_evalue_select_fit(ctx->ev_sink, soff, size, nspec, bin_width, cutoff_perc, out_fit, ctx->stream);
+        if (!rc) rc = hfx_evalue_apply(out_s, out_k, out_fit, nspec, p->top_n, out_ev, ctx->stream);
+        if (rc) return cuda_fail(ctx, (cudaError_t)rc, "E-values");
+        return search_finish(ctx);
+    }
     // the search over the step's ion lists, eagerly
     hfx_search_params q = *p;
     q.batch_mode = 1;
     q.use_graph = 0;
-    Batch b{mz, it, pcr, z, tol, off, nspec};
     int32_t rc = search_device(ctx, &q, b, out_s, out_k, out_pep, out_ncand);
     if (rc) return rc;
     // every candidate's FP32 score (Search.hs:116-121: the unmodified

@@ -676,10 +676,10 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
                 my_psm += (uint32_t)__popc(cur.act);
                 const float sc = reduce_scatter<G>(acc);
                 if (sink) {
-                    // every pair's score, at its member's window offset
+                    // every pair's score, at its member's window offset (the
+                    // admission below still keeps the top-K)
                     if ((lane & (32 / G - 1)) == 0 && ((cur.act >> my_slot) & 1u))
                         sink[s_off[my_slot] + (cur.p - s_wb[my_slot])] = sc;
-                    continue;
                 }
                 const bool want = (lane & (32 / G - 1)) == 0 && ((cur.act >> my_slot) & 1u) &&
                                   score_order(sc) >= *(volatile uint32_t *)(thr_u + my_slot);
