@@ -61,22 +61,22 @@ KERNEL_SRC = {
     "k_gen_iso_lists": ["hfx_gb300/csrc/iso_lists.cu", "hfx_gb300/csrc/mods_device.cuh"] + _COMMON_SRC,
     "k_score_iso_lists": ["hfx_gb300/csrc/iso_lists.cu", "hfx_gb300/csrc/mods_device.cuh"] + _COMMON_SRC,
 }
-# Scaled captures: the DRAM bytes of one launch on the 2,000-spectrum (full)
-# or 1,000-spectrum (mods) case, times the ratio of the full-size launch's
-# moved bytes (the run's work counters, per-kernel basis below) to the small
-# case's.
+# Scaled captures: the DRAM bytes (and the warp instructions, `inst`) of one
+# launch on the 2,000-spectrum (full) or 1,000-spectrum (mods) case, times
+# the ratio of the full-size launch's moved bytes (the run's work counters,
+# per-kernel basis below) to the small case's.
 TRAFFIC = {
     ("k_gen_lists", "full", 1, 10000): {
-        "src": "832f5404fab6", "bytes": 2208155082,
+        "src": "832f5404fab6", "bytes": 2208155082, "inst": 4522766000,
         "profile": "profiles/k_gen_lists_2k_bf16.md (2,000-spectrum capture x 1.729 moved-bytes ratio)"},
     ("k_score_lists", "full", 1, 10000): {
-        "src": "832f5404fab6", "bytes": 3323938567,
+        "src": "832f5404fab6", "bytes": 3323938567, "inst": 2311438000,
         "profile": "profiles/k_score_lists_2k_bf16.md (2,000-spectrum capture x 2.482 moved-bytes ratio)"},
     ("k_gen_iso_lists", "mods", 1, 10000): {
-        "src": "1615297cc087", "bytes": 50189462418,
+        "src": "1615297cc087", "bytes": 50189462418, "inst": 91095400000,
         "profile": "profiles/iso_lists_mods1k_bf16.md (1,000-spectrum capture x 3.904 moved-bytes ratio)"},
     ("k_score_iso_lists", "mods", 1, 10000): {
-        "src": "1615297cc087", "bytes": 62845138690,
+        "src": "1615297cc087", "bytes": 62845138690, "inst": 31132060000,
         "profile": "profiles/iso_lists_mods1k_bf16.md (1,000-spectrum capture x 4.816 moved-bytes ratio)"},
 }
 
@@ -125,14 +125,15 @@ def _src_hash(kern):
     return h.hexdigest()[:12]
 
 
-def _traffic(kern, workload, prec, ns):
-    """(bytes per launch, note) of a captured kernel, None when absent or stale."""
+def _traffic(kern, workload, prec, ns, field="bytes"):
+    """(bytes or instructions per launch, note) of a captured kernel, None
+    when absent or stale."""
     t = TRAFFIC.get((kern, workload, prec, ns))
     if t is None:
         return None, "no capture for this kernel and workload"
     if t["src"] != _src_hash(kern):
         return None, "stale: kernel source changed since the capture"
-    return t["bytes"], t["profile"]
+    return t[field], t["profile"]
 
 
 def _relaunch(a):
@@ -632,6 +633,16 @@ def main():
         kern_rows[kname] = {"stage_ms_per_step": ms_st, "share": ms_st / max(1e-9, step_ms_all),
                             "moved_bytes": moved, "bytes_basis": basis, "achieved": ach, "frac": ach / peak,
                             "traffic": tr, "traffic_note": tr_note}
+        # the axis that binds these kernels: warp-instruction issue (4 per
+        # SM per cycle at the highest SM clock seen)
+        ins, _ = _traffic(kname, a.workload, prec, ns, "inst")
+        if ins:
+            mhz = (clocks or {}).get("sm_max_mhz") or 2070.0
+            peak_i = torch.cuda.get_device_properties(d).multi_processor_count * 4 * mhz * 1e6
+            ach_i = ins / (ms_st / 1000.0)
+            kern_rows[kname]["issue"] = {"warp_inst_per_launch": ins, "achieved": ach_i, "peak": peak_i,
+                                         "unit": "warp instructions/s", "frac": ach_i / peak_i,
+                                         "basis": "ncu warp instructions of the small case, scaled like traffic"}
     dom = max(kern_rows, key=lambda k: kern_rows[k]["stage_ms_per_step"]) if kern_rows else kern
     drow = kern_rows.get(dom, {})
     step_ach = bpp * psm_step / (ms_step / 1000.0) / 1e9
@@ -664,6 +675,7 @@ def main():
                      "peak_kind": peak_kind,
                      "binding": "SM instruction issue and shared-memory wavefronts, not DRAM "
                                 "(ncu summaries under profiles/)",
+                     "issue": drow.get("issue"),
                      "kernels": kern_rows,
                      "step": {"achieved": step_ach, "frac": step_ach / peak, "bytes_per_psm": bpp,
                               "mean_distinct_bins": meanU, "u_basis": u_basis,
