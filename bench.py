@@ -67,11 +67,11 @@ KERNEL_SRC = {
 # per-kernel basis below) to the small case's.
 TRAFFIC = {
     ("k_gen_lists", "full", 1, 10000): {
-        "src": "832f5404fab6", "bytes": 2208155082, "inst": 4522766000,
+        "src": "b1c26e9ec340", "bytes": 2207584533, "inst": 4522799000,
         "profile": "profiles/k_gen_lists_2k_bf16.md (2,000-spectrum capture x 1.729 moved-bytes ratio)"},
     ("k_score_lists", "full", 1, 10000): {
-        "src": "832f5404fab6", "bytes": 3323938567, "inst": 2311438000,
-        "profile": "profiles/k_score_lists_2k_bf16.md (2,000-spectrum capture x 2.482 moved-bytes ratio)"},
+        "src": "b1c26e9ec340", "bytes": 3323255988, "inst": 2310098000,
+        "profile": "profiles/k_score_lists_2k_bf16.md (2,000-spectrum capture x 2.481 moved-bytes ratio)"},
     ("k_gen_iso_lists", "mods", 1, 10000): {
         "src": "1615297cc087", "bytes": 50189462418, "inst": 91095400000,
         "profile": "profiles/iso_lists_mods1k_bf16.md (1,000-spectrum capture x 3.904 moved-bytes ratio)"},

@@ -226,6 +226,44 @@ def test_search_mods_edge_charges(mods_tiny, oracle):
     assert (res.score[2][res.key[2] != np.iinfo(np.uint64).max] == 0).all()
 
 
+@pytest.mark.parametrize("precision,graph", [(0, 0), (1, 0), (1, 1), (0, 1)])
+def test_search_mods_empty_and_one_peak(mods_tiny, oracle, precision, graph):
+    """The isoform-list path on an empty spectrum, a one-peak spectrum and an
+    (almost) empty window, eager and replayed; then a batch with no
+    candidate at all (no isoform records)."""
+    import hfx_gb300
+    eng, prot, sp = mods_tiny
+    sub = sp.subset(np.arange(6))
+    mz, it, off = [], [], [0]
+    for i in range(6):
+        a, b = sub.off[i], sub.off[i + 1]
+        if i == 0:
+            a = b                                   # empty spectrum
+        if i == 3:
+            a = b - 1                               # one peak
+        mz.append(sub.mz[a:b])
+        it.append(sub.it[a:b])
+        off.append(off[-1] + (b - a))
+    sub.mz, sub.it, sub.off = np.concatenate(mz), np.concatenate(it), np.array(off, np.int64)
+    sub.tol[1] = 1e-7
+    db = _oracle_db(oracle, eng, prot)
+    ref = oracle.search(*db, sub, topn=10, ma=MA, ma_mass=MA_MASS, max_ma=4)
+    p = hfx_gb300.default_params(top_n=10, batch_mode=1, precision=precision, use_graph=graph,
+                                 rescore_k=32 if precision else 0)
+    for rep in range(2 if graph else 1):
+        _compare(eng.search(sub, p), ref, f"mods empty/one-peak precision={precision} graph={graph} rep={rep}")
+    none = sp.subset(np.arange(4))
+    none.z[:] = 2.0
+    none.pcr[:] = 3900.0                            # above every peptide and isoform mass
+    none.tol[:] = 1.0
+    ref = oracle.search(*db, none, topn=10, ma=MA, ma_mass=MA_MASS, max_ma=4)
+    assert int(ref[4].sum()) == 0
+    for rep in range(2 if graph else 1):
+        res = eng.search(none, p)
+        _compare(res, ref, f"mods no candidates precision={precision} graph={graph} rep={rep}")
+        assert (res.key == np.iinfo(np.uint64).max).all()
+
+
 def _ref_match(prot, r, tc, tn, k, ions, counts=None, rank=None, per_type=False, oracle=None):
     """Location.hs:42-58 lookup and Fragment.hs:84-106 modifyFragment,
     transcribed independently: peptide text with flanks, (M+H)+, '*' after

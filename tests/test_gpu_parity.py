@@ -164,11 +164,9 @@ def test_search_deterministic(full_engine):
     assert np.array_equal(a.key, b.key)
 
 
-def test_search_edge_cases(tiny_engine, oracle):
-    """Empty spectrum, empty window, charge without ions (max charge > 4
-    scores 0 in the reference's plain kernel), a one-peak spectrum."""
-    import hfx_gb300
-    eng, prot, sp = tiny_engine
+def _edge_spectra(sp):
+    """Six spectra: an empty one, an (almost) empty window, a charge without
+    ions (max charge 5), a one-peak spectrum and two ordinary ones."""
     sub = sp.subset(np.arange(6))
     mz, it, off = [], [], [0]
     for i in range(6):
@@ -183,11 +181,50 @@ def test_search_edge_cases(tiny_engine, oracle):
     sub.mz, sub.it, sub.off = np.concatenate(mz), np.concatenate(it), np.array(off, np.int64)
     sub.tol[1] = 1e-7                               # (almost) empty window
     sub.z[2] = 6.0                                  # max charge 5: no ions
+    return sub
+
+
+# (batch_mode, precision, use_graph): the per-spectrum path, the list path in
+# FP32 and BF16 (eager and replayed) and the fused path
+EDGE_MODES = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (1, 1, 1), (1, 0, 1), (2, 0, 0)]
+
+
+@pytest.mark.parametrize("mode,precision,graph", EDGE_MODES)
+def test_search_edge_cases(tiny_engine, oracle, mode, precision, graph):
+    """Empty spectrum, empty window, charge without ions (max charge > 4
+    scores 0 in the reference's plain kernel), a one-peak spectrum, on
+    every search path."""
+    import hfx_gb300
+    eng, prot, sp = tiny_engine
+    sub = _edge_spectra(sp)
     ref = oracle.search(*_oracle_db(oracle, eng, prot), sub, topn=10)
-    res = eng.search(sub, hfx_gb300.default_params(top_n=10))
-    _compare(res, ref, "edges")
-    assert res.ncand[0] == 0
-    assert (res.score[2][res.key[2] != np.iinfo(np.uint64).max] == 0).all()
+    p = hfx_gb300.default_params(top_n=10, batch_mode=mode, precision=precision, use_graph=graph,
+                                 rescore_k=32 if precision else 0)
+    for rep in range(2 if graph else 1):
+        res = eng.search(sub, p)
+        _compare(res, ref, f"edges mode={mode} precision={precision} graph={graph} rep={rep}")
+        assert res.ncand[0] == 0
+        assert (res.score[2][res.key[2] != np.iinfo(np.uint64).max] == 0).all()
+
+
+@pytest.mark.parametrize("mode,precision,graph", EDGE_MODES)
+def test_no_candidates_in_the_batch(tiny_engine, oracle, mode, precision, graph):
+    """A batch whose windows are all empty (precursors far above the
+    database): no lists, no work items, every result the empty key."""
+    import hfx_gb300
+    eng, prot, sp = tiny_engine
+    sub = sp.subset(np.arange(5))
+    sub.z[:] = 2.0
+    sub.pcr[:] = 3900.0                             # ~7,798 Da: above every peptide, rows < 8,192 bins
+    sub.tol[:] = 1.0
+    ref = oracle.search(*_oracle_db(oracle, eng, prot), sub, topn=10)
+    assert int(ref[4].sum()) == 0
+    p = hfx_gb300.default_params(top_n=10, batch_mode=mode, precision=precision, use_graph=graph,
+                                 rescore_k=32 if precision else 0)
+    for rep in range(2 if graph else 1):
+        res = eng.search(sub, p)
+        _compare(res, ref, f"no candidates mode={mode} precision={precision} graph={graph} rep={rep}")
+        assert (res.key == np.iinfo(np.uint64).max).all()
 
 
 @pytest.mark.parametrize("mode", [1, 2])
