@@ -344,6 +344,10 @@ k_score_iso_lists(const uint16_t *__restrict__ lists, uint64_t list_total, const
                   uint32_t *__restrict__ err) {
     static_assert(kC == 1 || kC == 4, "1 or 4 isoforms per warp");
     constexpr int kW = 32 / kC;
+    // FP32 with four isoforms per warp keeps the canonical order: entry i of
+    // a list goes to partial sum i % 32, i.e. entry k of each round of 32 to
+    // this lane's partial set k (8 lanes per isoform)
+    constexpr bool kSets4 = std::is_same<T, float>::value && kC > 1;
     static_assert(G <= kW, "a lane group takes up to one spectrum of the group per lane");
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -457,6 +461,11 @@ k_score_iso_lists(const uint16_t *__restrict__ lists, uint64_t list_total, const
             float acc[G];
 #pragma unroll
             for (int j = 0; j < G; ++j) acc[j] = 0.0f;
+            float acc4[kSets4 ? 4 : 1][G];
+#pragma unroll
+            for (int k = 0; k < (kSets4 ? 4 : 1); ++k)
+#pragma unroll
+                for (int j = 0; j < G; ++j) acc4[k][j] = 0.0f;
             int nmax = n;
 #pragma unroll
             for (int o = kW; o < 32; o <<= 1) nmax = max(nmax, __shfl_xor_sync(kFullMask, nmax, o));
@@ -468,7 +477,17 @@ k_score_iso_lists(const uint16_t *__restrict__ lists, uint64_t list_total, const
                     e[k] = i < n ? (uint32_t)__ldg(lp + i) : pad;
                 }
 #pragma unroll
-                for (int k = 0; k < 4; ++k) TileFma<T, G>::fma(stile, e[k] >> 2, e[k] & 3u, acc);
+                for (int k = 0; k < 4; ++k) {
+                    float *a = acc;
+                    if constexpr (kSets4) a = acc4[k];
+                    TileFma<T, G>::fma(stile, e[k] >> 2, e[k] & 3u, *reinterpret_cast<float(*)[G]>(a));
+                }
+            }
+            if constexpr (kSets4) {
+                // the 32-lane butterfly's offsets 16 and 8, within the lane
+#pragma unroll
+                for (int j = 0; j < G; ++j)
+                    acc[j] = __fadd_rn(__fadd_rn(acc4[0][j], acc4[2][j]), __fadd_rn(acc4[1][j], acc4[3][j]));
             }
             float sc;
             if constexpr (kC == 1) sc = reduce_scatter<G>(acc);
@@ -711,10 +730,10 @@ int hfx_iso_score(const uint16_t *lists, uint64_t list_total, const uint32_t *ls
                                        num_pep, cap_iso, tiles, stride, mb, me, num_mod, ws, mlo, mhi, mchunk,  \
                                        item_off, n_gm, K, ps, pk, ncand, stats, err, st)
     if (elem_kind == 0) {
-        if (G == 4) HFX_IS(float, 4, 1);
-        if (G == 8) HFX_IS(float, 8, 1);
-        if (G == 2) HFX_IS(float, 2, 1);
-        if (G == 1) HFX_IS(float, 1, 1);
+        if (G == 4) HFX_IS(float, 4, 4);
+        if (G == 8) HFX_IS(float, 8, 4);
+        if (G == 2) HFX_IS(float, 2, 4);
+        if (G == 1) HFX_IS(float, 1, 4);
     } else if (elem_kind == 1) {
         if (G == 8) HFX_IS(__nv_bfloat16, 8, 4);
         if (G == 4) HFX_IS(__nv_bfloat16, 4, 4);

@@ -456,6 +456,9 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
               uint32_t *__restrict__ err) {
     static_assert(kC == 1 || kC == 2 || kC == 4, "1, 2 or 4 candidates per warp");
     constexpr int kW = 32 / kC;  // lanes per candidate
+    // FP32 with several candidates per warp: four partial-sum sets per lane
+    constexpr bool kSets4 = std::is_same<T, float>::value && kC > 1;
+    static_assert(!kSets4 || kW == 8, "the FP32 partial-sum sets assume 8 lanes per candidate");
     static_assert(G <= kW, "a lane group takes up to one spectrum of the group per lane");
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -620,6 +623,16 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
             float acc[G];
 #pragma unroll
             for (int j = 0; j < G; ++j) acc[j] = 0.0f;
+            // FP32 with four candidates per warp keeps the canonical order:
+            // entry i of a list goes to partial sum i % 32, and with 8 lanes
+            // per candidate entry k of each round of 32 is partial 8 k + lane,
+            // so each lane keeps four partial-sum sets and adds them as the
+            // 32-lane butterfly's offsets 16 and 8 do
+            float acc4[kSets4 ? 4 : 1][G];
+#pragma unroll
+            for (int k = 0; k < (kSets4 ? 4 : 1); ++k)
+#pragma unroll
+                for (int j = 0; j < G; ++j) acc4[k][j] = 0.0f;
             const int n = cur.n;
             int nmax = n;
 #pragma unroll
@@ -636,10 +649,14 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const uint32_t bin = e[k] >> 2;
+                    float *a = acc;
+                    if constexpr (kSets4) a = acc4[k];
                     if constexpr (kGlobal) {
-                        if ((int32_t)bin < nb) TileFma<T, G>::fma(tile, bin, e[k] & 3u, acc);
+                        if ((int32_t)bin < nb)
+                            TileFma<T, G>::fma(tile, bin, e[k] & 3u, *reinterpret_cast<float(*)[G]>(a));
                     } else {
-                        TileFma<T, G>::fma(tile, bin, e[k] & 3u, acc);  // zero beyond nb
+                        // zero beyond nb
+                        TileFma<T, G>::fma(tile, bin, e[k] & 3u, *reinterpret_cast<float(*)[G]>(a));
                     }
                 }
                 // lists ascend: once an entry lies beyond the tile, so do the rest
@@ -651,6 +668,12 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
                     const int i = i0 + 8 * kW + kW * k + hl;
                     f[k] = i < n ? (uint32_t)__ldg(cur.lp + i) : pad;
                 }
+            }
+            if constexpr (kSets4) {
+                // offsets 16 (partials l and l + 16, l + 8 and l + 24) and 8
+#pragma unroll
+                for (int j = 0; j < G; ++j)
+                    acc[j] = __fadd_rn(__fadd_rn(acc4[0][j], acc4[2][j]), __fadd_rn(acc4[1][j], acc4[3][j]));
             }
             if constexpr (kC > 1) {
                 const float sc = reduce_scatter_lanes<G, kW>(acc);
@@ -666,6 +689,9 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
                     // member j's sums sit in lanes j * kW / G of candidate q's
                     // group; its admission lane is j * 32 / G
                     const float sc_q = __shfl_sync(kFullMask, sc, q * kW + (lane / (32 / G)) * (kW / G));
+                    // every pair's score, at its member's window offset (E-values)
+                    if (sink && owner && ((act_q >> my_slot) & 1u))
+                        sink[s_off[my_slot] + (p_q - s_wb[my_slot])] = sc_q;
                     const bool want = owner && ((act_q >> my_slot) & 1u) &&
                                       score_order(sc_q) >= *(volatile uint32_t *)(thr_u + my_slot);
                     slots.offer(want, sc_q, p_q, my_slot, K);
@@ -826,7 +852,7 @@ int hfx_lists_score(const void *lists, int long_rows, const uint32_t *lstart, ui
     if (K > kMaxKept || (K > 32 && (elem_kind == 0 || G > 8))) return (int)cudaErrorInvalidValue;
 #define HFX_LL(T, GG, LL)                                                                                      \
     do {                                                                                                       \
-        constexpr int kP = std::is_same<T, float>::value || GG > 8 ? 1 : kLowpCands;                           \
+        constexpr int kP = GG > 8 ? 1 : kLowpCands;                                                            \
         if (long_rows)                                                                                         \
             return launch_lists_t<T, GG, uint32_t, true, kP, LL>((const uint32_t *)lists, lstart, total10,     \
                                                                  list_len, num_pep, stride, wb, we, ws, tiles, \
