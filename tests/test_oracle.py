@@ -285,6 +285,38 @@ def test_score_canonical_order(oracle):
     assert abs(s64 - float((w.astype(np.float64) * x[bins]).sum())) < 1e-9 * max(1, abs(s64)) + 1e-9
 
 
+def test_four_candidates_per_warp_keep_the_canonical_order(oracle):
+    """The FP32 scorers' four-candidates-per-warp form: 8 lanes per candidate,
+    entry k of every round of 32 into the lane's partial set k, the sets
+    added as (s0 + s2) + (s1 + s3) in the lane, then XOR offsets 4, 2, 1
+    within the 8 lanes.  The same float32 additions as the canonical 32
+    partial sums with offsets 16, 8, 4, 2, 1, so the same bits (and the
+    oracle's score)."""
+    rng = np.random.Generator(np.random.PCG64(11))
+    for n in (1, 7, 31, 32, 33, 95, 300, 1001):
+        x = rng.normal(0, 10, 4000).astype(np.float32)
+        bins = np.sort(rng.choice(4000, n, replace=False)).astype(np.uint32)
+        lvl = rng.integers(1, 4, n).astype(np.uint8)
+        w = np.array([0, 10, 25, 50], np.float32)[lvl]
+        prod = lambda i, a: np.float32(np.float64(w[i]) * np.float64(x[bins[i]]) + np.float64(a))
+        # canonical: lane i % 32 of one warp
+        acc = np.zeros(32, np.float32)
+        for i in range(n):
+            acc[i % 32] = prod(i, acc[i % 32])
+        for off in (16, 8, 4, 2, 1):
+            acc = (acc + acc[np.arange(32) ^ off]).astype(np.float32)
+        # four sets per lane, 8 lanes (entry i0 + 8 k + l of round i0 -> set k of lane l)
+        sets = np.zeros((8, 4), np.float32)
+        for i in range(n):
+            sets[i % 8, (i % 32) // 8] = prod(i, sets[i % 8, (i % 32) // 8])
+        lane = ((sets[:, 0] + sets[:, 2]).astype(np.float32) + (sets[:, 1] + sets[:, 3]).astype(np.float32))
+        lane = lane.astype(np.float32)
+        for off in (4, 2, 1):
+            lane = (lane + lane[np.arange(8) ^ off]).astype(np.float32)
+        assert lane[0].view(np.uint32) == acc[0].view(np.uint32), n
+        assert np.float32(oracle.score32(bins, lvl, x)).view(np.uint32) == lane[0].view(np.uint32), n
+
+
 def test_ion_charges(oracle):
     # Search.hs:182 round (max 1 (z-1)); plain kernel 1..4 only
     assert [oracle.ion_charges(z) for z in (1, 2, 3, 4, 5, 6)] == [1, 1, 2, 3, 4, 0]
