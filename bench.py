@@ -67,17 +67,17 @@ KERNEL_SRC = {
 # per-kernel basis below) to the small case's.
 TRAFFIC = {
     ("k_gen_lists", "full", 1, 10000): {
-        "src": "b1c26e9ec340", "bytes": 2207584533, "inst": 4522799000,
+        "src": "e21879438706", "bytes": 2208082467, "inst": 4522799000,
         "profile": "profiles/k_gen_lists_2k_bf16.md (2,000-spectrum capture x 1.729 moved-bytes ratio)"},
     ("k_score_lists", "full", 1, 10000): {
-        "src": "b1c26e9ec340", "bytes": 3323255988, "inst": 2310098000,
+        "src": "e21879438706", "bytes": 3319044367, "inst": 2309915000,
         "profile": "profiles/k_score_lists_2k_bf16.md (2,000-spectrum capture x 2.481 moved-bytes ratio)"},
     ("k_gen_iso_lists", "mods", 1, 10000): {
-        "src": "1615297cc087", "bytes": 50189462418, "inst": 91095400000,
+        "src": "e854838a6ae5", "bytes": 50176551169, "inst": 91095407000,
         "profile": "profiles/iso_lists_mods1k_bf16.md (1,000-spectrum capture x 3.904 moved-bytes ratio)"},
     ("k_score_iso_lists", "mods", 1, 10000): {
-        "src": "1615297cc087", "bytes": 62845138690, "inst": 31132060000,
-        "profile": "profiles/iso_lists_mods1k_bf16.md (1,000-spectrum capture x 4.816 moved-bytes ratio)"},
+        "src": "e854838a6ae5", "bytes": 62817937073, "inst": 31114669000,
+        "profile": "profiles/iso_lists_mods1k_bf16.md (1,000-spectrum capture x 4.815 moved-bytes ratio)"},
 }
 
 

@@ -689,9 +689,12 @@ k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, 
                     // member j's sums sit in lanes j * kW / G of candidate q's
                     // group; its admission lane is j * 32 / G
                     const float sc_q = __shfl_sync(kFullMask, sc, q * kW + (lane / (32 / G)) * (kW / G));
-                    // every pair's score, at its member's window offset (E-values)
-                    if (sink && owner && ((act_q >> my_slot) & 1u))
-                        sink[s_off[my_slot] + (p_q - s_wb[my_slot])] = sc_q;
+                    // every pair's score, at its member's window offset
+                    // (E-values; FP32 only, the host refuses a sink otherwise)
+                    if constexpr (std::is_same<T, float>::value) {
+                        if (sink && owner && ((act_q >> my_slot) & 1u))
+                            sink[s_off[my_slot] + (p_q - s_wb[my_slot])] = sc_q;
+                    }
                     const bool want = owner && ((act_q >> my_slot) & 1u) &&
                                       score_order(sc_q) >= *(volatile uint32_t *)(thr_u + my_slot);
                     slots.offer(want, sc_q, p_q, my_slot, K);
