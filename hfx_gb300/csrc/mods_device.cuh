@@ -170,48 +170,11 @@ struct ModIsoform {
     }
 };
 
-// The residues of [tc, tn) that an isoform modifies, one bit per residue:
-// bits[c] bit l is residue tc + 32 c + l.  The same decision as
-// ModIsoform::chunk_add, made once per isoform instead of once per ion
-// charge; `bits` holds ceil((tn - tc) / 32) words (per-warp shared memory).
-__device__ __forceinline__ void isoform_positions(const uint8_t *__restrict__ ions, uint32_t tc, uint32_t tn,
-                                                  const uint64_t (&mask)[kMaxMa], int num_ma, int per_type,
-                                                  uint32_t *bits) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t lt = (1u << lane) - 1u;
-    uint32_t seen_any = 0u, seen[kMaxMa];
-#pragma unroll
-    for (int i = 0; i < kMaxMa; ++i) seen[i] = 0u;
-    uint32_t c = 0;
-    for (uint32_t base = tc; base < tn; base += 32, ++c) {
-        const bool valid = base + lane < tn;
-        const uint32_t t = valid ? ((uint32_t)__ldg(ions + base + lane) >> 5) & 7u : 0u;
-        const uint32_t any = __ballot_sync(kFullMask, t != 0u);
-        uint32_t k = seen_any + __popc(any & lt);
-        seen_any += __popc(any);
-        uint32_t mytype_seen = 0;
-        uint64_t m = 0ull;
-#pragma unroll
-        for (int i = 0; i < kMaxMa; ++i) {
-            if (i >= num_ma) continue;
-            const uint32_t bi = __ballot_sync(kFullMask, t == (uint32_t)(i + 1));
-            if (t == (uint32_t)(i + 1)) {
-                mytype_seen = seen[i] + __popc(bi & lt);
-                m = mask[i];
-            }
-            seen[i] += __popc(bi);
-        }
-        if (per_type) k = mytype_seen;
-        const bool modded = t != 0u && (int)t <= num_ma && k < 64u && ((m >> k) & 1ull);
-        const uint32_t b = __ballot_sync(kFullMask, modded);
-        if (lane == 0) bits[c] = b;
-    }
-    __syncwarp();
-}
-
-// Residue-mass hook for build_planes over the positions of
-// isoform_positions: lane i of ma_lane holds acid i+1's modification mass.
-// Passed by value, so every build starts at the first 32-residue chunk.
+// Residue-mass hook for build_planes over an isoform's modified residues
+// (one bit per residue in 32-residue words, as k_iso_positions writes them;
+// the same decision as ModIsoform::chunk_add): lane i of ma_lane holds acid
+// i+1's modification mass.  Passed by value, so every build starts at the
+// first 32-residue chunk.
 struct ModPositions {
     const uint32_t *bits;
     float ma_lane;
