@@ -73,10 +73,10 @@ TRAFFIC = {
         "src": "e21879438706", "bytes": 3319044367, "inst": 2309915000,
         "profile": "profiles/k_score_lists_2k_bf16.md (2,000-spectrum capture x 2.481 moved-bytes ratio)"},
     ("k_gen_iso_lists", "mods", 1, 10000): {
-        "src": "e854838a6ae5", "bytes": 50176551169, "inst": 91095407000,
+        "src": "87f5f4694558", "bytes": 50181657886, "inst": 91095407000,
         "profile": "profiles/iso_lists_mods1k_bf16.md (1,000-spectrum capture x 3.904 moved-bytes ratio)"},
     ("k_score_iso_lists", "mods", 1, 10000): {
-        "src": "e854838a6ae5", "bytes": 62817937073, "inst": 31114669000,
+        "src": "87f5f4694558", "bytes": 62823028595, "inst": 31125280000,
         "profile": "profiles/iso_lists_mods1k_bf16.md (1,000-spectrum capture x 4.815 moved-bytes ratio)"},
 }
 
@@ -111,7 +111,8 @@ def _args():
                     help="N > 1: split ONE batch across the ranks by candidate counts (strong scaling) instead of "
                          "one batch per rank (weak scaling)")
     ap.add_argument("--tune", default="auto", choices=["auto", "on", "off"],
-                    help="hfx_autotune of group size and work-item size before the warm-up (auto: 'full' only)")
+                    help="hfx_autotune of group size and work-item size before the warm-up (auto = on "
+                         "unless --group-size or --chunk is given)")
     return ap.parse_args()
 
 
@@ -458,8 +459,7 @@ def main():
     out = outputs()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=d)
     tuned = None
-    if mode != 0 and a.group_size == 0 and a.chunk == 0 and (
-            a.tune == "on" or (a.tune == "auto" and a.workload in ("full", "tiny"))):
+    if mode != 0 and a.group_size == 0 and a.chunk == 0 and a.tune in ("on", "auto"):
         ms_t = eng.autotune(dev, p, out, reps=2)
         p_prof.group_size, p_prof.chunk = p.group_size, p.chunk
         tuned = {"group_size": p.group_size, "chunk": p.chunk, "ms": ms_t}
