@@ -244,8 +244,9 @@ __device__ __forceinline__ void emit_keys(float b, float y, const ChargeConst &k
     out[9] = key(bin_w<FastDiv>(__fsub_rn(m, k.dnh3), ibw), 1u);
 }
 
-// Warp-wide ascending bitonic sort of n2 (a power of two) keys in shared memory.
-__device__ __forceinline__ void warp_bitonic_sort(uint32_t *kb, int32_t n2) {
+// Warp-wide bitonic sort of n2 (a power of two) keys in shared memory,
+// ascending (or descending).
+__device__ __forceinline__ void warp_bitonic_sort(uint32_t *kb, int32_t n2, bool descending = false) {
     const int lane = threadIdx.x & 31;
     for (int32_t kk = 2; kk <= n2; kk <<= 1) {
         for (int32_t j = kk >> 1; j > 0; j >>= 1) {
@@ -253,7 +254,7 @@ __device__ __forceinline__ void warp_bitonic_sort(uint32_t *kb, int32_t n2) {
                 const int32_t l = i ^ j;
                 if (l > i) {
                     const uint32_t a = kb[i], b = kb[l];
-                    if ((a > b) == ((i & kk) == 0)) {
+                    if ((a > b) == (((i & kk) == 0) != descending)) {
                         kb[i] = b;
                         kb[l] = a;
                     }
@@ -262,6 +263,48 @@ __device__ __forceinline__ void warp_bitonic_sort(uint32_t *kb, int32_t n2) {
             __syncwarp();
         }
     }
+}
+
+// Ascending bitonic merge of n2 keys whose first half ascends and second
+// half descends.
+__device__ __forceinline__ void warp_bitonic_merge(uint32_t *kb, int32_t n2) {
+    const int lane = threadIdx.x & 31;
+    for (int32_t j = n2 >> 1; j > 0; j >>= 1) {
+        for (int32_t i = lane; i < n2; i += 32) {
+            const int32_t l = i ^ j;
+            if (l > i) {
+                const uint32_t a = kb[i], b = kb[l];
+                if (a > b) {
+                    kb[i] = b;
+                    kb[l] = a;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Keeps the last key of each bin (its highest level) of the ascending keys
+// kb[0, n2), packed in order at kb[0, n) (in place: a round reads its keys
+// before it writes, and writes only at or below them), and, when out is
+// given, at out[0, min(n, cap)).  Returns n.
+__device__ __forceinline__ int32_t warp_keep_highest(uint32_t *kb, int32_t n2, uint32_t *out, int32_t cap) {
+    const int lane = threadIdx.x & 31;
+    int32_t n = 0;
+    for (int32_t i0 = 0; i0 < n2; i0 += 32) {
+        const int32_t i = i0 + lane;
+        const uint32_t k = i < n2 ? kb[i] : 0xFFFFFFFFu;
+        const bool keep = k != 0xFFFFFFFFu && (i + 1 >= n2 || (kb[i + 1] >> 2) != (k >> 2));
+        const uint32_t bal = __ballot_sync(kFullMask, keep);
+        const int32_t at = n + __popc(bal & ((1u << lane) - 1u));
+        if (keep) {
+            kb[at] = k;
+            if (out && at < cap) out[at] = k;
+        }
+        n += __popc(bal);
+    }
+    __syncwarp();
+    return n;
 }
 
 template <bool FastDiv>
@@ -297,6 +340,68 @@ __global__ void __launch_bounds__(256) k_gen_lists_long(DevDB db, const int32_t 
         if (tn < tc || nmax > (uint32_t)kLongKeys) {
             if (lane == 0) atomicOr(err, kErrTooLong);
             if (lane < kLevels && ((need >> lane) & 1u)) list_len[(size_t)lane * db.num_pep + p] = 0;
+            continue;
+        }
+        // Incremental levels where they fit: the level-z list is the
+        // level-(z-1) list (ascending, in the lower half) merged with the
+        // sorted charge-z keys (descending, in the upper half) by one bitonic
+        // merge, then reduced to each bin's highest level -- the same list as
+        // sorting every charge <= z at once, with a tenth of the
+        // compare-exchanges.  A peptide whose lists outgrow half the buffer
+        // takes the full sort below.
+        const int32_t nk = 10 * (int32_t)(tn - tc);  // keys of one charge
+        int32_t hmax = 32;
+        while (hmax < max(nk, nk * (zmax - 1))) hmax <<= 1;
+        if (2 * hmax <= kLongKeys) {
+            int32_t n_prev = 0;
+            for (int z = 1; z <= zmax; ++z) {
+                int32_t h = 32;
+                while (h < max(nk, n_prev)) h <<= 1;
+                const int32_t lo = z == 1 ? 0 : h;  // where the charge-z keys go
+                const int32_t n2 = z == 1 ? h : 2 * h;
+                for (int32_t i = n_prev + lane; i < n2; i += 32) kb[i] = 0xFFFFFFFFu;
+                __syncwarp();
+                float carry = 0.0f;
+                for (uint32_t ci = 0; ci < nchunk; ++ci) {
+                    const uint32_t base = tc + 32u * ci;
+                    const int cnt = (int)min(32u, tn - base);
+                    uint32_t byte = 0;
+                    if (lane < cnt) byte = __ldg(db.ions + base + lane);
+                    float v = residue_mass(mt_lane, byte);
+                    if (lane >= cnt) v = 0.0f;
+                    if (lane == 0) v = __fadd_rn(v, carry);
+#pragma unroll
+                    for (int d = 1; d < 32; d <<= 1) {
+                        const float u = __shfl_up_sync(kFullMask, v, d);
+                        if (lane >= d) v = __fadd_rn(v, u);
+                    }
+                    carry = __shfl_sync(kFullMask, v, cnt - 1);
+                    if (lane < cnt)
+                        emit_keys<FastDiv>(v, __fsub_rn(r, v), charge_const<FastDiv>(z), nbins, ibw,
+                                           kb + lo + (size_t)(32u * ci + (uint32_t)lane) * 10);
+                }
+                __syncwarp();
+                if (z == 1) {
+                    warp_bitonic_sort(kb, n2);
+                } else {
+                    warp_bitonic_sort(kb + h, h, true);
+                    warp_bitonic_merge(kb, n2);
+                }
+                const bool needed = (need >> (z - 1)) & 1u;
+                const int32_t slot = 10 * z * (int32_t)(tn - tc);
+                int32_t n = warp_keep_highest(kb, n2, needed ? lists + list_offset(lstart, total10, z, p) : nullptr,
+                                              slot);
+                n_prev = n;
+                if (!needed) continue;
+                if (n > slot) {
+                    if (lane == 0) atomicOr(err, kErrListOverflow);
+                    n = slot;
+                }
+                if (lane == 0) list_len[(size_t)(z - 1) * db.num_pep + p] = (uint16_t)min(n, 65535);
+                my_lists += 1u;
+                my_entries += (uint32_t)n;
+                __syncwarp();
+            }
             continue;
         }
         for (int z = 1; z <= zmax; ++z) {
