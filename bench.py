@@ -67,10 +67,10 @@ KERNEL_SRC = {
 # per-kernel basis below) to the small case's.
 TRAFFIC = {
     ("k_gen_lists", "full", 1, 10000): {
-        "src": "e21879438706", "bytes": 2208082467, "inst": 4522799000,
+        "src": "50d9930d1446", "bytes": 2206019845, "inst": 4522799000,
         "profile": "profiles/k_gen_lists_2k_bf16.md (2,000-spectrum capture x 1.729 moved-bytes ratio)"},
     ("k_score_lists", "full", 1, 10000): {
-        "src": "e21879438706", "bytes": 3319044367, "inst": 2309915000,
+        "src": "50d9930d1446", "bytes": 3321900459, "inst": 2309930000,
         "profile": "profiles/k_score_lists_2k_bf16.md (2,000-spectrum capture x 2.481 moved-bytes ratio)"},
     ("k_gen_iso_lists", "mods", 1, 10000): {
         "src": "87f5f4694558", "bytes": 50181657886, "inst": 91095407000,
