@@ -192,7 +192,12 @@ int32_t hfx_search_device(hfx_ctx *ctx, const hfx_search_params *p, const float 
  * (bin centre / 10000, log10(count / bin_width)) gives alpha and beta, and a
  * result of score s gets 10 ** (alpha + beta * s / 10000).  out_ev [nspec]
  * [top_n] (NaN for empty slots), out_fit [nspec][3] = alpha, beta, histogram
- * points.  The reference's defaults are bin_width 350 and cutoff_perc 3. */
+ * points.  The reference's defaults are bin_width 350 and cutoff_perc 3.
+ * Without modifications the search runs as one FP32 pass over the step's
+ * ion lists whatever p->precision asks (its top-N equals the BF16/FP16
+ * search rescored in FP32; group_size is chosen for FP32); with
+ * modifications the requested search runs first and a second FP32 pass
+ * scores every pair. */
 int32_t hfx_search_evalues(hfx_ctx *ctx, const hfx_search_params *p, const float *mz, const float *it,
                            const int64_t *off, const float *pcr, const float *z, const float *tol, int32_t nspec,
                            int32_t bin_width, float cutoff_perc, float *out_score, uint64_t *out_key,
