@@ -67,16 +67,16 @@ KERNEL_SRC = {
 # per-kernel basis below) to the small case's.
 TRAFFIC = {
     ("k_gen_lists", "full", 1, 10000): {
-        "src": "50d9930d1446", "bytes": 2206019845, "inst": 4522799000,
+        "src": "577a09613aeb", "bytes": 2206019845, "inst": 4522799000,
         "profile": "profiles/k_gen_lists_2k_bf16.md (2,000-spectrum capture x 1.729 moved-bytes ratio)"},
     ("k_score_lists", "full", 1, 10000): {
-        "src": "50d9930d1446", "bytes": 3321900459, "inst": 2309930000,
+        "src": "577a09613aeb", "bytes": 3321900459, "inst": 2309930000,
         "profile": "profiles/k_score_lists_2k_bf16.md (2,000-spectrum capture x 2.481 moved-bytes ratio)"},
     ("k_gen_iso_lists", "mods", 1, 10000): {
-        "src": "87f5f4694558", "bytes": 50181657886, "inst": 91095407000,
+        "src": "b9b44833cf01", "bytes": 50181657886, "inst": 91095407000,
         "profile": "profiles/iso_lists_mods1k_bf16.md (1,000-spectrum capture x 3.904 moved-bytes ratio)"},
     ("k_score_iso_lists", "mods", 1, 10000): {
-        "src": "87f5f4694558", "bytes": 62823028595, "inst": 31125280000,
+        "src": "b9b44833cf01", "bytes": 62823028595, "inst": 31125280000,
         "profile": "profiles/iso_lists_mods1k_bf16.md (1,000-spectrum capture x 4.815 moved-bytes ratio)"},
 }
 
@@ -117,12 +117,18 @@ def _args():
 
 
 def _src_hash(kern):
+    """Hash of a kernel's source files without their comments and runs of
+    whitespace, so that only a change of code marks a capture stale."""
     import hashlib
+    import re
     files = KERNEL_SRC.get(kern, ["hfx_gb300/csrc/lists.cu"] + _COMMON_SRC)
     h = hashlib.sha1()
     for f in files:
-        with open(os.path.join(ROOT, f), "rb") as fh:
-            h.update(fh.read())
+        with open(os.path.join(ROOT, f), encoding="utf-8") as fh:
+            text = fh.read()
+        text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)  # block comments
+        text = re.sub(r"//[^\n]*", " ", text)                 # line comments
+        h.update(" ".join(text.split()).encode())
     return h.hexdigest()[:12]
 
 

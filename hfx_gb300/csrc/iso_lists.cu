@@ -17,11 +17,12 @@
 //      scans give every isoform a global index and every slot an offset;
 //   3. one record per isoform: its ordering key (combination, position,
 //      rank; Search.hs:119-123) and its slot;
-//   4. one warp per isoform: unrank the modified residues
-//      (gen_mod_pep.cu:127-227, combinatorics.h:90-134), build the bit
-//      planes of charges 1..zmax with the modified masses (residual + delta,
-//      residue mass + acid delta) and write the distinct-bin list of every
-//      needed level (the list format of lists.cu);
+//   4. one thread per isoform: unrank the modified residues
+//      (gen_mod_pep.cu:127-227, combinatorics.h:90-134) into a bit per
+//      residue; then one warp per isoform: build the bit planes of charges
+//      1..zmax with the modified masses (residual + delta, residue mass +
+//      acid delta) and write the distinct-bin list of every needed level
+//      (the list format of lists.cu);
 //   5. the scorer: work items (spectrum group, combination, chunk of
 //      positions) as in the fused path; an item's isoforms are a contiguous
 //      index range; each is streamed against the group's tile.
@@ -328,7 +329,7 @@ __global__ void __launch_bounds__(256) k_gen_iso_lists(DevDB db, DevMods mods, c
 // (group, combination, chunk of positions); the group's tile is staged by
 // one bulk copy; an item's isoforms are [index(mu, p0), index(mu, p1)); kC
 // isoforms per warp (32 / kC lanes each, entry i of a list by lane i % (32 /
-// kC)); FP32 tiles take one isoform per warp, the canonical order.
+// kC)); in FP32 each lane keeps four partial-sum sets, the canonical order.
 template <typename T, int G, int kC>
 __global__ void __launch_bounds__(512, 1)
 k_score_iso_lists(const uint16_t *__restrict__ lists, uint64_t list_total, const uint32_t *__restrict__ lstart,
