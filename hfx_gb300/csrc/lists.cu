@@ -545,9 +545,11 @@ __global__ void __launch_bounds__(256) k_rescore_lists(const E *__restrict__ lis
 // kC: candidates per warp (1, 2 or 4), one per group of 32 / kC lanes (entry
 // i of a list by lane i % (32 / kC) of its group).  The per-candidate work
 // around the list -- the claim, the reduction, the admission -- is then
-// shared by kC candidates.  It changes the order of the sums, so kC > 1
-// serves the BF16/FP16 pass only, whose scores pick the candidates that FP32
-// rescoring orders; FP32 scoring keeps the canonical order (kC = 1).
+// shared by kC candidates.  In FP32 with four candidates each lane keeps four
+// partial-sum sets (entry k of every round of 32 in set k) and adds them as
+// the 32-lane butterfly would, so the sums keep the canonical order; the
+// BF16/FP16 pass sums in one set (its scores only pick the candidates that
+// FP32 rescoring orders).
 template <typename T, int G, typename E, bool kGlobal, int kC, int L>
 __global__ void __launch_bounds__(1024, 1)
 k_score_lists(const E *__restrict__ lists, const uint32_t *__restrict__ lstart, uint64_t total10,
@@ -890,7 +892,7 @@ int hfx_lists_generate(const DevDB &db, const int32_t *cover, int64_t npep1, int
     return (int)cudaGetLastError();
 }
 
-// Candidates per warp in the BF16/FP16 pass (groups of up to 8 spectra).
+// Candidates per warp with groups of up to 8 spectra (FP32 and BF16/FP16).
 constexpr int kLowpCands = 4;
 
 // Warps per list-scorer CTA: 16 (two CTAs per SM) up to 8 spectra per
@@ -952,11 +954,11 @@ int hfx_lists_score(const void *lists, int long_rows, const uint32_t *lstart, ui
                     const uint32_t *we, const BatchedWs &ws, void *tiles, int32_t G, int32_t K, int nw,
                     float *part_s, uint64_t *part_k, unsigned long long *stats, uint32_t *err, cudaStream_t st,
                     float *sink, const uint64_t *sink_off) {
-    // BF16/FP16 groups of up to 8 spectra score two candidates per warp
-    // (their scores only choose what FP32 rescoring orders); FP32 scoring,
-    // with or without a sink, keeps the canonical order
+    // groups of up to 8 spectra score four candidates per warp (FP32 in the
+    // canonical order, with or without a sink; BF16/FP16 scores only choose
+    // what FP32 rescoring orders)
     if (elem_kind != 0 && sink) return (int)cudaErrorInvalidValue;
-    // up to 64 kept candidates per member in the BF16/FP16 two-per-warp pass
+    // up to 64 kept candidates per member in the BF16/FP16 pass
     if (K > kMaxKept || (K > 32 && (elem_kind == 0 || G > 8))) return (int)cudaErrorInvalidValue;
 #define HFX_LL(T, GG, LL)                                                                                      \
     do {                                                                                                       \
