@@ -67,11 +67,11 @@ KERNEL_SRC = {
 # per-kernel basis below) to the small case's.
 TRAFFIC = {
     ("k_gen_lists", "full", 1, 10000): {
-        "src": "577a09613aeb", "bytes": 2206019845, "inst": 4522799000,
+        "src": "514a0af75598", "bytes": 2205793354, "inst": 4522799000,
         "profile": "profiles/k_gen_lists_2k_bf16.md (2,000-spectrum capture x 1.729 moved-bytes ratio)"},
     ("k_score_lists", "full", 1, 10000): {
-        "src": "577a09613aeb", "bytes": 3321900459, "inst": 2309930000,
-        "profile": "profiles/k_score_lists_2k_bf16.md (2,000-spectrum capture x 2.481 moved-bytes ratio)"},
+        "src": "514a0af75598", "bytes": 3319129096, "inst": 2310847000,
+        "profile": "profiles/k_score_lists_2k_bf16.md (2,000-spectrum capture x 2.482 moved-bytes ratio)"},
     ("k_gen_iso_lists", "mods", 1, 10000): {
         "src": "b9b44833cf01", "bytes": 50181657886, "inst": 91095407000,
         "profile": "profiles/iso_lists_mods1k_bf16.md (1,000-spectrum capture x 3.904 moved-bytes ratio)"},

@@ -504,10 +504,22 @@ __global__ void __launch_bounds__(256) k_rescore_lists(const E *__restrict__ lis
                 const uint32_t p = (uint32_t)kk;
                 const int n = list_len[(size_t)(z - 1) * num_pep + p];
                 const E *lp = lists + list_offset(lstart, total10, z, p);
-                for (int i = lane; i < n; i += 32) {
-                    const uint32_t e = (uint32_t)__ldg(lp + i);
-                    const uint32_t bin = e >> 2;
-                    if ((int32_t)bin < m.len) acc = __fmaf_rn(level_weight(e & 3u), __ldg(row + bin), acc);
+                // four entries per lane in flight, then their row values,
+                // then the sums in the lane's ascending entry order
+                for (int i0 = lane; i0 < n; i0 += 128) {
+                    uint32_t e[4];
+                    float x[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) e[k] = i0 + 32 * k < n ? (uint32_t)__ldg(lp + i0 + 32 * k) : ~0u;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const uint32_t bin = e[k] >> 2;
+                        x[k] = (i0 + 32 * k < n && (int32_t)bin < m.len) ? __ldg(row + bin) : 0.0f;
+                    }
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (i0 + 32 * k < n && (int32_t)(e[k] >> 2) < m.len)
+                            acc = __fmaf_rn(level_weight(e[k] & 3u), x[k], acc);
                 }
             } else if (kk >> 63) {
                 if (lane == 0) atomicOr(err, kErrBounds);
