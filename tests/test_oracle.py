@@ -317,6 +317,32 @@ def test_four_candidates_per_warp_keep_the_canonical_order(oracle):
         assert np.float32(oracle.score32(bins, lvl, x)).view(np.uint32) == lane[0].view(np.uint32), n
 
 
+def test_incremental_level_lists_equal_the_full_sort():
+    """The long-row list generator's level recurrence: the level-z list is
+    the level-(z-1) list merged with the charge-z keys (bin << 2 | level),
+    each bin keeping its highest level -- the same list as sorting the keys
+    of every charge <= z at once and keeping each bin's last key."""
+    rng = np.random.Generator(np.random.PCG64(13))
+
+    def keep_highest(keys):
+        keys = np.sort(keys)
+        last = np.ones(len(keys), bool)
+        last[:-1] = (keys[1:] >> 2) != (keys[:-1] >> 2)
+        return keys[last]
+
+    for _ in range(200):
+        nk = int(rng.integers(1, 400))
+        span = int(rng.integers(50, 5000))
+        charges = [(rng.integers(0, span, nk).astype(np.uint32) << 2) | rng.integers(1, 4, nk).astype(np.uint32)
+                   for _ in range(4)]
+        prev = np.zeros(0, np.uint32)
+        for z in range(1, 5):
+            inc = keep_highest(np.concatenate([prev, charges[z - 1]]))
+            full = keep_highest(np.concatenate(charges[:z]))
+            assert np.array_equal(inc, full), (nk, span, z)
+            prev = inc
+
+
 def test_ion_charges(oracle):
     # Search.hs:182 round (max 1 (z-1)); plain kernel 1..4 only
     assert [oracle.ion_charges(z) for z in (1, 2, 3, 4, 5, 6)] == [1, 1, 2, 3, 4, 0]
